@@ -1,0 +1,95 @@
+"""Build libflctgpu.so (the C-ABI library) in-tree with nvcc for sm_103a.
+
+    python -m pyflct_gb300.build [--force] [--jobs N]
+
+Every .cu under csrc/ is compiled to an object in parallel
+(-gencode arch=compute_103a,code=sm_103a), then linked into
+pyflct_gb300/libflctgpu.so with the static CUDA runtime.  Objects go to
+pyflct_gb300/_build/ (git-ignored); a source is recompiled only when it or a
+header changed.
+"""
+from __future__ import annotations
+
+import argparse
+import concurrent.futures as cf
+import glob
+import os
+import shutil
+import subprocess
+import sys
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+BUILD = os.path.join(PKG, "_build")
+LIB = os.path.join(PKG, "libflctgpu.so")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVFLAGS = ["-std=c++20", "-O3", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
+           "-Xcompiler", "-fvisibility=hidden", "-I", CSRC, "-I", os.path.join(ROOT, "include")]
+
+
+def nvcc() -> str:
+    for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libflctgpu.so")
+
+
+def _stale(obj: str, src: str, headers: list[str]) -> bool:
+    if not os.path.exists(obj):
+        return True
+    t = os.path.getmtime(obj)
+    return any(os.path.getmtime(p) > t for p in [src] + headers)
+
+
+def build(force: bool = False, jobs: int | None = None, verbose: bool = False) -> str:
+    os.makedirs(BUILD, exist_ok=True)
+    srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    headers = sorted(glob.glob(os.path.join(CSRC, "*.cuh")) +
+                     glob.glob(os.path.join(ROOT, "include", "*.h")))
+    cc = nvcc()
+    todo = []
+    objs = []
+    for s in srcs:
+        o = os.path.join(BUILD, os.path.basename(s)[:-3] + ".o")
+        objs.append(o)
+        if force or _stale(o, s, headers):
+            todo.append((s, o))
+
+    def run(so):
+        s, o = so
+        cmd = [cc] + ARCH + NVFLAGS + ["-c", s, "-o", o]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed on {os.path.basename(s)}:\n{r.stderr}")
+        if verbose and r.stderr.strip():
+            print(r.stderr)
+        return s
+
+    if todo:
+        jobs = jobs or min(len(todo), os.cpu_count() or 4)
+        with cf.ThreadPoolExecutor(jobs) as ex:
+            for s in ex.map(run, todo):
+                if verbose:
+                    print("compiled", os.path.basename(s))
+    if todo or force or not os.path.exists(LIB):
+        tmp = LIB + ".tmp"
+        cmd = [cc] + ARCH + ["-shared", "-cudart", "static", "-o", tmp] + objs + ["-lpthread"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("link failed:\n" + r.stderr)
+        os.replace(tmp, LIB)
+    return LIB
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--force", action="store_true")
+    ap.add_argument("--jobs", type=int, default=None)
+    ap.add_argument("-v", "--verbose", action="store_true")
+    a = ap.parse_args(argv)
+    print(build(a.force, a.jobs, a.verbose))
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,219 @@
+// fft_reg.cuh -- register-resident mixed-radix FFT for one thread.
+//
+// A length-L complex transform of an array held in a thread's registers,
+// fully unrolled at compile time: decimation in frequency, L = R * M with
+// R in {4, 2, 3, 5, 7, ...} (a prime R > 5 uses a direct R-point DFT), so
+// every box size the sliding window can take (n = 2*nsize, a multiple of 4)
+// has a kernel.  Output frequency k lands in register dif_pos<L>(k); every
+// index is a compile-time constant, so the permutation costs nothing.
+//
+// Twiddles are compile-time constants: the angle 2*pi*k/L is reduced exactly
+// with integer arithmetic to the first octant and evaluated by a Taylor
+// series in double inside constexpr functions (written for this project),
+// then rounded once to float.
+#pragma once
+#include <cuda_runtime.h>
+#include <type_traits>
+
+#define FLCT_HD __host__ __device__ __forceinline__
+
+namespace flct {
+
+// ------------------------------------------------ compile-time helpers --
+
+template <int B, int E, class F>
+FLCT_HD void sfor(F&& f) {
+    if constexpr (B < E) {
+        f(std::integral_constant<int, B>{});
+        sfor<B + 1, E>(f);
+    }
+}
+
+constexpr double kPi = 3.14159265358979323846264338327950288;
+
+constexpr double taylor_sin(double y) {
+    double term = y, sum = y, y2 = y * y;
+    for (int k = 1; k < 14; ++k) {
+        term *= -y2 / ((2.0 * k) * (2.0 * k + 1.0));
+        sum += term;
+    }
+    return sum;
+}
+
+constexpr double taylor_cos(double y) {
+    double term = 1.0, sum = 1.0, y2 = y * y;
+    for (int k = 1; k < 14; ++k) {
+        term *= -y2 / ((2.0 * k - 1.0) * (2.0 * k));
+        sum += term;
+    }
+    return sum;
+}
+
+// cos and sin of 2*pi*num/den, with the angle reduced exactly to
+// [-pi/4, pi/4] plus a whole number of quarter turns.
+struct CS {
+    double c, s;
+};
+constexpr CS ct_cossin(long num, long den) {
+    long r = ((num % den) + den) % den;            // [0, den)
+    long q = (8 * r + den) / (2 * den);            // nearest quarter turn, 0..4
+    long rem = 4 * r - q * den;                    // angle = 2pi*(q/4 + rem/(4den))
+    double y = 2.0 * kPi * (double)rem / (4.0 * (double)den);
+    double c = taylor_cos(y), s = taylor_sin(y);
+    switch (q % 4) {
+        case 0: return {c, s};
+        case 1: return {-s, c};
+        case 2: return {-c, -s};
+        default: return {s, -c};
+    }
+}
+
+template <int L>
+constexpr int radix_of() {
+    if constexpr (L % 4 == 0) return 4;
+    else if constexpr (L % 2 == 0) return 2;
+    else if constexpr (L % 3 == 0) return 3;
+    else if constexpr (L % 5 == 0) return 5;
+    else if constexpr (L % 7 == 0) return 7;
+    else if constexpr (L % 11 == 0) return 11;
+    else if constexpr (L % 13 == 0) return 13;
+    else return L;
+}
+
+// Register position of output frequency k after dif<L>.
+template <int L>
+constexpr int dif_pos(int k) {
+    if constexpr (L == 1) {
+        return 0;
+    } else {
+        constexpr int R = radix_of<L>(), M = L / R;
+        return M * (k % R) + dif_pos<M>(k / R);
+    }
+}
+
+// ------------------------------------------------------ complex helpers --
+
+FLCT_HD float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+FLCT_HD float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// multiply by DIR*i
+template <int DIR>
+FLCT_HD float2 mul_i(float2 a) {
+    if constexpr (DIR < 0) return make_float2(a.y, -a.x);
+    else return make_float2(-a.y, a.x);
+}
+
+// a * exp(DIR * 2*pi*i * NUM/DEN), specialised for the exact cases.
+template <int DIR, long NUM, long DEN>
+FLCT_HD float2 twmul(float2 a) {
+    constexpr long r = ((NUM % DEN) + DEN) % DEN;
+    if constexpr (r == 0) {
+        return a;
+    } else if constexpr (4 * r == DEN) {
+        return mul_i<DIR>(a);
+    } else if constexpr (2 * r == DEN) {
+        return make_float2(-a.x, -a.y);
+    } else if constexpr (4 * r == 3 * DEN) {
+        return mul_i<-DIR>(a);
+    } else if constexpr (8 * r == DEN || 8 * r == 3 * DEN || 8 * r == 5 * DEN || 8 * r == 7 * DEN) {
+        constexpr CS w = ct_cossin(r, DEN);
+        constexpr float c = (float)w.c, s = (float)(DIR * w.s);
+        // |c| == |s| at odd multiples of pi/4
+        constexpr float h = c;
+        if constexpr ((c > 0) == (s > 0)) {
+            return make_float2(h * (a.x - a.y), h * (a.x + a.y));
+        } else {
+            return make_float2(h * (a.x + a.y), h * (a.y - a.x));
+        }
+    } else {
+        constexpr CS w = ct_cossin(r, DEN);
+        constexpr float c = (float)w.c, s = (float)(DIR * w.s);
+        return make_float2(a.x * c - a.y * s, a.x * s + a.y * c);
+    }
+}
+
+// ----------------------------------------------------------- butterflies --
+
+template <int R, int DIR>
+FLCT_HD void small_dft(float2* t) {
+    if constexpr (R == 2) {
+        float2 a = t[0], b = t[1];
+        t[0] = cadd(a, b);
+        t[1] = csub(a, b);
+    } else if constexpr (R == 4) {
+        float2 s0 = cadd(t[0], t[2]), s1 = csub(t[0], t[2]);
+        float2 s2 = cadd(t[1], t[3]), s3 = mul_i<DIR>(csub(t[1], t[3]));
+        t[0] = cadd(s0, s2);
+        t[2] = csub(s0, s2);
+        t[1] = cadd(s1, s3);
+        t[3] = csub(s1, s3);
+    } else if constexpr (R == 3) {
+        constexpr float h = 0.866025403784438646763723170752936183f;
+        float2 p = cadd(t[1], t[2]), m = csub(t[1], t[2]);
+        float2 a = t[0];
+        float2 u = make_float2(a.x - 0.5f * p.x, a.y - 0.5f * p.y);
+        float2 v = mul_i<DIR>(make_float2(h * m.x, h * m.y));
+        t[0] = cadd(a, p);
+        t[1] = cadd(u, v);
+        t[2] = csub(u, v);
+    } else if constexpr (R == 5) {
+        constexpr CS w1 = ct_cossin(1, 5), w2 = ct_cossin(2, 5);
+        constexpr float c1 = (float)w1.c, c2 = (float)w2.c, s1 = (float)w1.s, s2 = (float)w2.s;
+        float2 x0 = t[0];
+        float2 a1 = cadd(t[1], t[4]), a2 = cadd(t[2], t[3]);
+        float2 b1 = csub(t[1], t[4]), b2 = csub(t[2], t[3]);
+        float2 t1 = make_float2(x0.x + c1 * a1.x + c2 * a2.x, x0.y + c1 * a1.y + c2 * a2.y);
+        float2 t2 = make_float2(x0.x + c2 * a1.x + c1 * a2.x, x0.y + c2 * a1.y + c1 * a2.y);
+        float2 u1 = mul_i<DIR>(make_float2(s1 * b1.x + s2 * b2.x, s1 * b1.y + s2 * b2.y));
+        float2 u2 = mul_i<DIR>(make_float2(s2 * b1.x - s1 * b2.x, s2 * b1.y - s1 * b2.y));
+        t[0] = make_float2(x0.x + a1.x + a2.x, x0.y + a1.y + a2.y);
+        t[1] = cadd(t1, u1);
+        t[4] = csub(t1, u1);
+        t[2] = cadd(t2, u2);
+        t[3] = csub(t2, u2);
+    } else {
+        // direct R-point DFT for a prime R
+        float2 o[R];
+        sfor<0, R>([&](auto sc) {
+            constexpr int s = decltype(sc)::value;
+            float2 acc = t[0];
+            sfor<1, R>([&](auto rc) {
+                constexpr int r = decltype(rc)::value;
+                float2 v = twmul<DIR, (long)r * s, R>(t[r]);
+                acc = cadd(acc, v);
+            });
+            o[s] = acc;
+        });
+        sfor<0, R>([&](auto sc) {
+            constexpr int s = decltype(sc)::value;
+            t[s] = o[s];
+        });
+    }
+}
+
+// In-place DIF transform of x[OFF .. OFF+L): out freq k at x[OFF + dif_pos<L>(k)].
+// DIR = -1 forward (exp(-i...)), +1 backward; unnormalised.
+template <int L, int OFF, int DIR>
+FLCT_HD void dif(float2* x) {
+    if constexpr (L > 1) {
+        constexpr int R = radix_of<L>(), M = L / R;
+        sfor<0, M>([&](auto mc) {
+            constexpr int m = decltype(mc)::value;
+            float2 t[R];
+            sfor<0, R>([&](auto rc) {
+                constexpr int r = decltype(rc)::value;
+                t[r] = x[OFF + m + M * r];
+            });
+            small_dft<R, DIR>(t);
+            sfor<0, R>([&](auto sc) {
+                constexpr int s = decltype(sc)::value;
+                x[OFF + m + M * s] = twmul<DIR, (long)m * s, L>(t[s]);
+            });
+        });
+        sfor<0, R>([&](auto sc) {
+            constexpr int s = decltype(sc)::value;
+            dif<M, OFF + M * s, DIR>(x);
+        });
+    }
+}
+
+}  // namespace flct

@@ -1,0 +1,31 @@
+// window_fp32_inst.cuh -- explicit instantiation of the FP32 window kernel
+// for one box size (each per-size .cu file includes this once per size, so
+// the sizes compile in parallel).
+#pragma once
+#include "window_fp32.cuh"
+
+#define FLCT_INSTANTIATE_WINDOW_FP32(N)                                                        \
+    namespace flct {                                                                           \
+    template <>                                                                                \
+    cudaError_t launch_window_fp32<N>(const WinArgs& a, int grid, cudaStream_t st) {           \
+        using S = WinShape<N>;                                                                 \
+        cudaError_t e = cudaFuncSetAttribute(k_window_fp32<N>,                                 \
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,      \
+                                             (int)S::smem);                                    \
+        if (e != cudaSuccess) return e;                                                        \
+        k_window_fp32<N><<<grid, S::THREADS, S::smem, st>>>(a);                                \
+        return cudaGetLastError();                                                             \
+    }                                                                                          \
+    template <>                                                                                \
+    int window_fp32_blocks_per_sm<N>() {                                                       \
+        using S = WinShape<N>;                                                                 \
+        int nb = 0;                                                                            \
+        if (cudaFuncSetAttribute(k_window_fp32<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                 (int)S::smem) != cudaSuccess)                                 \
+            return 0;                                                                          \
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_window_fp32<N>, S::THREADS,   \
+                                                          S::smem) != cudaSuccess)             \
+            return 0;                                                                          \
+        return nb;                                                                             \
+    }                                                                                          \
+    }

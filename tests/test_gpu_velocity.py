@@ -1,0 +1,194 @@
+"""GPU parity of the velocity path (the flct program) against the FP64 oracle
+and the reference's golden vectors.  Every call goes through the C ABI
+(libflctgpu.so) via pyflct_gb300.
+
+Tolerance: max |dv| <= 1e-3 px/frame against the FP64 oracle on computed
+and interpolated pixels, bit-exact mask (vm), identical integer peaks except
+at argmax ties documented by _compare.classify_ties.
+"""
+import numpy as np
+import pytest
+
+import pyoracle as po
+from _compare import TOL, compare
+from _golden import cli_cases, load, parse_cli_args, window_cases
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def gpu():
+    from pyflct_gb300 import build
+    build.build()
+    from pyflct_gb300 import _lib
+    return _lib.context(0)
+
+
+def gpu_flct(f1, f2, kw):
+    from pyflct_gb300.flct import flct
+    thresh = kw.get("thresh")
+    if thresh is not None and kw.get("thresh_abs"):
+        thresh = f"{thresh!r}a"
+    skip = None
+    if kw.get("skip"):
+        s = kw["skip"]
+        skip = f"{s}p{kw.get('poffset', 0)}q{kw.get('qoffset', 0)}" + ("i" if kw.get("interpolate") else "")
+        if s < 0:
+            skip = "0"
+    return flct(f1, f2, kw.get("deltat", 1.0), kw.get("deltas", 1.0), kw["sigma"], thresh=thresh,
+                kr=kw.get("kr"), skip=skip, hires=kw.get("hires", False))
+
+
+def test_reference_shipped_fixture():
+    """flct hashgauss.dat out 1 1 5 -k 0.5 against tests/testgaussvel.dat."""
+    z = load("reference_tests.npz")
+    f1, f2 = z["f1"].astype(np.float64), z["f2"].astype(np.float64)
+    kw = dict(deltat=1, deltas=1, sigma=5, kr=0.5)
+    got = gpu_flct(f1, f2, kw)
+    ref = po.velocity(f1, f2, **kw)
+    rep = compare(f1, f2, got, ref, kw)
+    assert np.array_equal(got[2], z["vm"].astype(np.float64))
+    fix = (z["vx"].astype(np.float64), z["vy"].astype(np.float64))
+    ok = got[2] == 1
+    assert np.abs(got[0] - fix[0])[ok].max() < TOL + 1e-6
+    assert np.abs(got[1] - fix[1])[ok].max() < TOL + 1e-6
+    print(rep)
+
+
+ERR = {"err_skip_zero": 2, "err_skip_offset": 3, "err_skip_too_big": 4, "err_box_size": 5}
+
+
+@pytest.mark.parametrize("case", cli_cases(), ids=lambda c: c[0])
+def test_cli_case(case):
+    from pyflct_gb300.flct import FlctError
+    name, args, rc, f1, f2, golden = case
+    kw = parse_cli_args(args)
+    if rc != 0:
+        with pytest.raises(FlctError) as e:
+            gpu_flct(f1, f2, kw)
+        assert e.value.code == ERR[name]
+        return
+    if kw.get("hires") or kw["sigma"] <= 0:
+        pytest.skip("-h and sigma=0 are not on the GPU path yet")
+    got = gpu_flct(f1, f2, kw)
+    ref = po.velocity(f1, f2, **kw)
+    rep = compare(f1, f2, got, ref, kw)
+    # the golden file holds the reference's float32-rounded output
+    assert np.array_equal(got[2], golden[2])
+    print(name, rep)
+
+
+@pytest.mark.parametrize("wc", window_cases(), ids=lambda w: f"n{w[0]}_kr{w[1]}")
+def test_cross_cor_windows(wc):
+    from pyflct_gb300.flct import cross_cor
+    n, kr, g1, g2, sx, sy = wc
+    gx, gy = cross_cor(g1, g2, kr=kr)
+    assert np.abs(gx - sx).max() <= TOL
+    assert np.abs(gy - sy).max() <= TOL
+
+
+def test_interpcc2d_bit_exact():
+    from pyflct_gb300.flct import interpcc2d
+    z = load("ref_interp_cases.npz")
+    for q in range(int(z["count"])):
+        out = interpcc2d(z[f"i{q}_f"], float(z[f"i{q}_xmiss"]), z[f"i{q}_xw"], z[f"i{q}_yw"])
+        assert np.array_equal(out, z[f"i{q}_out"]), q
+
+
+def test_config1_blobs_128():
+    from pyflct_gb300 import synth
+    f1, f2, kw = synth.config1()
+    got = gpu_flct(f1, f2, kw)
+    ref = po.velocity(f1, f2, **kw)
+    rep = compare(f1, f2, got, ref, kw)
+    # the applied shift is (+0.3 fast, -0.2 slow); FLCT's small-window bias
+    # pulls sigma=4 estimates toward zero (the FP64 oracle shows the same),
+    # so only the direction is a physics check here
+    c = (slice(20, 108), slice(20, 108))
+    assert 0.05 < np.median(got[0][c]) < 0.35 and -0.25 < np.median(got[1][c]) < -0.03
+    print(rep)
+
+
+@pytest.mark.parametrize("shape,sigma,extra", [
+    ((96, 80), 3, {}), ((64, 72), 5, {"kr": 0.25}), ((120, 100), 12, {}),
+    ((200, 210), 15, {"kr": 0.5}), ((50, 60), 7, {}), ((70, 66), 9, {"thresh": 0.3}),
+    ((80, 84), 4, {"skip": 3, "poffset": 2, "qoffset": -1, "interpolate": True}),
+    ((90, 90), 6, {"skip": 5, "interpolate": True, "thresh": 0.4, "thresh_abs": True}),
+])
+def test_random_fields(shape, sigma, extra):
+    from pyflct_gb300 import synth
+    rng = np.random.default_rng(hash((shape, sigma)) % 2**32)
+    f1 = synth.kfield(shape, rng)
+    f2 = synth.fourier_shift(f1, *rng.uniform(-1.5, 1.5, 2))
+    kw = dict(sigma=sigma, **extra)
+    rep = compare(f1, f2, gpu_flct(f1, f2, kw), po.velocity(f1, f2, **kw), kw)
+    print(shape, sigma, rep)
+
+
+def test_config3_full_size_1024():
+    """The headline workload (1024^2, sigma 8, -s 4i) against the oracle."""
+    from pyflct_gb300 import synth
+    rng = np.random.default_rng(20263)
+    f1 = synth.kfield((1024, 1024), rng)
+    dfast, dslow = synth.vortex_shift(f1.shape, rng)
+    f2 = synth.spline_warp(f1, dfast, dslow)
+    kw = dict(sigma=8, skip=4, interpolate=True)
+    rep = compare(f1, f2, gpu_flct(f1, f2, kw), po.velocity(f1, f2, **kw), kw)
+    assert rep["computed"] == 256 * 256
+    print(rep)
+
+
+def test_config2_full_size_512_threshold():
+    """512^2, sigma 8, -t 0.1a -k 0.5 with near-zero pixels (mask exercise)."""
+    from pyflct_gb300 import synth
+    rng = np.random.default_rng(20262)
+    f1 = synth.config2_image1(rng)
+    dfast, dslow = synth.rotation_shift(f1.shape, 0.01)
+    f2 = synth.spline_warp(f1, dfast, dslow)
+    kw = dict(sigma=8, thresh=0.1, thresh_abs=True, kr=0.5)
+    got = gpu_flct(f1, f2, kw)
+    rep = compare(f1, f2, got, po.velocity(f1, f2, **kw), kw)
+    assert 0 < rep["computed"] < 512 * 512
+    print(rep)
+
+
+def test_edge_cases():
+    from pyflct_gb300.flct import flct
+    z = np.zeros((40, 44))
+    got = flct(z, z, 1, 1, 4)
+    assert np.all(got[0] == 0) and np.all(got[1] == 0) and np.all(got[2] == 1)
+    rng = np.random.default_rng(3)
+    a = rng.standard_normal((12, 12))
+    b = np.roll(a, 1, axis=1)
+    kw = dict(sigma=2)  # box 4 on a 12x12 frame
+    compare(a, b, gpu_flct(a, b, kw), po.velocity(a, b, **kw), kw)
+    # constant frames give g == 0 exactly: zero shift everywhere
+    c = np.full((30, 30), 3.25)
+    got = flct(c, c, 1, 1, 3)
+    assert np.all(got[0] == 0) and np.all(got[1] == 0)
+    # relative threshold above every pixel: nothing computed, all zero
+    got = flct(a, b, 1, 1, 2, thresh=0.999)
+    ref = po.velocity(a, b, sigma=2, thresh=0.999)
+    assert np.array_equal(got[2], ref[2])
+
+
+def test_error_codes():
+    from pyflct_gb300.flct import FlctError, flct
+    a = np.ones((30, 30))
+    for kw, code in [(dict(skip="0"), 2), (dict(skip="3p3"), 3), (dict(skip="30"), 4),
+                     (dict(skip="15i"), 6)]:
+        with pytest.raises(FlctError) as e:
+            flct(a, a, 1, 1, 3, **kw)
+        assert e.value.code == code, kw
+    with pytest.raises(FlctError) as e:
+        flct(a, a, 1, 1, 0.5)
+    assert e.value.code == 5
+
+
+def test_repeat_calls_are_identical():
+    from pyflct_gb300 import synth
+    f1, f2, kw = synth.config1()
+    a = gpu_flct(f1, f2, kw)
+    b = gpu_flct(f1, f2, kw)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
