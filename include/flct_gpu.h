@@ -125,8 +125,9 @@ FLCT_API flct_status flct_gpu_velocity(flct_ctx *ctx, const flct_params *p,
                               int ny, double *vx, double *vy, double *vm);
 
 /* Device buffers on the caller's CUDA stream (cudaStream_t passed as a
- * void*; NULL means the context's own stream).  Asynchronous with respect
- * to the host: returns once everything is enqueued. */
+ * void*; NULL means the CUDA default stream, as everywhere in CUDA).
+ * Asynchronous with respect to the host: returns once everything is
+ * enqueued.  flct_gpu_last_timing waits for the call to finish. */
 FLCT_API flct_status flct_gpu_velocity_device(flct_ctx *ctx, const flct_params *p,
                                      const double *d_f1, const double *d_f2,
                                      int nx, int ny, double *d_vx,

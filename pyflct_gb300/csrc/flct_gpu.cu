@@ -293,7 +293,7 @@ flct_status flct_gpu_velocity_device(flct_ctx* ctx, const flct_params* p, const 
         return fail(ctx, FLCT_ERR_ARG, "null pointer or empty image (%d x %d)", nx, ny);
     if ((long long)nx * ny >= (1ll << 31)) return fail(ctx, FLCT_ERR_UNSUPPORTED, "image larger than 2^31 pixels");
     CK(cudaSetDevice(ctx->device));
-    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    cudaStream_t st = (cudaStream_t)stream;  // NULL: the CUDA default stream
     Derived d;
     flct_status s = derive(ctx, p, nx, ny, &d);
     if (s != FLCT_OK) return s;
