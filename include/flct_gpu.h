@@ -173,6 +173,34 @@ FLCT_API flct_status flct_gpu_warp_frac2d(flct_ctx *ctx, const double *arr,
                                  const double *delx, const double *dely,
                                  double *out, int nx, int ny, int transp);
 
+/* ---- without device allocation ---------------------------------------- */
+
+/* Largest nxi and nyi flct_gpu_interpcc2d_noalloc accepts. */
+#define FLCT_NOALLOC_MAX_AXIS 16384
+
+/* interpcc2d for callers that cannot allocate GPU memory: programs that hand
+ * all device memory to their own pool or fix their device-memory budget at
+ * start-up, and so cannot let a library call cudaMalloc.  It has no
+ * counterpart in the reference; it computes what flct_gpu_interpcc2d
+ * computes, on device pointers (fdata nx x ny, xwant nxi, ywant nyi, out
+ * nxi x nyi) on `stream` (NULL: the CUDA default stream), and allocates
+ * nothing: its only scratch is a fixed 1.2 MB array inside the library that
+ * every GPU which loads the library keeps until the process exits.
+ *   - nxi or nyi above FLCT_NOALLOC_MAX_AXIS: FLCT_ERR_UNSUPPORTED;
+ *     nx or ny below 3: FLCT_ERR_GRID_TOO_SMALL.
+ *   - The first call on a device looks up that array's device address once
+ *     (with that device current); make that first call before any stream
+ *     capture begins.
+ *   - All calls share the one array: calls that overlap on the GPU (other
+ *     streams, other host threads) race and must be serialised by the
+ *     caller.
+ *   - Asynchronous: returns once the work is enqueued. */
+FLCT_API flct_status flct_gpu_interpcc2d_noalloc(const double *d_fdata, double xmiss,
+                                                 int nx, int ny,
+                                                 const double *d_xwant, int nxi,
+                                                 const double *d_ywant, int nyi,
+                                                 double *d_out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

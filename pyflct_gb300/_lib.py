@@ -87,6 +87,8 @@ SIGNATURES = {
     "flct_gpu_shift_frac2d": (C.c_int, [_vp, _dp, C.c_double, C.c_double, _dp, C.c_int, C.c_int,
                                         C.c_int]),
     "flct_gpu_warp_frac2d": (C.c_int, [_vp, _dp, _dp, _dp, _dp, C.c_int, C.c_int, C.c_int]),
+    "flct_gpu_interpcc2d_noalloc": (C.c_int, [_vp, C.c_double, C.c_int, C.c_int, _vp, C.c_int, _vp,
+                                              C.c_int, _vp, _vp]),
 }
 
 _lock = threading.Lock()
