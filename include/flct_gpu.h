@@ -98,6 +98,7 @@ typedef struct {
     int launches;        /* kernels launched by the call */
     int box;             /* box side n = 2*nsize of the last call */
     int form;            /* flct_form actually used */
+    float ms_fit;        /* FP64 peak fit, velocity and mask pass */
 } flct_timing;
 
 /* ---- context ------------------------------------------------------- */

@@ -46,6 +46,7 @@ class Timing(C.Structure):
         ("ms_total", C.c_float), ("ms_window", C.c_float), ("ms_prepass", C.c_float),
         ("ms_interp", C.c_float), ("ms_h2d", C.c_float), ("ms_d2h", C.c_float),
         ("windows", C.c_longlong), ("launches", C.c_int), ("box", C.c_int), ("form", C.c_int),
+        ("ms_fit", C.c_float),
     ]
 
 

@@ -79,10 +79,10 @@ struct flct_ctx {
         size_t n = 0;
     };
     Buf b_s1, b_s2, b_work, b_ctr, b_r1, b_r2, b_b1, b_b2, b_gvx, b_gvy, b_ix, b_iy;
-    Buf b_f1, b_f2, b_vx, b_vy, b_vm, b_aux1, b_aux2;
+    Buf b_f1, b_f2, b_vx, b_vy, b_vm, b_aux1, b_aux2, b_means, b_peaks, b_hrow;
     std::vector<Buf*> all() {
-        return {&b_s1, &b_s2, &b_work, &b_ctr, &b_r1, &b_r2, &b_b1, &b_b2, &b_gvx,
-                &b_gvy, &b_ix, &b_iy, &b_f1, &b_f2, &b_vx, &b_vy, &b_vm, &b_aux1, &b_aux2};
+        return {&b_s1, &b_s2, &b_work, &b_ctr, &b_r1, &b_r2, &b_b1, &b_b2, &b_gvx, &b_gvy, &b_ix,
+                &b_iy, &b_f1, &b_f2, &b_vx, &b_vy, &b_vm, &b_aux1, &b_aux2, &b_means, &b_peaks, &b_hrow};
     }
     int bps[sizeof(kWin) / sizeof(kWin[0])] = {0};
     bool pending = false;  // a velocity call's events await collection
@@ -316,8 +316,11 @@ flct_status flct_gpu_velocity_device(flct_ctx* ctx, const flct_params* p, const 
     ENSURE(ctx->b_r2, (size_t)nx * W * sizeof(double));
     ENSURE(ctx->b_b1, (size_t)H * W * sizeof(double));
     ENSURE(ctx->b_b2, (size_t)H * W * sizeof(double));
+    ENSURE(ctx->b_means, npx * sizeof(float4));
+    ENSURE(ctx->b_peaks, npx * sizeof(PeakRec));
     const bool interp = d.skip > 0 && p->interpolate;
     if (interp) {
+        ENSURE(ctx->b_hrow, (size_t)(d.icnt + 2) * ny * (2 * sizeof(double) + 1));
         ENSURE(ctx->b_gvx, (size_t)d.icnt * d.jcnt * sizeof(double));
         ENSURE(ctx->b_gvy, (size_t)d.icnt * d.jcnt * sizeof(double));
         ENSURE(ctx->b_ix, (size_t)nx * (4 * sizeof(double) + sizeof(int) + 1) + 64);
@@ -376,6 +379,23 @@ flct_status flct_gpu_velocity_device(flct_ctx* ctx, const flct_params* p, const 
                                                          (double*)ctx->b_b1.p, (double*)ctx->b_b2.p);
         launches += 2;
     }
+    {
+        // FP64 local means per work item, one window per lane
+        MeansArgs ma{};
+        ma.work = (const int*)ctx->b_work.p;
+        ma.nwork = d_nwork;
+        ma.nx = nx;
+        ma.ny = ny;
+        ma.nsize = d.nsize;
+        ma.bsw = W;
+        ma.bs1 = (const double*)ctx->b_b1.p;
+        ma.bs2 = (const double*)ctx->b_b2.p;
+        ma.inv_n2 = 1. / ((double)n * n);
+        ma.means = (float4*)ctx->b_means.p;
+        long blocks = std::min<long>((long)(npx + 255) / 256, (long)ctx->nsm * 8);
+        k_means<<<(int)std::max(1l, blocks), 256, 0, st>>>(ma);
+        ++launches;
+    }
     CK(cudaGetLastError());
     CK(cudaEventRecord(ctx->ev[1], st));
 
@@ -384,31 +404,41 @@ flct_status flct_gpu_velocity_device(flct_ctx* ctx, const flct_params* p, const 
     wa.use_filter = p->filter;
     wa.s1 = (const float2*)ctx->b_s1.p;
     wa.s2 = (const float2*)ctx->b_s2.p;
-    wa.bs1 = (const double*)ctx->b_b1.p;
-    wa.bs2 = (const double*)ctx->b_b2.p;
+    wa.means = (const float4*)ctx->b_means.p;
     wa.work = (const int*)ctx->b_work.p;
     wa.nwork = d_nwork;
     wa.nx = nx;
     wa.ny = ny;
     wa.nsize = d.nsize;
-    wa.bsw = W;
-    wa.inv_n2 = 1. / ((double)n * n);
-    wa.deltinv = 1. / p->deltat;  // flct.c:343
-    wa.deltas = p->deltas;
-    wa.interpolate = interp;
-    wa.skip = d.skip > 0 ? d.skip : 1;
-    wa.xoff = d.xoff;
-    wa.yoff = d.yoff;
-    wa.jcnt = d.jcnt;
-    wa.vx = d_vx;
-    wa.vy = d_vy;
-    wa.vm = d_vm;
-    wa.gvx = ca.gvx;
-    wa.gvy = ca.gvy;
+    wa.peaks = (PeakRec*)ctx->b_peaks.p;
     const int grid = win_grid(ctx, n);
     CK(we->launch(wa, grid, st));
     ++launches;
     CK(cudaEventRecord(ctx->ev[2], st));
+    {
+        FitArgs fa{};
+        fa.work = (const int*)ctx->b_work.p;
+        fa.nwork = d_nwork;
+        fa.peaks = (const PeakRec*)ctx->b_peaks.p;
+        fa.n = n;
+        fa.ny = ny;
+        fa.deltinv = 1. / p->deltat;  // flct.c:343
+        fa.deltas = p->deltas;
+        fa.skip = d.skip > 0 ? d.skip : 1;
+        fa.xoff = d.xoff;
+        fa.yoff = d.yoff;
+        fa.jcnt = d.jcnt;
+        fa.vx = d_vx;
+        fa.vy = d_vy;
+        fa.vm = d_vm;
+        fa.gvx = ca.gvx;
+        fa.gvy = ca.gvy;
+        long blocks = std::min<long>((long)(npx + 127) / 128, (long)ctx->nsm * 8);
+        k_fit<<<(int)std::max(1l, blocks), 128, 0, st>>>(fa);
+        ++launches;
+    }
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ctx->ev[7], st));
 
     if (interp) {
         unsigned char* ix = (unsigned char*)ctx->b_ix.p;
@@ -437,12 +467,18 @@ flct_status flct_gpu_velocity_device(flct_ctx* ctx, const flct_params* p, const 
         ia.zy = zy;
         ia.wy = wy;
         ia.oky = oky;
+        const size_t hn = (size_t)(d.icnt + 2) * ny;
+        ia.hx = (double*)ctx->b_hrow.p;
+        ia.hy = ia.hx + hn;
+        ia.hbad = (unsigned char*)(ia.hy + hn);
         ia.vx = d_vx;
         ia.vy = d_vy;
         ia.vm = d_vm;
+        long rblocks = std::min<long>((long)(hn + 255) / 256, (long)ctx->nsm * 8);
+        k_interp_rows<<<(int)std::max(1l, rblocks), 256, 0, st>>>(ia);
         long blocks = std::min<long>((long)(npx + 255) / 256, (long)ctx->nsm * 16);
         k_interp<<<(int)std::max(1l, blocks), 256, 0, st>>>(ia);
-        launches += 3;
+        launches += 4;
         CK(cudaGetLastError());
     }
     CK(cudaEventRecord(ctx->ev[3], st));
@@ -467,7 +503,8 @@ static flct_status collect_timing(flct_ctx* ctx) {
     ctx->timing.windows = nwork;
     ctx->timing.ms_prepass = ev_ms(ctx->ev[0], ctx->ev[1]);
     ctx->timing.ms_window = ev_ms(ctx->ev[1], ctx->ev[2]);
-    ctx->timing.ms_interp = ev_ms(ctx->ev[2], ctx->ev[3]);
+    ctx->timing.ms_fit = ev_ms(ctx->ev[2], ctx->ev[7]);
+    ctx->timing.ms_interp = ev_ms(ctx->ev[7], ctx->ev[3]);
     ctx->timing.ms_total = ev_ms(ctx->ev[0], ctx->ev[3]);
     if (status & kStatusRange)
         return fail(ctx, FLCT_ERR_UNSUPPORTED, "an input magnitude exceeds the FP32 range of the GPU kernels");
@@ -574,28 +611,35 @@ flct_status flct_gpu_cross_cor_batch(flct_ctx* ctx, const double* g1, const doub
     wa.use_filter = filter;
     wa.s1 = (const float2*)ctx->b_s1.p;
     wa.s2 = (const float2*)ctx->b_s2.p;
-    wa.bs1 = nullptr;
-    wa.bs2 = nullptr;
+    wa.means = nullptr;
     wa.work = (const int*)ctx->b_work.p;
     wa.nwork = (const int*)ctr;
     wa.nx = nwin * n;
     wa.ny = n;
     wa.nsize = n / 2;
-    wa.bsw = 1;
-    wa.inv_n2 = 0.;
-    wa.skip = 1;
-    wa.shx = (double*)ctx->b_vx.p;
-    wa.shy = (double*)ctx->b_vy.p;
     wa.direct = 1;
+    ENSURE(ctx->b_peaks, (size_t)nwin * sizeof(PeakRec));
+    wa.peaks = (PeakRec*)ctx->b_peaks.p;
     CK(we->launch(wa, win_grid(ctx, n), st));
     CK(cudaEventRecord(ctx->ev[2], st));
+    FitArgs fa{};
+    fa.work = (const int*)ctx->b_work.p;
+    fa.nwork = (const int*)ctr;
+    fa.peaks = (const PeakRec*)ctx->b_peaks.p;
+    fa.n = n;
+    fa.ny = n;
+    fa.skip = 1;
+    fa.shx = (double*)ctx->b_vx.p;
+    fa.shy = (double*)ctx->b_vy.p;
+    k_fit<<<(int)std::max(1, std::min((nwin + 127) / 128, ctx->nsm * 8)), 128, 0, st>>>(fa);
+    CK(cudaGetLastError());
     CK(cudaMemcpyAsync(shiftx, ctx->b_vx.p, nwin * sizeof(double), cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(shifty, ctx->b_vy.p, nwin * sizeof(double), cudaMemcpyDeviceToHost, st));
     CK(cudaEventRecord(ctx->ev[3], st));
     CK(cudaStreamSynchronize(st));
     ctx->timing = flct_timing{};
     ctx->timing.windows = nwin;
-    ctx->timing.launches = 2;
+    ctx->timing.launches = 3;
     ctx->timing.box = n;
     ctx->timing.form = FLCT_FORM_FP32;
     ctx->timing.ms_window = ev_ms(ctx->ev[1], ctx->ev[2]);

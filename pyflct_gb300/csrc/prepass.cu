@@ -269,22 +269,64 @@ __device__ __forceinline__ double interp_one(const double* __restrict__ g, int g
     return bad ? xmiss : acc;
 }
 
+// Separable form of the velocity pipeline's interpolation.  Every output in
+// column j contracts the same cdata rows with the same ry weights, so
+//   H[a][j] = sum_q cdata[a][jz(j)+q] ry_j[q]      (k_interp_rows, once)
+//   out[i][j] = sum_p rx_i[p] H[iz(i)+p][j]          (k_interp, per pixel)
+// which is the reference's 4x4 sum regrouped (equal up to the last bits of
+// the FP64 rounding); the xmiss test is the same set of 16 comparisons,
+// split the same way, so the mask is exact.
+__global__ void k_interp_rows(InterpArgs a) {
+    const long n = (long)(a.gx + 2) * a.ny;
+    for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
+        const int r = (int)(k / a.ny), j = (int)(k - (long)(k / a.ny) * a.ny);
+        if (!a.oky[j]) continue;  // out of range: every output of column j is xmiss
+        const int jz = a.zy[j];
+        double hx = 0., hy = 0.;
+        unsigned char bad = 0;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const double ry = a.wy[(size_t)j * 4 + q];
+            const int b = jz + q;
+            double cx, cy;
+            if (r >= 1 && r <= a.gx && b >= 1 && b <= a.gy) {
+                cx = a.gvx[(size_t)(r - 1) * a.gy + (b - 1)];
+                cy = a.gvy[(size_t)(r - 1) * a.gy + (b - 1)];
+            } else {
+                cx = cdata_at(a.gvx, a.gx, a.gy, r, b);
+                cy = cdata_at(a.gvy, a.gx, a.gy, r, b);
+            }
+            hx = fma(cx, ry, hx);
+            hy = fma(cy, ry, hy);
+            bad |= (cx == kXmiss ? 1 : 0) | (cy == kXmiss ? 2 : 0);
+        }
+        a.hx[k] = hx;
+        a.hy[k] = hy;
+        a.hbad[k] = bad;
+    }
+}
+
 __global__ void k_interp(InterpArgs a) {
     const long n = (long)a.nx * a.ny;
     for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
         const int i = (int)(k / a.ny), j = (int)(k - (long)(k / a.ny) * a.ny);
         const bool gi = !((i - a.xoff) % a.skip), gj = !((j - a.yoff) % a.skip);
         if (gi && gj) continue;  // grid points keep their computed value
-        double rx[4], ry[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            rx[q] = a.wx[(size_t)i * 4 + q];
-            ry[q] = a.wy[(size_t)j * 4 + q];
-        }
         double vx = kXmiss, vy = kXmiss;
         if (a.okx[i] && a.oky[j]) {
-            vx = interp_one(a.gvx, a.gx, a.gy, kXmiss, a.zx[i], rx, a.zy[j], ry);
-            vy = interp_one(a.gvy, a.gx, a.gy, kXmiss, a.zx[i], rx, a.zy[j], ry);
+            const int iz = a.zx[i];
+            double sx = 0., sy = 0.;
+            unsigned char bad = 0;
+#pragma unroll
+            for (int p = 0; p < 4; ++p) {
+                const double rx = a.wx[(size_t)i * 4 + p];
+                const size_t h = (size_t)(iz + p) * a.ny + j;
+                sx = fma(rx, a.hx[h], sx);
+                sy = fma(rx, a.hy[h], sy);
+                bad |= a.hbad[h];
+            }
+            vx = (bad & 1) ? kXmiss : sx;
+            vy = (bad & 2) ? kXmiss : sy;
         }
         double vm = 0.5;
         // the final xmiss reset (flct.c:1125-1133)

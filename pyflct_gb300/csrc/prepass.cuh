@@ -33,6 +33,8 @@ struct InterpArgs {
     const int* zy;
     const double* wy;
     const unsigned char* oky;
+    double *hx, *hy;          // row contractions [(gx+2) x ny]
+    unsigned char* hbad;      // xmiss flags of those rows (bit 0: vx, bit 1: vy)
     double *vx, *vy, *vm;
 };
 
@@ -44,6 +46,7 @@ __global__ void k_rowsum(const double* f1, const double* f2, int nx, int ny, int
 __global__ void k_colsum(const double* r1, const double* r2, int nx, int W, int n, double* b1, double* b2);
 __global__ void k_interp_axis(int n, int gcount, int off, int skip, const double* want, int* zero,
                               double* wts, unsigned char* ok);
+__global__ void k_interp_rows(InterpArgs a);
 __global__ void k_interp(InterpArgs a);
 __global__ void k_interp_general(const double* f, int gx, int gy, double xmiss, const int* zx,
                                  const double* wx, const unsigned char* okx, int nxi, const int* zy,

@@ -1,0 +1,57 @@
+// window_common.cuh -- the FP64 passes around the window-correlation
+// kernels, shared by every window form.
+//
+// GB300's FP64 pipe is narrow, and an FP64 instruction executed by one lane
+// of a warp costs as much pipe time as one executed by all 32.  So the
+// per-window FP64 work of the reference's loop body runs here with one
+// window per lane instead of inside the window kernels:
+//   k_means  FP64 local means from the box sums (flct.c:815-827), split into
+//            float hi + lo for the FP32 window load;
+//   k_fit    the 3x3 Taylor fit around the integer peak (flct.c:1536-1553,
+//            1639-1640), velocity (flct.c:901-905), mask, skip-grid copy and
+//            the final xmiss reset (flct.c:918-942, 1125-1133).
+#pragma once
+#include "common.cuh"
+
+namespace flct {
+
+constexpr int kMaxBox = 64;  // largest box side with a compiled window kernel
+
+// What a window kernel hands to k_fit: |c| at the 3x3 stencil around the
+// integer peak (half-shifted frame, row-major) and the peak itself.
+struct PeakRec {
+    float v[9];
+    unsigned meta;  // I | J << 8 | dofit << 16
+};
+
+__host__ __device__ __forceinline__ unsigned peak_meta(int I, int J, bool dofit) {
+    return (unsigned)I | ((unsigned)J << 8) | ((dofit ? 1u : 0u) << 16);
+}
+
+struct MeansArgs {
+    const int* work;
+    const int* nwork;
+    int nx, ny, nsize, bsw;
+    const double* bs1;
+    const double* bs2;
+    double inv_n2;
+    float4* means;
+};
+
+struct FitArgs {
+    const int* work;
+    const int* nwork;
+    const PeakRec* peaks;
+    int n;                 // box side
+    int ny;
+    double deltinv, deltas;
+    int skip, xoff, yoff, jcnt;
+    double *vx, *vy, *vm;  // outputs [nx*ny] or null (window-only calls)
+    double *gvx, *gvy;     // skip-grid copies or null
+    double *shx, *shy;     // raw shifts per work item or null
+};
+
+__global__ void k_means(MeansArgs a);
+__global__ void k_fit(FitArgs a);
+
+}  // namespace flct

@@ -5,8 +5,10 @@
 // takes the n x n box around the pixel from both frames, subtracts the FP64
 // local means, applies the Gaussian centred on the pixel, transforms both
 // sub-images, forms conj(A)*B (times the squared k-space filter for -k),
-// transforms back, takes |c| in the half-shifted frame, finds the first
-// strict maximum and refines it with the FP64 3x3 Taylor fit.
+// transforms back, takes |c| in the half-shifted frame and finds the first
+// strict maximum.  The FP64 parts run in one-window-per-lane passes around
+// it (window_common.cuh): k_means before, k_fit (3x3 Taylor fit, velocity,
+// mask) after; this kernel does no FP64 arithmetic.
 //
 // Layout: a "team" of n threads owns one window; a CTA runs TEAMS teams in
 // lockstep.  The two real sub-images travel as one complex array
@@ -18,28 +20,20 @@
 #pragma once
 #include "common.cuh"
 #include "fft_reg.cuh"
+#include "window_common.cuh"
 
 namespace flct {
-
-constexpr int kMaxBox = 64;  // largest box side with a compiled kernel
 
 struct WinArgs {
     const float2* s1;     // f1 split (hi, lo) [nx*ny]
     const float2* s2;     // f2 split
-    const double* bs1;    // f1 box sums [(nx-n+1) x bsw]
-    const double* bs2;
+    const float4* means;  // per work item (m1 hi, m1 lo, m2 hi, m2 lo), or null: zero means
     const int* work;      // pixel indices i*ny + j
     const int* nwork;     // number of work items (device)
-    int nx, ny, nsize, bsw;
-    double inv_n2;        // 1 / n^2
-    double deltinv, deltas;
+    int nx, ny, nsize;
     int use_filter;       // -k given
-    int direct;           // windows given directly: box w starts at row w*n, no mean, unit weights
-    int interpolate, skip, xoff, yoff, jcnt;
-    double *vx, *vy, *vm; // outputs [nx*ny]
-    double *gvx, *gvy;    // skip-grid copies of vx, vy (interpolation) or null
-    double* shx;          // optional raw shifts per work item (slow axis)
-    double* shy;          // optional raw shifts per work item (fast axis)
+    int direct;           // windows given directly: box w starts at row w*n, unit weights
+    PeakRec* peaks;       // per work item: integer peak and its 3x3 |c| stencil
     float gauss[2 * kMaxBox + 1];  // weight of offset d at d + n (separable Gaussian)
     float filt2[kMaxBox];          // squared k-space filter factor by frequency index
 };
@@ -53,31 +47,12 @@ struct WinShape {
     static constexpr size_t smem = head + (size_t)TEAMS * BUF * 8 + (size_t)TEAMS * N * N * 4;
 };
 
-// Reference-order FP64 helpers (no contraction into FMA).
-__device__ __forceinline__ double dm(double a, double b) { return __dmul_rn(a, b); }
-__device__ __forceinline__ double da(double a, double b) { return __dadd_rn(a, b); }
-__device__ __forceinline__ double ds(double a, double b) { return __dsub_rn(a, b); }
-
-// 3x3 Taylor fit (flct.c:1536-1553) on |c| values around the peak.
-// v[a][b] = |c| at (I-1+a, J-1+b).
-__device__ __forceinline__ void taylor_fit(const double v[3][3], double* sx, double* sy) {
-    double fx = dm(0.5, ds(v[2][1], v[0][1]));
-    double fy = dm(0.5, ds(v[1][2], v[1][0]));
-    double fxx = ds(da(v[2][1], v[0][1]), dm(2., v[1][1]));
-    double fyy = ds(da(v[1][2], v[1][0]), dm(2., v[1][1]));
-    double fxy = dm(0.25, ds(ds(da(v[2][2], v[0][0]), v[2][0]), v[0][2]));
-    double den = ds(dm(fxy, fxy), dm(fxx, fyy));
-    *sx = ds(dm(fyy, fx), dm(fy, fxy)) / den;
-    *sy = ds(dm(fxx, fy), dm(fx, fxy)) / den;
-}
-
 template <int N>
 __global__ void __launch_bounds__(WinShape<N>::THREADS)
 k_window_fp32(WinArgs a) {
     using S = WinShape<N>;
     constexpr int TEAMS = S::TEAMS;
     extern __shared__ __align__(16) unsigned char sm[];
-    float4* s_mean = reinterpret_cast<float4*>(sm);
     unsigned long long* s_key = reinterpret_cast<unsigned long long*>(sm + 16 * TEAMS);
     unsigned* s_max = reinterpret_cast<unsigned*>(sm + 24 * TEAMS);
     float* s_g = reinterpret_cast<float*>(sm + 32 * TEAMS);
@@ -92,12 +67,18 @@ k_window_fp32(WinArgs a) {
     float2* buf = s_buf + team * S::BUF;
     float* ab = s_abs + team * N * N;
     const int nwork = *a.nwork;
+    if (ln == 0) {
+        s_max[2 * team] = 0u;
+        s_max[2 * team + 1] = 0u;
+        s_key[team] = 0ull;
+    }
     __syncthreads();
 
     for (int base = blockIdx.x * TEAMS; base < nwork; base += gridDim.x * TEAMS) {
         const int w = base + team;
         const bool valid = w < nwork;
-        const int pix = a.work[valid ? w : base];
+        const int wi = valid ? w : base;
+        const int pix = a.work[wi];
         int i, j, imin, jmin;
         if (a.direct) {
             imin = pix / a.ny;
@@ -111,25 +92,10 @@ k_window_fp32(WinArgs a) {
             jmin = box_start(j, a.ny, a.nsize);
         }
 
-        // FP64 local means from the box sums, split into float hi + lo
-        if (ln == 0) {
-            float2 m1 = make_float2(0.f, 0.f), m2 = m1;
-            if (!a.direct) {
-                const size_t b = (size_t)imin * a.bsw + jmin;
-                m1 = split_double(dm(a.bs1[b], a.inv_n2));
-                m2 = split_double(dm(a.bs2[b], a.inv_n2));
-            }
-            s_mean[team] = make_float4(m1.x, m1.y, m2.x, m2.y);
-            s_max[2 * team] = 0u;
-            s_max[2 * team + 1] = 0u;
-            s_key[team] = 0ull;
-        }
-        __syncthreads();
-
         // windowed, mean-subtracted column jj = ln of both frames: z = g1 + i g2
         float2 x[N];
         {
-            const float4 mm = s_mean[team];
+            const float4 mm = a.means ? __ldg(a.means + wi) : make_float4(0.f, 0.f, 0.f, 0.f);
             const float wc = s_g[ln + jmin - j + N];
             const float2* p1 = a.s1 + (size_t)imin * a.ny + jmin + ln;
             const float2* p2 = a.s2 + (size_t)imin * a.ny + jmin + ln;
@@ -163,6 +129,13 @@ k_window_fp32(WinArgs a) {
             buf[k * (N + 1) + ln] = x[dif_pos<N>(k)];
         });
         __syncthreads();
+        // every lane has read this window's scale factors and the previous
+        // window's peak key: clear both for the next use
+        if (ln == 0) {
+            s_max[2 * team] = 0u;
+            s_max[2 * team + 1] = 0u;
+            s_key[team] = 0ull;
+        }
         sfor<0, N>([&](auto jc) {
             constexpr int jj = decltype(jc)::value;
             x[jj] = buf[ln * (N + 1) + jj];
@@ -225,7 +198,9 @@ k_window_fp32(WinArgs a) {
         }
         __syncthreads();
 
-        if (ln == 0 && valid) {
+        // integer peak (all lanes decode the same key), then the team stores
+        // the peak record for k_fit
+        {
             int I, J;
             bool have;
             const float v0 = ab[0];
@@ -241,40 +216,17 @@ k_window_fp32(WinArgs a) {
                 I = have ? (int)(L / N) : N / 2;
                 J = have ? (int)(L % N) : N / 2;
             }
-            double sx = 0., sy = 0.;
-            if (have && I > 0 && I < N - 1 && J > 0 && J < N - 1) {
-                double v[3][3];
-#pragma unroll
-                for (int p = 0; p < 3; ++p)
-#pragma unroll
-                    for (int q = 0; q < 3; ++q) v[p][q] = (double)ab[(I - 1 + p) * N + (J - 1 + q)];
-                taylor_fit(v, &sx, &sy);
-            }
-            const double shx = ds(da((double)I, sx), (double)(N / 2));
-            const double shy = ds(da((double)J, sy), (double)(N / 2));
-            if (a.shx) {
-                a.shx[w] = shx;
-                a.shy[w] = shy;
-            }
-            if (a.vx) {
-                // transposed storage: vx from the fast-axis shift (flct.c:901-905)
-                double vxx = dm(dm(shy, a.deltinv), a.deltas);
-                double vyy = dm(dm(shx, a.deltinv), a.deltas);
-                double vmm = 1.;
-                if (a.gvx) {
-                    const int ic = (i - a.xoff) / a.skip, jc = (j - a.yoff) / a.skip;
-                    a.gvx[(size_t)ic * a.jcnt + jc] = vxx;
-                    a.gvy[(size_t)ic * a.jcnt + jc] = vyy;
+            const bool dofit = have && I > 0 && I < N - 1 && J > 0 && J < N - 1;
+            if (valid) {
+                // 10 words per record; teams narrower than 10 lanes loop
+                float* rec = reinterpret_cast<float*>(a.peaks + w);
+                for (int k = ln; k < 10; k += N) {
+                    if (k < 9) {
+                        rec[k] = dofit ? ab[(I - 1 + k / 3) * N + (J - 1 + k % 3)] : 0.f;
+                    } else {
+                        rec[9] = __uint_as_float(peak_meta(I, J, dofit));
+                    }
                 }
-                // the final xmiss reset (flct.c:1125-1133)
-                if (vxx == kXmiss) {
-                    vmm = 0.;
-                    vxx = 0.;
-                }
-                if (vyy == kXmiss) vyy = 0.;
-                a.vx[pix] = vxx;
-                a.vy[pix] = vyy;
-                a.vm[pix] = vmm;
             }
         }
     }
