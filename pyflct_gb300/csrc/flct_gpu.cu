@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "prepass.cuh"
+#include "warp.cuh"
 #include "window_fp32.cuh"
 
 using namespace flct;
@@ -692,18 +693,90 @@ flct_status flct_gpu_interpcc2d(flct_ctx* ctx, const double* fdata, double xmiss
     return FLCT_OK;
 }
 
+static flct_status warp_check(flct_ctx* ctx, const double* arr, const double* out, int nx, int ny) {
+    if (!arr || !out || nx < 1 || ny < 1) return fail(ctx, FLCT_ERR_ARG, "null pointer or empty image");
+    if (nx > kWarpMaxAxis || ny > kWarpMaxAxis)
+        return fail(ctx, FLCT_ERR_UNSUPPORTED, "warp axes are limited to %d points", kWarpMaxAxis);
+    if ((long long)nx * ny >= (1ll << 31)) return fail(ctx, FLCT_ERR_UNSUPPORTED, "image larger than 2^31 pixels");
+    return FLCT_OK;
+}
+
 flct_status flct_gpu_shift_frac2d(flct_ctx* ctx, const double* arr, double delx, double dely, double* out,
                                   int nx, int ny, int transp) {
-    (void)arr; (void)delx; (void)dely; (void)out; (void)nx; (void)ny; (void)transp;
     if (!ctx) return FLCT_ERR_ARG;
-    return fail(ctx, FLCT_ERR_UNSUPPORTED, "shift_frac2d is not available on the GPU path yet");
+    flct_status s = warp_check(ctx, arr, out, nx, ny);
+    if (s != FLCT_OK) return s;
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    const size_t n = (size_t)nx * ny;
+    ENSURE(ctx->b_f1, n * sizeof(double));
+    ENSURE(ctx->b_vx, n * sizeof(double));
+    ENSURE(ctx->b_s1, n * sizeof(float2));
+    ENSURE(ctx->b_s2, n * sizeof(float2));
+    ENSURE(ctx->b_aux1, (size_t)(nx + ny) * sizeof(float2) + 64);
+    ENSURE(ctx->b_aux2, (size_t)2 * std::max(nx, ny) * sizeof(double2));
+    float2* sx = (float2*)ctx->b_aux1.p;
+    float2* sy = sx + nx;
+    // warp.c:811-820: shifts normalised by the axis lengths; transp swaps them
+    const double dxarg = transp ? -dely / ((double)nx) : -delx / ((double)nx);
+    const double dyarg = transp ? -delx / ((double)ny) : -dely / ((double)ny);
+    CK(cudaMemcpyAsync(ctx->b_f1.p, arr, n * sizeof(double), cudaMemcpyHostToDevice, st));
+    CK(cudaEventRecord(ctx->ev[0], st));
+    CK(launch_shift_vector(nx, dxarg, (double2*)ctx->b_aux2.p, sx, st));
+    CK(launch_shift_vector(ny, dyarg, (double2*)ctx->b_aux2.p, sy, st));
+    CK(launch_axis_fast(0, true, ctx->b_f1.p, nx, ny, sy, (float2*)ctx->b_s1.p, st));
+    CK(launch_axis_slow(0, (const float2*)ctx->b_s1.p, ny, nx, sx, (float2*)ctx->b_s2.p, st));
+    CK(launch_real_part((const float2*)ctx->b_s2.p, (long)n, (double*)ctx->b_vx.p, st));
+    CK(cudaEventRecord(ctx->ev[1], st));
+    CK(cudaMemcpyAsync(out, ctx->b_vx.p, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    ctx->timing = flct_timing{};
+    ctx->timing.launches = 7;
+    ctx->timing.ms_total = ev_ms(ctx->ev[0], ctx->ev[1]);
+    return FLCT_OK;
 }
 
 flct_status flct_gpu_warp_frac2d(flct_ctx* ctx, const double* arr, const double* delx, const double* dely,
                                  double* out, int nx, int ny, int transp) {
-    (void)arr; (void)delx; (void)dely; (void)out; (void)nx; (void)ny; (void)transp;
     if (!ctx) return FLCT_ERR_ARG;
-    return fail(ctx, FLCT_ERR_UNSUPPORTED, "warp_frac2d is not available on the GPU path yet");
+    flct_status s = warp_check(ctx, arr, out, nx, ny);
+    if (s != FLCT_OK) return s;
+    if (!delx || !dely) return fail(ctx, FLCT_ERR_ARG, "null shift array");
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    const size_t n = (size_t)nx * ny;
+    ENSURE(ctx->b_f1, n * sizeof(double));
+    ENSURE(ctx->b_f2, n * sizeof(double));
+    ENSURE(ctx->b_vy, n * sizeof(double));
+    ENSURE(ctx->b_vx, n * sizeof(double));
+    ENSURE(ctx->b_s1, n * sizeof(float2));
+    ENSURE(ctx->b_s2, n * sizeof(float2));
+    ENSURE(ctx->b_means, n * sizeof(float4));
+    ENSURE(ctx->b_aux1, (size_t)(nx + ny) * sizeof(float2) + 64);
+    float2* twx = (float2*)ctx->b_aux1.p;
+    float2* twy = twx + nx;
+    CK(cudaMemcpyAsync(ctx->b_f1.p, arr, n * sizeof(double), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(ctx->b_f2.p, delx, n * sizeof(double), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(ctx->b_vy.p, dely, n * sizeof(double), cudaMemcpyHostToDevice, st));
+    CK(cudaEventRecord(ctx->ev[0], st));
+    // F = forward DFT of the image (warp.c:899-934)
+    CK(launch_twiddles(nx, -1, twx, st));
+    CK(launch_twiddles(ny, -1, twy, st));
+    CK(launch_axis_fast(1, true, ctx->b_f1.p, nx, ny, twy, (float2*)ctx->b_s1.p, st));
+    CK(launch_axis_slow(1, (const float2*)ctx->b_s1.p, ny, nx, twx, (float2*)ctx->b_s2.p, st));
+    CK(launch_warp_phase((const double*)ctx->b_f2.p, (const double*)ctx->b_vy.p, nx, ny, transp,
+                         (float4*)ctx->b_means.p, st));
+    CK(cudaEventRecord(ctx->ev[1], st));
+    CK(launch_warp_sum((const float2*)ctx->b_s2.p, (const float4*)ctx->b_means.p, nx, ny, (double*)ctx->b_vx.p, st));
+    CK(cudaEventRecord(ctx->ev[2], st));
+    CK(cudaMemcpyAsync(out, ctx->b_vx.p, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    ctx->timing = flct_timing{};
+    ctx->timing.launches = 6;
+    ctx->timing.ms_prepass = ev_ms(ctx->ev[0], ctx->ev[1]);
+    ctx->timing.ms_window = ev_ms(ctx->ev[1], ctx->ev[2]);
+    ctx->timing.ms_total = ev_ms(ctx->ev[0], ctx->ev[2]);
+    return FLCT_OK;
 }
 
 flct_status flct_gpu_velocity_batch(flct_ctx* ctx, int npairs, const flct_pair* pairs, void* stream) {

@@ -1,0 +1,22 @@
+// warp.cuh -- launchers for warp.cu (uniform shift and non-uniform warp).
+#pragma once
+#include <cuda_runtime.h>
+
+namespace flct {
+
+constexpr int kWarpMaxAxis = 16384;  // axis tables live in shared memory
+
+// mode 0: circulant tab[(c - k) mod L]; mode 1: DFT tab[(c k) mod L]
+cudaError_t launch_axis_fast(int mode, bool real_in, const void* in, int nrows, int L, const float2* tab,
+                             float2* out, cudaStream_t st);
+cudaError_t launch_axis_slow(int mode, const float2* in, int ncols, int L, const float2* tab, float2* out,
+                             cudaStream_t st);
+// scratch: 2n double2
+cudaError_t launch_shift_vector(int n, double darg, double2* scratch, float2* v, cudaStream_t st);
+cudaError_t launch_twiddles(int L, int sign, float2* tw, cudaStream_t st);
+cudaError_t launch_real_part(const float2* in, long n, double* out, cudaStream_t st);
+cudaError_t launch_warp_phase(const double* delx, const double* dely, int nx, int ny, int transp, float4* ph,
+                              cudaStream_t st);
+cudaError_t launch_warp_sum(const float2* F, const float4* ph, int nx, int ny, double* out, cudaStream_t st);
+
+}  // namespace flct

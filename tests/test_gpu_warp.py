@@ -1,0 +1,89 @@
+"""GPU parity of the warp program's transforms (shift_frac2d, warp_frac2d)
+against the FP64 oracle and the reference's golden outputs.
+
+The GPU evaluates the transforms in FP32 with FP64 phase bases and FP64
+circulant/twiddle tables; the tolerance is max |d| <= 2e-5 * max |image|
+(the golden files themselves are float32-rounded).
+"""
+import numpy as np
+import pytest
+
+import pyoracle as po
+from _golden import load
+
+pytestmark = pytest.mark.gpu
+REL = 2e-5
+
+
+@pytest.fixture(scope="module", autouse=True)
+def gpu():
+    from pyflct_gb300 import _lib, build
+    build.build()
+    return _lib.context(0)
+
+
+def close(a, b, scale):
+    return np.abs(a - b).max() <= REL * scale
+
+
+def test_golden_warp_and_shift():
+    from pyflct_gb300.flct import shift_frac2d, warp_frac2d
+    z = load("ref_warp_cases.npz")
+    img = z["warp_img"].astype(np.float64)
+    s = np.abs(img).max()
+    out = warp_frac2d(img, z["warp_dx"].astype(np.float64), z["warp_dy"].astype(np.float64))
+    assert close(out, z["warp_out"].astype(np.float64), s)
+    sx, sy = (float(v) for v in z["shift_xy"])
+    out = shift_frac2d(img, sx, sy)
+    assert close(out, z["shift_out"].astype(np.float64), s)
+
+
+@pytest.mark.parametrize("shape", [(37, 53), (64, 48), (101, 201), (16, 16), (5, 7)])
+@pytest.mark.parametrize("transp", [1, 0])
+def test_shift_sizes(shape, transp):
+    from pyflct_gb300.flct import shift_frac2d
+    rng = np.random.default_rng(shape[0] * 1000 + shape[1] + transp)
+    img = rng.standard_normal(shape) + 3.0
+    dx, dy = rng.uniform(-6, 6, 2)
+    got = shift_frac2d(img, dx, dy, transp)
+    ref = po.shift_frac2d(img, dx, dy, transp)
+    assert close(got, ref, np.abs(img).max())
+
+
+@pytest.mark.parametrize("shape", [(37, 53), (64, 48), (20, 31), (9, 8)])
+@pytest.mark.parametrize("transp", [1, 0])
+def test_warp_sizes(shape, transp):
+    from pyflct_gb300 import synth
+    from pyflct_gb300.flct import warp_frac2d
+    rng = np.random.default_rng(shape[0] * 77 + shape[1] + transp)
+    img = synth.kfield(shape, rng)
+    dfast, dslow = synth.smooth_shift(shape, rng, rms=1.5)
+    got = warp_frac2d(img, dfast, dslow, transp)
+    ref = po.warp_frac2d(img, dfast, dslow, transp)
+    assert close(got, ref, np.abs(img).max())
+
+
+def test_warp_dispatch_and_constant_field():
+    from pyflct_gb300.flct import FlctError, warp
+    rng = np.random.default_rng(4)
+    img = rng.standard_normal((24, 30))
+    a = warp(img, np.full(img.shape, 0.7), np.full(img.shape, -1.2))
+    b = warp(img, 0.7, -1.2)
+    assert np.abs(a - b).max() <= REL * np.abs(img).max()
+    with pytest.raises(FlctError) as e:
+        warp(img, np.zeros((3, 3)), np.zeros((3, 3)))
+    assert e.value.code == 11
+
+
+def test_warp_crop_256_and_shift_512():
+    """A 256^2 crop through the non-uniform warp and a 512^2 uniform shift."""
+    from pyflct_gb300 import synth
+    from pyflct_gb300.flct import shift_frac2d, warp_frac2d
+    rng = np.random.default_rng(20265)
+    img = synth.kfield((512, 512), rng)
+    got = shift_frac2d(img, 0.37, -2.6)
+    assert close(got, po.shift_frac2d(img, 0.37, -2.6), np.abs(img).max())
+    crop = img[100:356, 40:296]
+    dfast, dslow = synth.smooth_shift(crop.shape, rng, rms=0.3)
+    got = warp_frac2d(crop, dfast, dslow)
+    assert close(got, po.warp_frac2d(crop, dfast, dslow), np.abs(crop).max())
