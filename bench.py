@@ -7,7 +7,7 @@ Gaussian vortices, sigma = 8 (box 32), -s 4i (every 4th pixel correlated,
 the rest cubic-convolution interpolated), thresh = 0.  That is 65,536
 correlation windows and 1,048,576 output pixels per step.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--form fp32|auto]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--form tc_fp16|tc_bf16|fp32]
     python bench.py --impl reference ...   # the CPU implementation arm
 
 value  = correlation windows per second with inputs resident in HBM
@@ -163,6 +163,12 @@ def run_reference(a):
     print(json.dumps(line), flush=True)
 
 
+# MMA work the tensor-core form executes per 32x32 window: four M=128 GEMM
+# stages over 8 windows, each product as hi*hi + hi*lo + lo*hi.
+TC_MACS_PER_8 = 3 * (4 * 128 * 32 * 32 + 2 * 128 * 64 * 64 + 128 * 64 * 64 + 2 * 128 * 32 * 32)
+TC_FLOPS_PER_WINDOW = 2 * TC_MACS_PER_8 / 8
+
+
 def run_ours(a):
     import torch
     from pyflct_gb300 import _lib
@@ -180,35 +186,43 @@ def run_ours(a):
     dev = torch.device("cuda", local)
     d_f1 = torch.from_numpy(f1).to(dev)
     d_f2 = torch.from_numpy(f2).to(dev)
-    d_out = [torch.empty(NSIDE, NSIDE, dtype=torch.float64, device=dev) for _ in range(3)]
+    outs = {}
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
-    p = make_params(1.0, 1.0, SIGMA, skip=SKIP, form=a.form)
     stream = torch.cuda.current_stream(dev)
     sh = C.c_void_p(stream.cuda_stream)
-
-    def step():
-        ctx.check(lib.flct_gpu_velocity_device(
-            ctx.h, C.byref(p), C.c_void_p(d_f1.data_ptr()), C.c_void_p(d_f2.data_ptr()), NSIDE, NSIDE,
-            C.c_void_p(d_out[0].data_ptr()), C.c_void_p(d_out[1].data_ptr()),
-            C.c_void_p(d_out[2].data_ptr()), sh))
-
-    for _ in range(max(3, a.warmup)):
-        step()
-    torch.cuda.synchronize()
-    t = ctx.timing()
-    windows, launches, box = int(t.windows), int(t.launches), int(t.box)
 
     def barrier():
         if ws > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-           for _ in range(a.steps)]
-    win_ms = []
-    barrier()
-    wall0 = time.perf_counter()
-    with Clocks(local) as clk:
+    forms = [a.form] + [f for f in ("fp32", "tc_fp16", "tc_bf16") if f != a.form and not a.only]
+    res = {}
+    clk = None
+    for form in forms:
+        p = make_params(1.0, 1.0, SIGMA, skip=SKIP, form=form)
+        d_out = [torch.empty(NSIDE, NSIDE, dtype=torch.float64, device=dev) for _ in range(3)]
+        outs[form] = d_out
+
+        def step():
+            ctx.check(lib.flct_gpu_velocity_device(
+                ctx.h, C.byref(p), C.c_void_p(d_f1.data_ptr()), C.c_void_p(d_f2.data_ptr()), NSIDE, NSIDE,
+                C.c_void_p(d_out[0].data_ptr()), C.c_void_p(d_out[1].data_ptr()),
+                C.c_void_p(d_out[2].data_ptr()), sh))
+
+        for _ in range(max(3, a.warmup)):
+            step()
+        torch.cuda.synchronize()
+        t = ctx.timing()
+        windows, launches, box = int(t.windows), int(t.launches), int(t.box)
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(a.steps)]
+        win_ms = []
+        barrier()
+        wall0 = time.perf_counter()
+        clocks = Clocks(local) if form == a.form else None
+        if clocks:
+            clocks.__enter__()
         for k in range(a.steps):
             flush.zero_()  # L2 flush between steps (outside the step's events)
             evs[k][0].record(stream)
@@ -216,14 +230,22 @@ def run_ours(a):
             evs[k][1].record(stream)
             win_ms.append(ctx.timing().ms_window)
         barrier()
-    wall = time.perf_counter() - wall0
-    step_ms = [e0.elapsed_time(e1) for e0, e1 in evs]
-    total_ms = sum(step_ms)
-    if ws > 1:
-        tt = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(tt.item())
-    value = windows * a.steps * ws / (total_ms / 1e3)
+        if clocks:
+            clocks.__exit__()
+            clk = clocks
+        wall = time.perf_counter() - wall0
+        total_ms = sum(e0.elapsed_time(e1) for e0, e1 in evs)
+        if ws > 1:
+            tt = torch.tensor([total_ms], device=dev)
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            total_ms = float(tt.item())
+        res[form] = dict(value=windows * a.steps * ws / (total_ms / 1e3), ms_per_step=total_ms / a.steps,
+                         window_ms=statistics.mean(win_ms), windows=windows, launches=launches, box=box,
+                         wall_s=wall)
+
+    head = res[a.form]
+    windows, launches, box = head["windows"], head["launches"], head["box"]
+    p = make_params(1.0, 1.0, SIGMA, skip=SKIP, form=a.form)
 
     # end to end through the host-buffer entry point with pinned buffers
     pin = [torch.empty(NSIDE, NSIDE, dtype=torch.float64, pin_memory=True) for _ in range(5)]
@@ -245,7 +267,6 @@ def run_ours(a):
         e2e_step()
     barrier()
     e2e_s = time.perf_counter() - t0
-    # remove the flushes from the e2e clock: time them alone
     t1 = time.perf_counter()
     for _ in range(a.steps):
         flush.zero_()
@@ -260,39 +281,49 @@ def run_ours(a):
 
     pk, src = peaks()
     fl = window_flops(box)
-    win_avg = statistics.mean(win_ms) if win_ms else float("nan")
-    if a.form in ("fp32",):
-        # FP32 SIMT peak derived from the measured max SM clock:
-        # 152 SMs x 128 FP32 lanes x 2 flops (FMA)
-        nsm = torch.cuda.get_device_properties(dev).multi_processor_count
-        peak = nsm * 128 * 2 * pk.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
-        bound, peak_note = "fp32", f"derived: {nsm} SMs x 128 lanes x 2 x {pk.get('sm_max_mhz')} MHz ({src} clock)"
-    else:
+    nsm = torch.cuda.get_device_properties(dev).multi_processor_count
+
+    def roofline(form):
+        r = res[form]
+        achieved = r["windows"] * fl / (r["window_ms"] / 1e3) / 1e12
+        if form == "fp32":
+            peak = nsm * 128 * 2 * pk.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
+            return {"bound": "fp32", "kernel": f"k_window_fp32<{box}>", "achieved": achieved, "peak": peak,
+                    "unit": "TFLOP/s", "frac": achieved / peak, "flops_per_window": fl,
+                    "window_ms": r["window_ms"],
+                    "peak_source": f"derived: {nsm} SMs x 128 FP32 lanes x 2 x {pk.get('sm_max_mhz')} MHz "
+                                   f"({src} max clock); no FP32 figure in MEASURED_PEAKS.json"}
         peak = pk["bf16_tflops"]
-        bound, peak_note = "tensor", f"{src} bf16_tflops"
-    achieved = windows * fl / (win_avg / 1e3) / 1e12
-    traffic = None
+        tensor = r["windows"] * TC_FLOPS_PER_WINDOW / (r["window_ms"] / 1e3) / 1e12
+        return {"bound": "tensor", "kernel": f"k_window_tc32<{'half' if form == 'tc_fp16' else 'bf16'}>",
+                "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                "flops_per_window": fl, "window_ms": r["window_ms"],
+                "tensor_flops_per_window": TC_FLOPS_PER_WINDOW, "tensor_achieved": tensor,
+                "tensor_frac": tensor / peak, "peak_source": f"{src} bf16_tflops (dense 16-bit rate)"}
+
+    rl = roofline(a.form)
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tp):
         with open(tp) as fh:
-            traffic = json.load(fh).get(f"window_{a.form}_n{box}")
+            rl["traffic"] = json.load(fh).get(f"window_{a.form}_n{box}")
+    else:
+        rl["traffic"] = None
 
-    # accuracy against the FP64 oracle on the same frame
-    acc = None
-    cpu = None
+    # accuracy against the FP64 oracle on the same frame, and the CPU baseline
+    acc, cpu = {}, None
     if not a.no_cpu:
         po = oracle()
-        got = [x.cpu().numpy() for x in d_out]
         kw = dict(sigma=SIGMA, skip=4, interpolate=True)
         ref = po.velocity(f1, f2, nthreads=os.cpu_count(), **kw)
         comp = ref[2] == 1.0
-        dv = np.maximum(np.abs(got[0] - ref[0]), np.abs(got[1] - ref[1]))
-        acc = {"mask_equal": bool(np.array_equal(got[2], ref[2])),
-               "max_dv_computed": float(dv[comp].max()), "rms_dv_computed": float(np.sqrt(np.mean(dv[comp] ** 2))),
-               "n_over_1e-3": int((dv[comp] > 1e-3).sum()),
-               "max_dv_interp": float(dv[ref[2] == 0.5].max()),
-               "median_dv_interp": float(np.median(dv[ref[2] == 0.5]))}
-        # the CPU baseline: the same frame, one thread
+        for form, d_out in outs.items():
+            got = [x.cpu().numpy() for x in d_out]
+            dv = np.maximum(np.abs(got[0] - ref[0]), np.abs(got[1] - ref[1]))
+            acc[form] = {"mask_equal": bool(np.array_equal(got[2], ref[2])),
+                         "max_dv_computed": float(dv[comp].max()),
+                         "rms_dv_computed": float(np.sqrt(np.mean(dv[comp] ** 2))),
+                         "n_over_1e-3": int((dv[comp] > 1e-3).sum()),
+                         "max_dv_interp": float(dv[ref[2] == 0.5].max())}
         t0 = time.perf_counter()
         po.velocity(f1, f2, nthreads=1, **kw)
         cdt = time.perf_counter() - t0
@@ -301,25 +332,30 @@ def run_ours(a):
                          "of flct.c over the project double FFT (FFTW unavailable)"}
 
     line = {
-        "metric": METRIC, "value": value, "unit": "windows/s", "n_gpus": ws, "steps": a.steps,
-        "warmup": a.warmup, "ms_per_step": total_ms / a.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32" if a.form == "fp32" else "f16x2",
+        "metric": METRIC, "value": head["value"], "unit": "windows/s", "n_gpus": ws, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": {"fp32": "f32", "tc_fp16": "f16x2 split (f32 accumulate)",
+                  "tc_bf16": "bf16x2 split (f32 accumulate)"}[a.form],
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "form": a.form, "box": box, "windows_per_step": windows,
                    "output_pixels_per_step": npx, "l2": "flushed (256 MiB write) between steps",
                    "parallelism": f"replicas x{ws}"},
         "e2e": {"value": e2e_val, "unit": "windows/s", "h2d_bytes_per_step": 2 * npx * 8,
                 "d2h_bytes_per_step": 3 * npx * 8},
-        "roofline": {"bound": bound, "kernel": f"k_window_{a.form}<{box}>", "achieved": achieved,
-                     "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
-                     "flops_per_window": fl, "window_ms": win_avg, "peak_source": peak_note},
+        "roofline": rl,
+        "forms": {f: {"value": r["value"], "ms_per_step": r["ms_per_step"], "window_ms": r["window_ms"]}
+                  for f, r in res.items()},
         "cpu_baseline": cpu,
         "accuracy_vs_fp64_oracle": acc,
         "gpu_launches": launches * a.steps,
-        "clocks": clk.summary(),
-        "wall_s_timed": wall,
-        "output_pixels_per_s": value / windows * npx,
+        "clocks": clk.summary() if clk else None,
+        "wall_s_timed": head["wall_s"],
+        "output_pixels_per_s": head["value"] / windows * npx,
     }
+    if "fp32" in res and a.form != "fp32":
+        line["speedup_over_fp32_form"] = head["value"] / res["fp32"]["value"]
+        line["window_kernel_speedup_over_fp32"] = res["fp32"]["window_ms"] / head["window_ms"]
     print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
@@ -331,7 +367,8 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--form", default="fp32", choices=["fp32", "tc_fp16", "tc_bf16", "auto"])
+    ap.add_argument("--form", default="tc_fp16", choices=["fp32", "tc_fp16", "tc_bf16"])
+    ap.add_argument("--only", action="store_true", help="time only --form (skip the other forms)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the oracle accuracy and CPU baseline")
     a = ap.parse_args()
     if a.impl == "reference":

@@ -20,6 +20,7 @@
 #include "prepass.cuh"
 #include "warp.cuh"
 #include "window_fp32.cuh"
+#include "window_tc.cuh"
 
 using namespace flct;
 
@@ -83,9 +84,12 @@ struct flct_ctx {
     Buf b_f1, b_f2, b_vx, b_vy, b_vm, b_aux1, b_aux2, b_means, b_peaks, b_hrow;
     std::vector<Buf*> all() {
         return {&b_s1, &b_s2, &b_work, &b_ctr, &b_r1, &b_r2, &b_b1, &b_b2, &b_gvx, &b_gvy, &b_ix,
-                &b_iy, &b_f1, &b_f2, &b_vx, &b_vy, &b_vm, &b_aux1, &b_aux2, &b_means, &b_peaks, &b_hrow};
+                &b_iy, &b_f1, &b_f2, &b_vx, &b_vy, &b_vm, &b_aux1, &b_aux2, &b_means, &b_peaks, &b_hrow, &b_tc};
     }
     int bps[sizeof(kWin) / sizeof(kWin[0])] = {0};
+    int bps_tc[2] = {0, 0};
+    Buf b_tc;              // tensor-core DFT matrices (b1 32x32, b2 64x64 floats)
+    bool tc_ready = false;
     bool pending = false;  // a velocity call's events await collection
 };
 
@@ -200,6 +204,83 @@ int win_grid(flct_ctx* ctx, int n) {
     return ctx->nsm * ctx->bps[k];
 }
 
+// The tensor-core form's constant matrices, built once per context in FP64:
+// b1[c][j] (S1: real input -> half spectrum columns) and b2[n][k] (S2:
+// complex DFT along the other axis, re/im interleaved by halves).
+flct_status ensure_tc_tables(flct_ctx* ctx) {
+    if (ctx->tc_ready) return FLCT_OK;
+    ENSURE(ctx->b_tc, (32 * 32 + 64 * 64) * sizeof(float));
+    std::vector<float> t(32 * 32 + 64 * 64);
+    const double tw = 2.0 * 3.14159265358979323846 / 32.0;
+    for (int c = 0; c < 32; ++c)
+        for (int j = 0; j < 32; ++j) {
+            const double v = (c <= 16) ? std::cos(tw * ((c * j) % 32)) : -std::sin(tw * (((c - 16) * j) % 32));
+            t[c * 32 + j] = (float)v;
+        }
+    float* b2 = t.data() + 32 * 32;
+    for (int n = 0; n < 64; ++n)
+        for (int k = 0; k < 64; ++k) {
+            const int pp = n / 32, kx = n % 32, pk = k / 32, i = k % 32;
+            const double th = tw * ((kx * i) % 32);
+            double v;
+            if (pk == 0 && pp == 0) v = std::cos(th);
+            else if (pk == 1 && pp == 0) v = std::sin(th);
+            else if (pk == 0 && pp == 1) v = -std::sin(th);
+            else v = std::cos(th);
+            b2[n * 64 + k] = (float)v;
+        }
+    CK(cudaMemcpy(ctx->b_tc.p, t.data(), t.size() * sizeof(float), cudaMemcpyHostToDevice));
+    ctx->tc_ready = true;
+    return FLCT_OK;
+}
+
+// Resolve FLCT_FORM_AUTO and check that the form exists for box size n.
+flct_status pick_form(flct_ctx* ctx, int requested, int n, int* form) {
+    int f = requested;
+    if (f == FLCT_FORM_AUTO) f = (n == 32) ? FLCT_FORM_TC_FP16 : FLCT_FORM_FP32;
+    if ((f == FLCT_FORM_TC_FP16 || f == FLCT_FORM_TC_BF16) && n != 32)
+        return fail(ctx, FLCT_ERR_UNSUPPORTED, "the tensor-core form is built for 32x32 boxes (sigma 8); box %d", n);
+    if (f < 0 || f > FLCT_FORM_TC_BF16) return fail(ctx, FLCT_ERR_ARG, "unknown window form %d", requested);
+    *form = f;
+    return FLCT_OK;
+}
+
+// Launch the window kernel of the chosen form on the prepared work list.
+flct_status launch_windows(flct_ctx* ctx, int form, const WinEntry* we, int n, const WinArgs& wa, unsigned* status,
+                           cudaStream_t st) {
+    if (form == FLCT_FORM_FP32) {
+        CK(we->launch(wa, win_grid(ctx, n), st));
+        return FLCT_OK;
+    }
+    flct_status s = ensure_tc_tables(ctx);
+    if (s != FLCT_OK) return s;
+    TcArgs ta{};
+    ta.s1 = wa.s1;
+    ta.s2 = wa.s2;
+    ta.means = wa.means;
+    ta.work = wa.work;
+    ta.nwork = wa.nwork;
+    ta.nx = wa.nx;
+    ta.ny = wa.ny;
+    ta.nsize = wa.nsize;
+    ta.direct = wa.direct;
+    ta.use_filter = wa.use_filter;
+    ta.peaks = wa.peaks;
+    ta.b1 = (const float*)ctx->b_tc.p;
+    ta.b2 = (const float*)ctx->b_tc.p + 32 * 32;
+    ta.status = status;
+    for (int k = 0; k < 2 * kMaxBox + 1; ++k) ta.gauss[k] = wa.gauss[k];
+    for (int k = 0; k < kMaxBox; ++k) ta.filt2[k] = wa.filt2[k];
+    const int which = (form == FLCT_FORM_TC_BF16) ? 1 : 0;
+    if (ctx->bps_tc[which] == 0)
+        ctx->bps_tc[which] = std::max(1, which ? window_tc32_blocks_per_sm<__nv_bfloat16>()
+                                               : window_tc32_blocks_per_sm<__half>());
+    const int grid = ctx->nsm * ctx->bps_tc[which];
+    if (which) CK(launch_window_tc32<__nv_bfloat16>(ta, grid, st));
+    else CK(launch_window_tc32<__half>(ta, grid, st));
+    return FLCT_OK;
+}
+
 }  // namespace
 
 // ===================================================================== ABI
@@ -304,8 +385,9 @@ flct_status flct_gpu_velocity_device(flct_ctx* ctx, const flct_params* p, const 
     const int n = d.n;
     const WinEntry* we = find_win(n);
     if (!we) return fail(ctx, FLCT_ERR_UNSUPPORTED, "box size %d (sigma %g) has no GPU kernel", n, p->sigma);
-    if (p->form != FLCT_FORM_FP32 && p->form != FLCT_FORM_AUTO)
-        return fail(ctx, FLCT_ERR_UNSUPPORTED, "window form %d is not available yet", p->form);
+    int form = FLCT_FORM_FP32;
+    s = pick_form(ctx, p->form, n, &form);
+    if (s != FLCT_OK) return s;
 
     const size_t npx = (size_t)nx * ny;
     const int W = ny - n + 1, H = nx - n + 1;
@@ -412,8 +494,8 @@ flct_status flct_gpu_velocity_device(flct_ctx* ctx, const flct_params* p, const 
     wa.ny = ny;
     wa.nsize = d.nsize;
     wa.peaks = (PeakRec*)ctx->b_peaks.p;
-    const int grid = win_grid(ctx, n);
-    CK(we->launch(wa, grid, st));
+    s = launch_windows(ctx, form, we, n, wa, d_status, st);
+    if (s != FLCT_OK) return s;
     ++launches;
     CK(cudaEventRecord(ctx->ev[2], st));
     {
@@ -486,7 +568,7 @@ flct_status flct_gpu_velocity_device(flct_ctx* ctx, const flct_params* p, const 
     ctx->timing = flct_timing{};
     ctx->timing.launches = launches;
     ctx->timing.box = n;
-    ctx->timing.form = FLCT_FORM_FP32;
+    ctx->timing.form = form;
     ctx->pending = true;
     return FLCT_OK;
 }
@@ -509,6 +591,8 @@ static flct_status collect_timing(flct_ctx* ctx) {
     ctx->timing.ms_total = ev_ms(ctx->ev[0], ctx->ev[3]);
     if (status & kStatusRange)
         return fail(ctx, FLCT_ERR_UNSUPPORTED, "an input magnitude exceeds the FP32 range of the GPU kernels");
+    if (status & kStatusTimeout)
+        return fail(ctx, FLCT_ERR_TIMEOUT, "a tensor-core stage did not complete within its wait limit");
     return FLCT_OK;
 }
 
@@ -556,8 +640,11 @@ flct_status flct_gpu_cross_cor_batch(flct_ctx* ctx, const double* g1, const doub
     if (nwin == 0) return FLCT_OK;
     const WinEntry* we = find_win(n);
     if (!we) return fail(ctx, FLCT_ERR_UNSUPPORTED, "window size %d has no GPU kernel", n);
-    if (form != FLCT_FORM_FP32 && form != FLCT_FORM_AUTO)
-        return fail(ctx, FLCT_ERR_UNSUPPORTED, "window form %d is not available yet", form);
+    int fsel = FLCT_FORM_FP32;
+    {
+        flct_status fs = pick_form(ctx, form, n, &fsel);
+        if (fs != FLCT_OK) return fs;
+    }
     if (filter && !(kr > 0.)) return fail(ctx, FLCT_ERR_UNSUPPORTED, "-k with kr <= 0 is not available on the GPU path");
     if ((long long)nwin * n * n >= (1ll << 31)) return fail(ctx, FLCT_ERR_UNSUPPORTED, "too many windows in one batch");
     CK(cudaSetDevice(ctx->device));
@@ -621,7 +708,10 @@ flct_status flct_gpu_cross_cor_batch(flct_ctx* ctx, const double* g1, const doub
     wa.direct = 1;
     ENSURE(ctx->b_peaks, (size_t)nwin * sizeof(PeakRec));
     wa.peaks = (PeakRec*)ctx->b_peaks.p;
-    CK(we->launch(wa, win_grid(ctx, n), st));
+    {
+        flct_status ls = launch_windows(ctx, fsel, we, n, wa, (unsigned*)(ctr + 4), st);
+        if (ls != FLCT_OK) return ls;
+    }
     CK(cudaEventRecord(ctx->ev[2], st));
     FitArgs fa{};
     fa.work = (const int*)ctx->b_work.p;
@@ -642,8 +732,14 @@ flct_status flct_gpu_cross_cor_batch(flct_ctx* ctx, const double* g1, const doub
     ctx->timing.windows = nwin;
     ctx->timing.launches = 3;
     ctx->timing.box = n;
-    ctx->timing.form = FLCT_FORM_FP32;
+    ctx->timing.form = fsel;
     ctx->timing.ms_window = ev_ms(ctx->ev[1], ctx->ev[2]);
+    {
+        unsigned status = 0;
+        CK(cudaMemcpy(&status, ctr + 4, sizeof(unsigned), cudaMemcpyDeviceToHost));
+        if (status & kStatusTimeout)
+            return fail(ctx, FLCT_ERR_TIMEOUT, "a tensor-core stage did not complete within its wait limit");
+    }
     ctx->timing.ms_total = ev_ms(ctx->ev[0], ctx->ev[2]);
     return FLCT_OK;
 }
