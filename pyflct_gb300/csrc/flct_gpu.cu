@@ -206,7 +206,7 @@ int win_grid(flct_ctx* ctx, int n) {
 
 // The tensor-core form's constant matrices, built once per context in FP64:
 // b1[c][j] (S1: real input -> half spectrum columns) and b2[n][k] (S2:
-// complex DFT along the other axis, re/im interleaved by halves).
+// complex DFT along the other axis, re/im by halves, columns in tc_kx order).
 flct_status ensure_tc_tables(flct_ctx* ctx) {
     if (ctx->tc_ready) return FLCT_OK;
     ENSURE(ctx->b_tc, (32 * 32 + 64 * 64) * sizeof(float));
@@ -220,7 +220,8 @@ flct_status ensure_tc_tables(flct_ctx* ctx) {
     float* b2 = t.data() + 32 * 32;
     for (int n = 0; n < 64; ++n)
         for (int k = 0; k < 64; ++k) {
-            const int pp = n / 32, kx = n % 32, pk = k / 32, i = k % 32;
+            // output column q holds wavenumber tc_kx(q): mirror pairs adjacent
+            const int pp = n / 32, kx = tc_kx(n % 32), pk = k / 32, i = k % 32;
             const double th = tw * ((kx * i) % 32);
             double v;
             if (pk == 0 && pp == 0) v = std::cos(th);

@@ -16,9 +16,11 @@
 //       rows (window, image, i), K = j (32), N = c (32)            4 tiles
 //   S2  along i on 16 packed complex columns per image:
 //       column 0 = T[:,0] + i T[:,16] (separated later by Hermitian symmetry),
-//       column kc = T[:,kc] (kc = 1..15); rows (window, image, kc),
-//       K = (re/im, i) (64), N = (re/im, kx) (64)                   2 tiles
-//   product conj(A) B filt^2 per (kx, ky), images exchanged between lanes
+//       column kc = T[:,kc] (kc = 1..15); rows (window, kc), one N = 64 GEMM
+//       per image into adjacent TMEM columns, K = (re/im, i) (64),
+//       N = (re/im, kx) (64)                                        1 tile
+//   product conj(A) B filt^2 per (kx, ky): one lane holds both images'
+//       spectra of its (window, kc) row
 //   S3  inverse along kx on 16 packed columns per window (ky = 0 and 16
 //       share column 0: both inverse transforms are real),
 //       rows (window, kc), K = (re/im, kx), N = (re/im, i)          1 tile
@@ -33,6 +35,7 @@
 #include <cuda_fp16.h>
 
 #include "common.cuh"
+#include "fft_reg.cuh"
 #include "tc_ptx.cuh"
 #include "window_common.cuh"
 
@@ -49,11 +52,20 @@ struct TcArgs {
     int use_filter;
     PeakRec* peaks;
     const float* b1;      // [c][j] 32 x 32: S1 matrix, row = output column c
-    const float* b2;      // [n][k] 64 x 64: S2 matrix, n = (re/im, kx), k = (re/im, i)
+    const float* b2;      // [n][k] 64 x 64: S2 matrix, n = (re/im, q), k = (re/im, i), kx = tc_kx(q)
     unsigned* status;
     float gauss[2 * kMaxBox + 1];
     float filt2[kMaxBox];
 };
+
+// Column order of S2's output (and S3's input): kx and -kx adjacent, so each
+// half of a spectrum row holds complete mirror pairs:
+//   q = 0 -> kx 0, q = 1 -> kx 16, q = 2j -> kx j, q = 2j+1 -> kx 32-j.
+__host__ __device__ constexpr int tc_kx(int q) {
+    return q == 0 ? 0 : (q == 1 ? 16 : ((q % 2 == 0) ? q / 2 : 32 - q / 2));
+}
+// Position of -kx for the column at position q.
+__host__ __device__ constexpr int tc_mirror(int q) { return q < 2 ? q : ((q % 2 == 0) ? q + 1 : q - 1); }
 
 template <typename T>
 struct Split16;
@@ -74,6 +86,13 @@ struct Split16<__half> {
         hi = make_uint4(h[0], h[1], h[2], h[3]);
         lo = make_uint4(l[0], l[1], l[2], l[3]);
     }
+    __device__ static __forceinline__ void pair(float v0, float v1, uint32_t& hi, uint32_t& lo) {
+        const __half2 a = __floats2half2_rn(v0, v1);
+        const float2 b = __half22float2(a);
+        const __half2 c = __floats2half2_rn(v0 - b.x, v1 - b.y);
+        hi = *reinterpret_cast<const uint32_t*>(&a);
+        lo = *reinterpret_cast<const uint32_t*>(&c);
+    }
 };
 template <>
 struct Split16<__nv_bfloat16> {
@@ -91,6 +110,13 @@ struct Split16<__nv_bfloat16> {
         hi = make_uint4(h[0], h[1], h[2], h[3]);
         lo = make_uint4(l[0], l[1], l[2], l[3]);
     }
+    __device__ static __forceinline__ void pair(float v0, float v1, uint32_t& hi, uint32_t& lo) {
+        const __nv_bfloat162 a = __floats2bfloat162_rn(v0, v1);
+        const float2 b = __bfloat1622float2(a);
+        const __nv_bfloat162 c = __floats2bfloat162_rn(v0 - b.x, v1 - b.y);
+        hi = *reinterpret_cast<const uint32_t*>(&a);
+        lo = *reinterpret_cast<const uint32_t*>(&c);
+    }
 };
 
 struct TcSmem {
@@ -105,9 +131,8 @@ struct TcSmem {
     static constexpr int off_b2lo = off_b2hi + B2;
     static constexpr int off_misc = off_b2lo + B2;  // 86016
     static constexpr int misc = 1024;
-    // + 1024 for aligning the base; + 16 KB so that descriptor reads stay
-    // inside the allocation under any stride interpretation
-    static constexpr int bytes = off_misc + misc + 1024 + 16384;
+    // + 1024 for aligning the base
+    static constexpr int bytes = off_misc + misc + 1024;
 };
 
 __device__ __forceinline__ float warp_max(float v) {
@@ -225,7 +250,9 @@ __global__ void __launch_bounds__(128) k_window_tc32(TcArgs a) {
 
         // ---- phase 0: windows -> A1 (K-major, 4 tiles of 128 rows) -------
         {
-            const int wl = t >> 6, img = (t >> 5) & 1, i = t & 31;
+            // warp (wl, img) of each tile; lane = column j, rows read
+            // cooperatively (coalesced), values scattered into the K-major rows
+            const int wl = warp >> 1, img = warp & 1;
 #pragma unroll 1
             for (int tile = 0; tile < 4; ++tile) {
                 const int w = 2 * tile + wl;
@@ -244,34 +271,40 @@ __global__ void __launch_bounds__(128) k_window_tc32(TcArgs a) {
                 }
                 const float4 mm = s_mean[w];
                 const float mh = img ? mm.z : mm.x, ml = img ? mm.w : mm.y;
-                const float2* src = (img ? a.s2 : a.s1) + (size_t)(imin + i) * a.ny + jmin;
-                const float gr = s_g[i + imin - ic + N];
-                const float* gc = s_g + (jmin - jc + N);
+                const float2* src = (img ? a.s2 : a.s1) + (size_t)imin * a.ny + jmin + lane;
+                const float* gr = s_g + (imin - ic + N);
+                const float gc = s_g[lane + jmin - jc + N];
                 float x[32];
                 float mx = 0.f;
 #pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    const float2 u = __ldg(src + j);
-                    x[j] = ((u.x - mh) + (u.y - ml)) * (gr * gc[j]);
-                    mx = fmaxf(mx, fabsf(x[j]));
+                for (int i = 0; i < 32; ++i) {
+                    const float2 u = __ldg(src + (size_t)i * a.ny);
+                    x[i] = ((u.x - mh) + (u.y - ml)) * (gr[i] * gc);
+                    mx = fmaxf(mx, fabsf(x[i]));
                 }
                 const float sc = pow2_scale(__float_as_uint(warp_max(mx)));
+                // even lanes store (j, j+1) as one 32-bit hi and one lo word
+                const int rowbase = tile * 8192 + (wl * 64 + img * 32) / 8 * 512 + (lane % 8) * 2 + (lane / 8) * 128;
 #pragma unroll
-                for (int j = 0; j < 32; ++j) x[j] *= sc;
-                const int rowoff = tile * 8192 + (t % 8) * 16 + (t / 8) * 512;
-#pragma unroll
-                for (int kc = 0; kc < 4; ++kc) {
-                    uint4 hi, lo;
-                    SP::run(x + 8 * kc, hi, lo);
-                    *reinterpret_cast<uint4*>(Ahi + rowoff + kc * 128) = hi;
-                    *reinterpret_cast<uint4*>(Alo + rowoff + kc * 128) = lo;
+                for (int i = 0; i < 32; ++i) {
+                    const float v = x[i] * sc;
+                    const float vn = __shfl_down_sync(0xffffffffu, v, 1);
+                    if ((lane & 1) == 0) {
+                        uint32_t hi, lo;
+                        SP::pair(v, vn, hi, lo);
+                        const int off = rowbase + (i % 8) * 16 + (i / 8) * 512;
+                        *reinterpret_cast<uint32_t*>(Ahi + off) = hi;
+                        *reinterpret_cast<uint32_t*>(Alo + off) = lo;
+                    }
                 }
             }
         }
         to_mma();
         if (t == 0) {
-            for (int tile = 0; tile < 4; ++tile)
-                for (int s = 0; s < 2; ++s)
+            // consecutive MMAs go to different accumulators (tiles) so that
+            // the tensor pipe can overlap them
+            for (int s = 0; s < 2; ++s)
+                for (int tile = 0; tile < 4; ++tile)
                     mma3(tmem + 32 * tile, tc::desc(ahi + tile * 8192 + s * 256, 128, 512),
                          tc::desc(alo + tile * 8192 + s * 256, 128, 512), tc::desc(b1hi + s * 256, 128, 512),
                          tc::desc(b1lo + s * 256, 128, 512), id1, s > 0);
@@ -290,9 +323,8 @@ __global__ void __launch_bounds__(128) k_window_tc32(TcArgs a) {
                 float d[32];
                 tc::tmem_ld32(tmem + lane_base + 32 * tile, d);
                 const int w = 2 * tile + wl;
-                const int t2 = w >> 2, wl2 = w & 3;
-                const int mcore = (wl2 * 32 + img * 16) / 8;  // first of two m-cores
-                const int base2 = t2 * 16384 + mcore * 128 + (i % 8) * 16;
+                // rows m = w*16 + kc (two m-cores), K block of this image
+                const int base2 = img * 16384 + (2 * w) * 128 + (i % 8) * 16;
 #pragma unroll
                 for (int part = 0; part < 2; ++part) {
                     const int off = base2 + (part * 4 + i / 8) * 2048;
@@ -309,10 +341,10 @@ __global__ void __launch_bounds__(128) k_window_tc32(TcArgs a) {
         tc::fence_before();
         to_mma();
         if (t == 0) {
-            for (int t2 = 0; t2 < 2; ++t2)
-                for (int s = 0; s < 4; ++s)
-                    mma3(tmem + 128 + 64 * t2, tc::desc(ahi + t2 * 16384 + s * 4096, 2048, 128),
-                         tc::desc(alo + t2 * 16384 + s * 4096, 2048, 128), tc::desc(b2hi + s * 256, 128, 1024),
+            for (int s = 0; s < 4; ++s)
+                for (int img = 0; img < 2; ++img)
+                    mma3(tmem + 128 + 64 * img, tc::desc(ahi + img * 16384 + s * 4096, 2048, 128),
+                         tc::desc(alo + img * 16384 + s * 4096, 2048, 128), tc::desc(b2hi + s * 256, 128, 1024),
                          tc::desc(b2lo + s * 256, 128, 1024), id2, s > 0);
             tc::commit(s_mbar);
         }
@@ -323,75 +355,59 @@ __global__ void __launch_bounds__(128) k_window_tc32(TcArgs a) {
 
         // ---- phase 2: spectra -> conj(A) B filt^2 -> A3 (K-major) --------
         {
-            const int img = lane >> 4, kc = lane & 15;
-#pragma unroll 1
-            for (int t2 = 0; t2 < 2; ++t2) {
-                float zr[32], zi[32];
-                tc::tmem_ld32(tmem + lane_base + 128 + 64 * t2, zr);
-                tc::tmem_ld32(tmem + lane_base + 128 + 64 * t2 + 32, zi);
-                float pr[32], pi[32];
+            // row t = (window w, packed column kc); both images in one lane
+            const int kc = t & 15;
+            const float h0 = kc ? 1.0f : 0.5f, z6 = kc ? 0.0f : 0.5f;
+            const float fk0 = kc ? s_f[kc] : s_f[0], fk6 = s_f[H];
+            float ur[32], ui[32];
+            float mx = 0.f;
+            sfor<0, 2>([&](auto hc) {
+                constexpr int half = decltype(hc)::value;
+                // columns q in [16 half, 16 half + 16): complete (kx, -kx) pairs
+                float ar[16], ai[16], br[16], bi[16];
+                tc::tmem_ld16(tmem + lane_base + 128 + 16 * half, ar);
+                tc::tmem_ld16(tmem + lane_base + 160 + 16 * half, ai);
+                tc::tmem_ld16(tmem + lane_base + 192 + 16 * half, br);
+                tc::tmem_ld16(tmem + lane_base + 224 + 16 * half, bi);
+                sfor<0, 16>([&](auto qc) {
+                    constexpr int qq = decltype(qc)::value;
+                    constexpr int q = 16 * half + qq;
+                    constexpr int mq = tc_mirror(q) - 16 * half;  // mirror within this half
+                    const float Ar = ar[qq], Ai = ai[qq], Br = br[qq], Bi = bi[qq];
+                    const float sr = kc ? 0.0f : ar[mq], si = kc ? 0.0f : ai[mq];
+                    const float tr = kc ? 0.0f : br[mq], ti = kc ? 0.0f : bi[mq];
+                    const float a0r = h0 * (Ar + sr), a0i = h0 * (Ai - si);
+                    const float a6r = z6 * (Ai + si), a6i = z6 * (sr - Ar);
+                    const float b0r = h0 * (Br + tr), b0i = h0 * (Bi - ti);
+                    const float b6r = z6 * (Bi + ti), b6i = z6 * (tr - Br);
+                    const float fx = s_f[tc_kx(q)];
+                    const float f0 = fx * fk0, f6 = fx * fk6;
+                    const float c0r = f0 * (a0r * b0r + a0i * b0i), c0i = f0 * (a0r * b0i - a0i * b0r);
+                    const float c6r = f6 * (a6r * b6r + a6i * b6i), c6i = f6 * (a6r * b6i - a6i * b6r);
+                    ur[q] = c0r - c6i;  // u = C0 + i C16 (C16 = 0 for kc > 0)
+                    ui[q] = c0i + c6r;
+                    mx = fmaxf(mx, fmaxf(fabsf(ur[q]), fabsf(ui[q])));
+                });
+            });
 #pragma unroll
-                for (int k = 0; k < 32; ++k) {
-                    pr[k] = __shfl_xor_sync(0xffffffffu, zr[k], 16);
-                    pi[k] = __shfl_xor_sync(0xffffffffu, zi[k], 16);
-                }
-                // A = image 1 spectrum, B = image 2; this lane handles kx in
-                // [16 img, 16 img + 16) (static register indices via selects)
-                float ur[16], ui[16];
-                const float fk = s_f[kc];
+            for (int o = 8; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+            const float sc = pow2_scale(__float_as_uint(mx));
 #pragma unroll
-                for (int q = 0; q < 16; ++q) {
-                    const int k0 = q, k1 = q + 16;               // kx for img 0 / img 1
-                    const int m0 = (32 - k0) & 31, m1 = (32 - k1) & 31;  // -kx
-                    const float ar = img ? pr[k1] : zr[k0], ai = img ? pi[k1] : zi[k0];
-                    const float br = img ? zr[k1] : pr[k0], bi = img ? zi[k1] : pi[k0];
-                    const int kx = img ? k1 : k0;
-                    const float fx = s_f[kx];
-                    if (kc != 0) {
-                        const float f = fx * fk;
-                        ur[q] = f * (ar * br + ai * bi);
-                        ui[q] = f * (ar * bi - ai * br);
-                    } else {
-                        // column 0 carries ky = 0 (real part) and ky = 16 (imag
-                        // part): P = Y0 + i Y16 with Y0, Y16 Hermitian in kx
-                        const float amr = img ? pr[m1] : zr[m0], ami = img ? pi[m1] : zi[m0];
-                        const float bmr = img ? zr[m1] : pr[m0], bmi = img ? zi[m1] : pi[m0];
-                        // Y0 = (P + conj(P-))/2, Y16 = (P - conj(P-))/(2i)
-                        const float a0r = 0.5f * (ar + amr), a0i = 0.5f * (ai - ami);
-                        const float a6r = 0.5f * (ai + ami), a6i = -0.5f * (ar - amr);
-                        const float b0r = 0.5f * (br + bmr), b0i = 0.5f * (bi - bmi);
-                        const float b6r = 0.5f * (bi + bmi), b6i = -0.5f * (br - bmr);
-                        const float f0 = fx * s_f[0], f6 = fx * s_f[H];
-                        const float c0r = f0 * (a0r * b0r + a0i * b0i), c0i = f0 * (a0r * b0i - a0i * b0r);
-                        const float c6r = f6 * (a6r * b6r + a6i * b6i), c6i = f6 * (a6r * b6i - a6i * b6r);
-                        // pack u = C0 + i C16 (both inverse transforms are real)
-                        ur[q] = c0r - c6i;
-                        ui[q] = c0i + c6r;
-                    }
-                }
-                float mx = 0.f;
+            for (int q = 0; q < 32; ++q) {
+                ur[q] *= sc;
+                ui[q] *= sc;
+            }
+            const int rowoff = (t % 8) * 16 + (t / 8) * 1024;
 #pragma unroll
-                for (int q = 0; q < 16; ++q) mx = fmaxf(mx, fmaxf(fabsf(ur[q]), fabsf(ui[q])));
-                const float sc = pow2_scale(__float_as_uint(warp_max(mx)));
+            for (int part = 0; part < 2; ++part) {
+                const float* src = part ? ui : ur;
 #pragma unroll
-                for (int q = 0; q < 16; ++q) {
-                    ur[q] *= sc;
-                    ui[q] *= sc;
-                }
-                const int wg = 4 * t2 + warp;
-                const int r3 = wg * 16 + kc;
-                const int rowoff = (r3 % 8) * 16 + (r3 / 8) * 1024;
-#pragma unroll
-                for (int part = 0; part < 2; ++part) {
-                    const float* src = part ? ui : ur;
-#pragma unroll
-                    for (int c = 0; c < 2; ++c) {
-                        const int k = part * 32 + img * 16 + 8 * c;
-                        uint4 hi, lo;
-                        SP::run(src + 8 * c, hi, lo);
-                        *reinterpret_cast<uint4*>(Ahi + rowoff + (k / 8) * 128) = hi;
-                        *reinterpret_cast<uint4*>(Alo + rowoff + (k / 8) * 128) = lo;
-                    }
+                for (int c = 0; c < 4; ++c) {
+                    uint4 hi, lo;
+                    SP::run(src + 8 * c, hi, lo);
+                    const int kcore = part * 4 + c;
+                    *reinterpret_cast<uint4*>(Ahi + rowoff + kcore * 128) = hi;
+                    *reinterpret_cast<uint4*>(Alo + rowoff + kcore * 128) = lo;
                 }
             }
         }
@@ -438,8 +454,8 @@ __global__ void __launch_bounds__(128) k_window_tc32(TcArgs a) {
         tc::fence_before();
         to_mma();
         if (t == 0) {
-            for (int t4 = 0; t4 < 2; ++t4)
-                for (int s = 0; s < 2; ++s)
+            for (int s = 0; s < 2; ++s)
+                for (int t4 = 0; t4 < 2; ++t4)
                     mma3(tmem + 128 + 32 * t4, tc::desc(ahi + t4 * 8192 + s * 4096, 2048, 128),
                          tc::desc(alo + t4 * 8192 + s * 4096, 2048, 128), tc::desc(b1hi + s * 1024, 512, 128),
                          tc::desc(b1lo + s * 1024, 512, 128), id4, s > 0);
