@@ -14,7 +14,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <string>
 #include <vector>
 
 #include "prepass.cuh"
@@ -73,6 +75,7 @@ struct flct_ctx {
     int nsm = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[8] = {};
+    cudaEvent_t tev[2] = {};  // autotuner
     char err[512] = {0};
     flct_timing timing{};
     // grow-only device workspace
@@ -83,14 +86,38 @@ struct flct_ctx {
     Buf b_s1, b_s2, b_work, b_ctr, b_r1, b_r2, b_b1, b_b2, b_gvx, b_gvy, b_ix, b_iy;
     Buf b_f1, b_f2, b_vx, b_vy, b_vm, b_aux1, b_aux2, b_means, b_peaks, b_hrow;
     std::vector<Buf*> all() {
-        return {&b_s1, &b_s2, &b_work, &b_ctr, &b_r1, &b_r2, &b_b1, &b_b2, &b_gvx, &b_gvy, &b_ix,
-                &b_iy, &b_f1, &b_f2, &b_vx, &b_vy, &b_vm, &b_aux1, &b_aux2, &b_means, &b_peaks, &b_hrow, &b_tc};
+        return {&b_s1,   &b_s2,   &b_work,   &b_ctr,    &b_r1,     &b_r2,     &b_b1,     &b_b2,
+                &b_gvx,  &b_gvy,  &b_ix,     &b_iy,     &b_f1,     &b_f2,     &b_vx,     &b_vy,
+                &b_vm,   &b_aux1, &b_aux2,   &b_means,  &b_peaks,  &b_hrow,   &b_tc,     &bb_arena,
+                &bb_work, &bb_means, &bb_peaks, &bb_ctr, &bb_meta};
     }
     int bps[sizeof(kWin) / sizeof(kWin[0])] = {0};
     int bps_tc[2] = {0, 0};
     Buf b_tc;              // tensor-core DFT matrices (b1 32x32, b2 64x64 floats)
     bool tc_ready = false;
     bool pending = false;  // a velocity call's events await collection
+    // autotuner: the fastest window configuration per box size
+    struct Tune {
+        int form = FLCT_FORM_FP32;
+        int grid_div = 1;        // CTAs per SM = occupancy limit / grid_div
+        float ns_per_window = 0.f;
+    };
+    std::map<int, Tune> tune;
+    std::string tune_path;       // JSON cache (FLCT_AUTOTUNE_CACHE), empty: none
+    std::string device_name;
+    // heterogeneous batches: own workspace (a batch's graph keeps pointing
+    // at it), branch streams of the captured graph, the instantiated graph
+    // of the last batch and the pairs it was built for
+    static constexpr int kBranches = 8;
+    Buf bb_arena, bb_work, bb_means, bb_peaks, bb_ctr, bb_meta;
+    cudaStream_t bstream[kBranches] = {};
+    cudaEvent_t bev[kBranches + 1] = {};
+    cudaEvent_t bdone = nullptr;  // recorded after each batch launch
+    cudaGraphExec_t gexec = nullptr;
+    std::vector<unsigned char> gkey;
+    int batch_pending = 0;        // pairs of the batch whose timing awaits collection
+    int batch_launches = 0;
+    int batch_box = 0, batch_form = 0;
 };
 
 namespace {
@@ -235,10 +262,14 @@ flct_status ensure_tc_tables(flct_ctx* ctx) {
     return FLCT_OK;
 }
 
-// Resolve FLCT_FORM_AUTO and check that the form exists for box size n.
+// Resolve FLCT_FORM_AUTO (the autotuner's choice once it has measured box
+// size n, else the FP32 form) and check that the form exists for n.
 flct_status pick_form(flct_ctx* ctx, int requested, int n, int* form) {
     int f = requested;
-    if (f == FLCT_FORM_AUTO) f = (n == 32) ? FLCT_FORM_TC_FP16 : FLCT_FORM_FP32;
+    if (f == FLCT_FORM_AUTO) {
+        auto it = ctx->tune.find(n);
+        f = (it != ctx->tune.end()) ? it->second.form : FLCT_FORM_FP32;
+    }
     if ((f == FLCT_FORM_TC_FP16 || f == FLCT_FORM_TC_BF16) && n != 32)
         return fail(ctx, FLCT_ERR_UNSUPPORTED, "the tensor-core form is built for 32x32 boxes (sigma 8); box %d", n);
     if (f < 0 || f > FLCT_FORM_TC_BF16) return fail(ctx, FLCT_ERR_ARG, "unknown window form %d", requested);
@@ -248,9 +279,10 @@ flct_status pick_form(flct_ctx* ctx, int requested, int n, int* form) {
 
 // Launch the window kernel of the chosen form on the prepared work list.
 flct_status launch_windows(flct_ctx* ctx, int form, const WinEntry* we, int n, const WinArgs& wa, unsigned* status,
-                           cudaStream_t st) {
+                           cudaStream_t st, int grid_div = 1) {
+    if (grid_div < 1) grid_div = 1;
     if (form == FLCT_FORM_FP32) {
-        CK(we->launch(wa, win_grid(ctx, n), st));
+        CK(we->launch(wa, std::max(ctx->nsm, win_grid(ctx, n) / grid_div), st));
         return FLCT_OK;
     }
     flct_status s = ensure_tc_tables(ctx);
@@ -267,6 +299,9 @@ flct_status launch_windows(flct_ctx* ctx, int form, const WinEntry* we, int n, c
     ta.direct = wa.direct;
     ta.use_filter = wa.use_filter;
     ta.peaks = wa.peaks;
+    ta.segs = wa.segs;
+    ta.seg_start = wa.seg_start;
+    ta.nseg = wa.nseg;
     ta.b1 = (const float*)ctx->b_tc.p;
     ta.b2 = (const float*)ctx->b_tc.p + 32 * 32;
     ta.status = status;
@@ -276,9 +311,729 @@ flct_status launch_windows(flct_ctx* ctx, int form, const WinEntry* we, int n, c
     if (ctx->bps_tc[which] == 0)
         ctx->bps_tc[which] = std::max(1, which ? window_tc32_blocks_per_sm<__nv_bfloat16>()
                                                : window_tc32_blocks_per_sm<__half>());
-    const int grid = ctx->nsm * ctx->bps_tc[which];
+    const int grid = std::max(ctx->nsm, ctx->nsm * ctx->bps_tc[which] / grid_div);
     if (which) CK(launch_window_tc32<__nv_bfloat16>(ta, grid, st));
     else CK(launch_window_tc32<__half>(ta, grid, st));
+    return FLCT_OK;
+}
+
+// ---------------------------------------------------------- autotuner --
+
+void tune_save(flct_ctx* ctx) {
+    if (ctx->tune_path.empty()) return;
+    FILE* f = fopen(ctx->tune_path.c_str(), "w");
+    if (!f) return;
+    fprintf(f, "{\"device\": \"%s\", \"entries\": [\n", ctx->device_name.c_str());
+    size_t k = 0;
+    for (const auto& e : ctx->tune) {
+        fprintf(f, "  {\"box\": %d, \"form\": %d, \"grid_div\": %d, \"ns_per_window\": %.4f}%s\n", e.first,
+                e.second.form, e.second.grid_div, e.second.ns_per_window, (++k < ctx->tune.size()) ? "," : "");
+    }
+    fprintf(f, "]}\n");
+    fclose(f);
+}
+
+// Reads entries written by tune_save (one per line) for this device name.
+void tune_load(flct_ctx* ctx) {
+    if (ctx->tune_path.empty()) return;
+    FILE* f = fopen(ctx->tune_path.c_str(), "r");
+    if (!f) return;
+    char line[512];
+    bool same_device = false;
+    while (fgets(line, sizeof(line), f)) {
+        if (strstr(line, "\"device\"")) same_device = strstr(line, ctx->device_name.c_str()) != nullptr;
+        int box, form, gd;
+        float ns;
+        const char* q = strstr(line, "\"box\"");
+        if (same_device && q &&
+            sscanf(q, "\"box\": %d, \"form\": %d, \"grid_div\": %d, \"ns_per_window\": %f", &box, &form, &gd,
+                   &ns) == 4 &&
+            form >= FLCT_FORM_FP32 && form <= FLCT_FORM_TC_BF16 && gd >= 1 && gd <= 8) {
+            flct_ctx::Tune t;
+            t.form = form;
+            t.grid_div = gd;
+            t.ns_per_window = ns;
+            ctx->tune[box] = t;
+        }
+    }
+    fclose(f);
+}
+
+// Times every candidate configuration of the window kernel for box size n
+// on the work list already prepared on `st` and keeps the fastest.  Needs
+// a synchronising stream, so it never runs inside a stream capture.
+flct_status tune_windows(flct_ctx* ctx, const WinEntry* we, int n, const WinArgs& wa, unsigned* status,
+                         const int* d_nwork, cudaStream_t st) {
+    struct Cand {
+        int form, grid_div;
+    };
+    // FLCT_FORM_AUTO chooses among the forms whose error is FP32-like: the
+    // radix form and the split-FP16 tensor-core form (the BF16 split keeps
+    // fewer mantissa bits and is only used when asked for)
+    std::vector<Cand> cands = {{FLCT_FORM_FP32, 1}, {FLCT_FORM_FP32, 2}};
+    if (n == 32) {
+        cands.push_back({FLCT_FORM_TC_FP16, 1});
+        cands.push_back({FLCT_FORM_TC_FP16, 2});
+    }
+    int nwork = 0;
+    CK(cudaMemcpyAsync(&nwork, d_nwork, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (nwork <= 0) return FLCT_OK;  // nothing to measure yet
+    float best = 1e30f;
+    flct_ctx::Tune bt;
+    for (const auto& c : cands) {
+        float ms = 1e30f;
+        for (int rep = 0; rep < 3; ++rep) {
+            CK(cudaEventRecord(ctx->tev[0], st));
+            flct_status s = launch_windows(ctx, c.form, we, n, wa, status, st, c.grid_div);
+            if (s != FLCT_OK) return s;
+            CK(cudaEventRecord(ctx->tev[1], st));
+            CK(cudaEventSynchronize(ctx->tev[1]));
+            if (rep > 0) ms = std::min(ms, ev_ms(ctx->tev[0], ctx->tev[1]));
+        }
+        if (ms < best) {
+            best = ms;
+            bt.form = c.form;
+            bt.grid_div = c.grid_div;
+        }
+    }
+    bt.ns_per_window = best * 1e6f / (float)nwork;
+    ctx->tune[n] = bt;
+    tune_save(ctx);
+    return FLCT_OK;
+}
+
+// ------------------------------------------------- velocity pipeline --
+
+bool capturing(cudaStream_t st) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return cs != cudaStreamCaptureStatusNone;
+}
+
+// One image pair's velocity job after the host-side checks and parameter
+// derivation (flct.c:337-487, 535-745).
+struct Job {
+    const flct_params* p = nullptr;
+    const double* f1 = nullptr;
+    const double* f2 = nullptr;
+    double* vx = nullptr;
+    double* vy = nullptr;
+    double* vm = nullptr;
+    int nx = 0, ny = 0;
+    Derived d;
+    int n = 0;
+    const WinEntry* we = nullptr;
+    bool interp = false;
+};
+
+flct_status plan_job(flct_ctx* ctx, const flct_params* p, const double* f1, const double* f2, int nx, int ny,
+                     double* vx, double* vy, double* vm, Job* j) {
+    if (!p || !f1 || !f2 || !vx || !vy || !vm || nx < 1 || ny < 1)
+        return fail(ctx, FLCT_ERR_ARG, "null pointer or empty image (%d x %d)", nx, ny);
+    if ((long long)nx * ny >= (1ll << 31)) return fail(ctx, FLCT_ERR_UNSUPPORTED, "image larger than 2^31 pixels");
+    flct_status s = derive(ctx, p, nx, ny, &j->d);
+    if (s != FLCT_OK) return s;
+    if (j->d.global)
+        return fail(ctx, FLCT_ERR_UNSUPPORTED, "sigma <= 0 (global-shift mode) is not available on the GPU path yet");
+    if (p->hires) return fail(ctx, FLCT_ERR_UNSUPPORTED, "-h (hires) is not available on the GPU path yet");
+    if (p->filter && !(p->kr > 0.))
+        return fail(ctx, FLCT_ERR_UNSUPPORTED, "-k with kr <= 0 is not available on the GPU path");
+    j->n = j->d.n;
+    j->we = find_win(j->n);
+    if (!j->we) return fail(ctx, FLCT_ERR_UNSUPPORTED, "box size %d (sigma %g) has no GPU kernel", j->n, p->sigma);
+    j->p = p;
+    j->f1 = f1;
+    j->f2 = f2;
+    j->vx = vx;
+    j->vy = vy;
+    j->vm = vm;
+    j->nx = nx;
+    j->ny = ny;
+    j->interp = j->d.skip > 0 && p->interpolate;
+    return FLCT_OK;
+}
+
+// Device workspace of one job: the context's single-call buffers, or a
+// slice of a batch's buffers.
+struct JobBufs {
+    float2* s1 = nullptr;
+    float2* s2 = nullptr;
+    int* work = nullptr;
+    float4* means = nullptr;
+    PeakRec* peaks = nullptr;
+    double* r1 = nullptr;
+    double* r2 = nullptr;
+    double* b1 = nullptr;
+    double* b2 = nullptr;
+    // 64 bytes: [0] work count (int), [4] status bits, [8..23] |f1|,|f2|
+    // maxima, [24..31] relative threshold
+    unsigned char* ctr = nullptr;
+    double* gvx = nullptr;
+    double* gvy = nullptr;
+    unsigned char* hrow = nullptr;
+    unsigned char* ix = nullptr;
+    unsigned char* iy = nullptr;
+};
+
+// Bytes of each workspace region of a job.
+struct JobSizes {
+    size_t s = 0, work = 0, means = 0, peaks = 0, r = 0, b = 0, gv = 0, hrow = 0, ix = 0, iy = 0;
+};
+
+JobSizes job_sizes(const Job& j) {
+    const size_t npx = (size_t)j.nx * j.ny;
+    const int W = j.ny - j.n + 1, H = j.nx - j.n + 1;
+    JobSizes z;
+    z.s = npx * sizeof(float2);
+    z.work = npx * sizeof(int);
+    z.means = npx * sizeof(float4);
+    z.peaks = npx * sizeof(PeakRec);
+    z.r = (size_t)j.nx * W * sizeof(double);
+    z.b = (size_t)H * W * sizeof(double);
+    if (j.interp) {
+        z.gv = (size_t)j.d.icnt * j.d.jcnt * sizeof(double);
+        z.hrow = (size_t)(j.d.icnt + 2) * j.ny * (2 * sizeof(double) + 1);
+        z.ix = (size_t)j.nx * (4 * sizeof(double) + sizeof(int) + 1) + 64;
+        z.iy = (size_t)j.ny * (4 * sizeof(double) + sizeof(int) + 1) + 64;
+    }
+    return z;
+}
+
+// Threshold, classification / work list, FP64 box sums and local means
+// (flct.c:684-827).  Zeroes the job's counters first.
+flct_status enqueue_prepass(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaStream_t st, int* launches) {
+    const flct_params* p = j.p;
+    const int nx = j.nx, ny = j.ny, n = j.n;
+    const size_t npx = (size_t)nx * ny;
+    const int W = ny - n + 1, H = nx - n + 1;
+    int* d_nwork = (int*)b.ctr;
+    unsigned* d_status = (unsigned*)(b.ctr + 4);
+    unsigned long long* d_absmax = (unsigned long long*)(b.ctr + 8);
+    double* d_thr = (double*)(b.ctr + 24);
+    CK(cudaMemsetAsync(b.ctr, 0, 32, st));
+    if (j.d.rel_thresh) {
+        k_absmax<<<ctx->nsm * 4, 256, 0, st>>>(j.f1, j.f2, (long)npx, d_absmax);
+        k_thresh_final<<<1, 1, 0, st>>>(j.f1, j.f2, d_absmax, p->thresh, d_thr);
+        *launches += 2;
+    }
+    ClassifyArgs ca{};
+    ca.f1 = j.f1;
+    ca.f2 = j.f2;
+    ca.nx = nx;
+    ca.ny = ny;
+    ca.thr_val = p->thresh;
+    ca.thr_ptr = j.d.rel_thresh ? d_thr : nullptr;
+    ca.skip = j.d.skip;
+    ca.xoff = j.d.xoff;
+    ca.yoff = j.d.yoff;
+    ca.interpolate = j.interp;
+    ca.jcnt = j.d.jcnt;
+    ca.s1 = b.s1;
+    ca.s2 = b.s2;
+    ca.work = b.work;
+    ca.nwork = d_nwork;
+    ca.vx = j.vx;
+    ca.vy = j.vy;
+    ca.vm = j.vm;
+    ca.gvx = j.interp ? b.gvx : nullptr;
+    ca.gvy = j.interp ? b.gvy : nullptr;
+    ca.status = d_status;
+    {
+        long blocks = std::min<long>((long)(npx + 255) / 256, (long)ctx->nsm * 8);
+        k_classify<<<(int)std::max(1l, blocks), 256, 0, st>>>(ca);
+        ++*launches;
+    }
+    {
+        const int nseg = (W + kSeg - 1) / kSeg;
+        long t = (long)nx * nseg;
+        k_rowsum<<<(int)((t + 127) / 128), 128, 0, st>>>(j.f1, j.f2, nx, ny, n, b.r1, b.r2);
+        const int hseg = (H + kSeg - 1) / kSeg;
+        t = (long)W * hseg;
+        k_colsum<<<(int)((t + 127) / 128), 128, 0, st>>>(b.r1, b.r2, nx, W, n, b.b1, b.b2);
+        *launches += 2;
+    }
+    {
+        // FP64 local means per work item, one window per lane
+        MeansArgs ma{};
+        ma.work = b.work;
+        ma.nwork = d_nwork;
+        ma.nx = nx;
+        ma.ny = ny;
+        ma.nsize = j.d.nsize;
+        ma.bsw = W;
+        ma.bs1 = b.b1;
+        ma.bs2 = b.b2;
+        ma.inv_n2 = 1. / ((double)n * n);
+        ma.means = b.means;
+        long blocks = std::min<long>((long)(npx + 255) / 256, (long)ctx->nsm * 8);
+        k_means<<<(int)std::max(1l, blocks), 256, 0, st>>>(ma);
+        ++*launches;
+    }
+    CK(cudaGetLastError());
+    return FLCT_OK;
+}
+
+void make_wargs(const Job& j, const JobBufs& b, WinArgs* wa) {
+    *wa = WinArgs{};
+    fill_tables(j.p, j.n, wa->gauss, wa->filt2);
+    wa->use_filter = j.p->filter;
+    wa->s1 = b.s1;
+    wa->s2 = b.s2;
+    wa->means = b.means;
+    wa->work = b.work;
+    wa->nwork = (const int*)b.ctr;
+    wa->nx = j.nx;
+    wa->ny = j.ny;
+    wa->nsize = j.d.nsize;
+    wa->peaks = b.peaks;
+}
+
+// 3x3 fit, velocity, mask and skip-grid copy per work item (flct.c:901-942).
+flct_status enqueue_fit(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaStream_t st, int* launches) {
+    FitArgs fa{};
+    fa.work = b.work;
+    fa.nwork = (const int*)b.ctr;
+    fa.peaks = b.peaks;
+    fa.n = j.n;
+    fa.ny = j.ny;
+    fa.deltinv = 1. / j.p->deltat;  // flct.c:343
+    fa.deltas = j.p->deltas;
+    fa.skip = j.d.skip > 0 ? j.d.skip : 1;
+    fa.xoff = j.d.xoff;
+    fa.yoff = j.d.yoff;
+    fa.jcnt = j.d.jcnt;
+    fa.vx = j.vx;
+    fa.vy = j.vy;
+    fa.vm = j.vm;
+    fa.gvx = j.interp ? b.gvx : nullptr;
+    fa.gvy = j.interp ? b.gvy : nullptr;
+    const size_t npx = (size_t)j.nx * j.ny;
+    long blocks = std::min<long>((long)(npx + 127) / 128, (long)ctx->nsm * 8);
+    k_fit<<<(int)std::max(1l, blocks), 128, 0, st>>>(fa);
+    ++*launches;
+    CK(cudaGetLastError());
+    return FLCT_OK;
+}
+
+// Cubic-convolution interpolation of the skip grid onto the skipped pixels
+// (flct.c:958-1133).
+flct_status enqueue_interp(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaStream_t st, int* launches) {
+    const int nx = j.nx, ny = j.ny;
+    const size_t npx = (size_t)nx * ny;
+    double* wx = (double*)b.ix;
+    int* zx = (int*)(b.ix + (size_t)nx * 4 * sizeof(double));
+    unsigned char* okx = b.ix + (size_t)nx * (4 * sizeof(double) + sizeof(int));
+    double* wy = (double*)b.iy;
+    int* zy = (int*)(b.iy + (size_t)ny * 4 * sizeof(double));
+    unsigned char* oky = b.iy + (size_t)ny * (4 * sizeof(double) + sizeof(int));
+    k_interp_axis<<<(nx + 127) / 128, 128, 0, st>>>(nx, j.d.icnt, j.d.xoff, j.d.skip, nullptr, zx, wx, okx);
+    k_interp_axis<<<(ny + 127) / 128, 128, 0, st>>>(ny, j.d.jcnt, j.d.yoff, j.d.skip, nullptr, zy, wy, oky);
+    InterpArgs ia{};
+    ia.nx = nx;
+    ia.ny = ny;
+    ia.skip = j.d.skip;
+    ia.xoff = j.d.xoff;
+    ia.yoff = j.d.yoff;
+    ia.gx = j.d.icnt;
+    ia.gy = j.d.jcnt;
+    ia.gvx = b.gvx;
+    ia.gvy = b.gvy;
+    ia.zx = zx;
+    ia.wx = wx;
+    ia.okx = okx;
+    ia.zy = zy;
+    ia.wy = wy;
+    ia.oky = oky;
+    const size_t hn = (size_t)(j.d.icnt + 2) * ny;
+    ia.hx = (double*)b.hrow;
+    ia.hy = ia.hx + hn;
+    ia.hbad = (unsigned char*)(ia.hy + hn);
+    ia.vx = j.vx;
+    ia.vy = j.vy;
+    ia.vm = j.vm;
+    long rblocks = std::min<long>((long)(hn + 255) / 256, (long)ctx->nsm * 8);
+    k_interp_rows<<<(int)std::max(1l, rblocks), 256, 0, st>>>(ia);
+    long blocks = std::min<long>((long)(npx + 255) / 256, (long)ctx->nsm * 16);
+    k_interp<<<(int)std::max(1l, blocks), 256, 0, st>>>(ia);
+    *launches += 4;
+    CK(cudaGetLastError());
+    return FLCT_OK;
+}
+
+// Occupancy queries and the tensor-core tables need the host; done before
+// a stream capture so the captured launches make none of these calls.
+flct_status prime_form(flct_ctx* ctx, int form, int n) {
+    if (form == FLCT_FORM_FP32) {
+        if (win_grid(ctx, n) <= 0) return fail(ctx, FLCT_ERR_CUDA, "no occupancy for the box-%d window kernel", n);
+        return FLCT_OK;
+    }
+    flct_status s = ensure_tc_tables(ctx);
+    if (s != FLCT_OK) return s;
+    const int which = (form == FLCT_FORM_TC_BF16) ? 1 : 0;
+    if (ctx->bps_tc[which] == 0)
+        ctx->bps_tc[which] = std::max(1, which ? window_tc32_blocks_per_sm<__nv_bfloat16>()
+                                               : window_tc32_blocks_per_sm<__half>());
+    return FLCT_OK;
+}
+
+// Form and CTAs-per-SM divisor for box size n: the request, or for
+// FLCT_FORM_AUTO the autotuner's measured choice.
+void resolved_config(flct_ctx* ctx, int requested, int n, int* form, int* grid_div) {
+    *grid_div = 1;
+    if (requested != FLCT_FORM_AUTO) {
+        *form = requested;
+        return;
+    }
+    auto it = ctx->tune.find(n);
+    if (it == ctx->tune.end()) {
+        *form = FLCT_FORM_FP32;
+        return;
+    }
+    *form = it->second.form;
+    *grid_div = it->second.grid_div;
+}
+
+// ------------------------------------------------------------- batches --
+
+// Pairs sharing a box size, requested form and window tables run through
+// one persistent window-kernel launch.
+struct BatchGroup {
+    int n = 0;
+    int req_form = 0;
+    int use_filter = 0;
+    float gauss[2 * kMaxBox + 1] = {};
+    float filt2[kMaxBox] = {};
+    std::vector<int> pairs;
+    int form = FLCT_FORM_FP32;
+    int grid_div = 1;
+};
+
+struct BatchPlan {
+    std::vector<Job> jobs;
+    std::vector<JobBufs> bufs;
+    std::vector<BatchGroup> groups;
+    WinSeg* segs = nullptr;  // device, group-major
+    int* starts = nullptr;   // device, per group nseg + 1 entries
+    int* seg_pair = nullptr; // device
+    int* first = nullptr;    // device, ngroups + 1
+    std::vector<int> h_first;
+};
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// The fields of a pair list that a captured batch depends on.
+std::vector<unsigned char> batch_key(int npairs, const flct_pair* pairs) {
+    std::vector<unsigned char> key;
+    auto put = [&key](const void* v, size_t n) {
+        const unsigned char* c = (const unsigned char*)v;
+        key.insert(key.end(), c, c + n);
+    };
+    for (int k = 0; k < npairs; ++k) {
+        const flct_pair& q = pairs[k];
+        const flct_params& p = q.params;
+        put(&q.f1, sizeof(q.f1));
+        put(&q.f2, sizeof(q.f2));
+        put(&q.vx, sizeof(q.vx));
+        put(&q.vy, sizeof(q.vy));
+        put(&q.vm, sizeof(q.vm));
+        const int ints[] = {q.nx, q.ny, p.thresh_abs, p.skip, p.poffset, p.qoffset, p.interpolate, p.filter,
+                            p.hires, p.form};
+        const double dbl[] = {p.deltat, p.deltas, p.sigma, p.thresh, p.kr};
+        put(ints, sizeof(ints));
+        put(dbl, sizeof(dbl));
+    }
+    return key;
+}
+
+flct_status pair_fail(flct_ctx* ctx, flct_status s, int k) {
+    char msg[sizeof(ctx->err)];
+    snprintf(msg, sizeof(msg), "pair %d: %.480s", k, ctx->err);
+    memcpy(ctx->err, msg, sizeof(msg));
+    return s;
+}
+
+// Checks every pair, groups the pairs, lays out and allocates the batch
+// workspace and uploads the segment tables.
+flct_status plan_batch(flct_ctx* ctx, int npairs, const flct_pair* pairs, BatchPlan* bp) {
+    bp->jobs.assign(npairs, Job{});
+    for (int k = 0; k < npairs; ++k) {
+        const flct_pair& q = pairs[k];
+        flct_status s = plan_job(ctx, &q.params, q.f1, q.f2, q.nx, q.ny, q.vx, q.vy, q.vm, &bp->jobs[k]);
+        if (s != FLCT_OK) return pair_fail(ctx, s, k);
+        int form = 0;
+        s = pick_form(ctx, q.params.form, bp->jobs[k].n, &form);  // rejects forms without a kernel for n
+        if (s != FLCT_OK) return pair_fail(ctx, s, k);
+    }
+    // groups: same box, requested form and window tables
+    for (int k = 0; k < npairs; ++k) {
+        const Job& j = bp->jobs[k];
+        BatchGroup g;
+        g.n = j.n;
+        g.req_form = j.p->form;
+        g.use_filter = j.p->filter ? 1 : 0;
+        fill_tables(j.p, j.n, g.gauss, g.filt2);
+        bool found = false;
+        for (auto& G : bp->groups)
+            if (G.n == g.n && G.req_form == g.req_form && G.use_filter == g.use_filter &&
+                !memcmp(G.gauss, g.gauss, sizeof(g.gauss)) && !memcmp(G.filt2, g.filt2, sizeof(g.filt2))) {
+                G.pairs.push_back(k);
+                found = true;
+                break;
+            }
+        if (!found) {
+            g.pairs.push_back(k);
+            bp->groups.push_back(g);
+        }
+    }
+    // workspace: per-pair arena slices, item-indexed arrays shared by all pairs
+    struct Off {
+        size_t s1, s2, r1, r2, b1, b2, gvx, gvy, hrow, ix, iy;
+        long long base;
+    };
+    std::vector<Off> off(npairs);
+    size_t arena = 0;
+    long long items = 0;
+    auto take = [&arena](size_t bytes) {
+        const size_t o = arena;
+        arena += align256(bytes);
+        return o;
+    };
+    for (int k = 0; k < npairs; ++k) {
+        const JobSizes z = job_sizes(bp->jobs[k]);
+        Off& o = off[k];
+        o.s1 = take(z.s);
+        o.s2 = take(z.s);
+        o.r1 = take(z.r);
+        o.r2 = take(z.r);
+        o.b1 = take(z.b);
+        o.b2 = take(z.b);
+        o.gvx = take(z.gv);
+        o.gvy = take(z.gv);
+        o.hrow = take(z.hrow);
+        o.ix = take(z.ix);
+        o.iy = take(z.iy);
+        o.base = items;
+        items += (long long)bp->jobs[k].nx * bp->jobs[k].ny;
+    }
+    if (items >= (1ll << 31)) return fail(ctx, FLCT_ERR_UNSUPPORTED, "batch larger than 2^31 pixels in total");
+    const int ng = (int)bp->groups.size();
+    const size_t seg_bytes = align256((size_t)npairs * sizeof(WinSeg));
+    const size_t start_bytes = align256((size_t)(npairs + ng) * sizeof(int));
+    const size_t pair_bytes = align256((size_t)npairs * sizeof(int));
+    const size_t first_bytes = align256((size_t)(ng + 1) * sizeof(int));
+    ENSURE(ctx->bb_arena, arena);
+    ENSURE(ctx->bb_work, (size_t)items * sizeof(int));
+    ENSURE(ctx->bb_means, (size_t)items * sizeof(float4));
+    ENSURE(ctx->bb_peaks, (size_t)items * sizeof(PeakRec));
+    ENSURE(ctx->bb_ctr, (size_t)npairs * 64);
+    ENSURE(ctx->bb_meta, seg_bytes + start_bytes + pair_bytes + first_bytes);
+    unsigned char* A = (unsigned char*)ctx->bb_arena.p;
+    bp->bufs.assign(npairs, JobBufs{});
+    for (int k = 0; k < npairs; ++k) {
+        const Off& o = off[k];
+        JobBufs& b = bp->bufs[k];
+        b.s1 = (float2*)(A + o.s1);
+        b.s2 = (float2*)(A + o.s2);
+        b.r1 = (double*)(A + o.r1);
+        b.r2 = (double*)(A + o.r2);
+        b.b1 = (double*)(A + o.b1);
+        b.b2 = (double*)(A + o.b2);
+        b.gvx = (double*)(A + o.gvx);
+        b.gvy = (double*)(A + o.gvy);
+        b.hrow = A + o.hrow;
+        b.ix = A + o.ix;
+        b.iy = A + o.iy;
+        b.work = (int*)ctx->bb_work.p + o.base;
+        b.means = (float4*)ctx->bb_means.p + o.base;
+        b.peaks = (PeakRec*)ctx->bb_peaks.p + o.base;
+        b.ctr = (unsigned char*)ctx->bb_ctr.p + 64 * (size_t)k;
+    }
+    // segment tables, group-major
+    std::vector<unsigned char> meta(seg_bytes + start_bytes + pair_bytes + first_bytes, 0);
+    WinSeg* hs = (WinSeg*)meta.data();
+    int* hpair = (int*)(meta.data() + seg_bytes + start_bytes);
+    int* hfirst = (int*)(meta.data() + seg_bytes + start_bytes + pair_bytes);
+    int e = 0;
+    for (int g = 0; g < ng; ++g) {
+        hfirst[g] = e;
+        for (int k : bp->groups[g].pairs) {
+            WinSeg sg{};
+            sg.s1 = bp->bufs[k].s1;
+            sg.s2 = bp->bufs[k].s2;
+            sg.nx = bp->jobs[k].nx;
+            sg.ny = bp->jobs[k].ny;
+            sg.base = (int)off[k].base;
+            hs[e] = sg;
+            hpair[e] = k;
+            ++e;
+        }
+    }
+    hfirst[ng] = e;
+    bp->h_first.assign(hfirst, hfirst + ng + 1);
+    unsigned char* M = (unsigned char*)ctx->bb_meta.p;
+    CK(cudaMemcpy(M, meta.data(), meta.size(), cudaMemcpyHostToDevice));
+    bp->segs = (WinSeg*)M;
+    bp->starts = (int*)(M + seg_bytes);
+    bp->seg_pair = (int*)(M + seg_bytes + start_bytes);
+    bp->first = (int*)(M + seg_bytes + start_bytes + pair_bytes);
+    return FLCT_OK;
+}
+
+// Window-kernel arguments of group g (all its pairs in one launch).
+void group_wargs(flct_ctx* ctx, const BatchPlan& bp, int g, WinArgs* wa) {
+    const BatchGroup& G = bp.groups[g];
+    *wa = WinArgs{};
+    memcpy(wa->gauss, G.gauss, sizeof(G.gauss));
+    memcpy(wa->filt2, G.filt2, sizeof(G.filt2));
+    wa->use_filter = G.use_filter;
+    wa->means = (const float4*)ctx->bb_means.p;
+    wa->work = (const int*)ctx->bb_work.p;
+    wa->peaks = (PeakRec*)ctx->bb_peaks.p;
+    wa->nsize = G.n / 2;
+    wa->nseg = bp.h_first[g + 1] - bp.h_first[g];
+    wa->segs = bp.segs + bp.h_first[g];
+    wa->seg_start = bp.starts + bp.h_first[g] + g;
+    wa->nwork = wa->seg_start + wa->nseg;
+}
+
+// Enqueues a planned batch on `bs`: every pair's prepass, the per-group
+// prefix sums, one persistent window launch per group, every pair's fit and
+// interpolation.  With `branches` the per-pair and per-group work spreads
+// over the context's branch streams (fork / join through events), which a
+// stream capture turns into parallel graph branches.
+flct_status enqueue_batch(flct_ctx* ctx, BatchPlan& bp, cudaStream_t bs, bool branches, int* launches) {
+    const int np = (int)bp.jobs.size();
+    const int ng = (int)bp.groups.size();
+    const int nb = branches ? std::min(np, flct_ctx::kBranches) : 0;
+    auto fork = [&]() -> flct_status {
+        if (!nb) return FLCT_OK;
+        CK(cudaEventRecord(ctx->bev[0], bs));
+        for (int k = 0; k < nb; ++k) CK(cudaStreamWaitEvent(ctx->bstream[k], ctx->bev[0], 0));
+        return FLCT_OK;
+    };
+    auto join = [&]() -> flct_status {
+        for (int k = 0; k < nb; ++k) {
+            CK(cudaEventRecord(ctx->bev[1 + k], ctx->bstream[k]));
+            CK(cudaStreamWaitEvent(bs, ctx->bev[1 + k], 0));
+        }
+        return FLCT_OK;
+    };
+    auto lane = [&](int i) { return nb ? ctx->bstream[i % nb] : bs; };
+    flct_status s = fork();
+    for (int k = 0; k < np && s == FLCT_OK; ++k) s = enqueue_prepass(ctx, bp.jobs[k], bp.bufs[k], lane(k), launches);
+    if (s == FLCT_OK) s = join();
+    if (s != FLCT_OK) return s;
+    k_batch_starts<<<(ng + 31) / 32, 32, 0, bs>>>((const unsigned char*)ctx->bb_ctr.p, bp.seg_pair, bp.first, ng,
+                                                   bp.starts);
+    ++*launches;
+    CK(cudaGetLastError());
+    s = fork();
+    for (int g = 0; g < ng && s == FLCT_OK; ++g) {
+        const BatchGroup& G = bp.groups[g];
+        WinArgs wa;
+        group_wargs(ctx, bp, g, &wa);
+        unsigned* status = (unsigned*)(bp.bufs[G.pairs[0]].ctr + 4);
+        s = launch_windows(ctx, G.form, find_win(G.n), G.n, wa, status, lane(g), G.grid_div);
+        ++*launches;
+    }
+    if (s == FLCT_OK) s = join();
+    if (s != FLCT_OK) return s;
+    s = fork();
+    for (int k = 0; k < np && s == FLCT_OK; ++k) {
+        s = enqueue_fit(ctx, bp.jobs[k], bp.bufs[k], lane(k), launches);
+        if (s == FLCT_OK && bp.jobs[k].interp) s = enqueue_interp(ctx, bp.jobs[k], bp.bufs[k], lane(k), launches);
+    }
+    if (s == FLCT_OK) s = join();
+    return s;
+}
+
+// Autotunes every FLCT_FORM_AUTO group whose box size has no measurement
+// yet, on the batch's own work lists (runs the prepasses eagerly, syncs).
+flct_status tune_batch(flct_ctx* ctx, BatchPlan& bp, cudaStream_t bs) {
+    bool any = false;
+    for (const auto& G : bp.groups) any |= G.req_form == FLCT_FORM_AUTO && !ctx->tune.count(G.n);
+    if (!any) return FLCT_OK;
+    int launches = 0;
+    for (size_t k = 0; k < bp.jobs.size(); ++k) {
+        flct_status s = enqueue_prepass(ctx, bp.jobs[k], bp.bufs[k], bs, &launches);
+        if (s != FLCT_OK) return s;
+    }
+    const int ng = (int)bp.groups.size();
+    k_batch_starts<<<(ng + 31) / 32, 32, 0, bs>>>((const unsigned char*)ctx->bb_ctr.p, bp.seg_pair, bp.first, ng,
+                                                   bp.starts);
+    CK(cudaGetLastError());
+    for (int g = 0; g < ng; ++g) {
+        const BatchGroup& G = bp.groups[g];
+        if (G.req_form != FLCT_FORM_AUTO || ctx->tune.count(G.n)) continue;
+        WinArgs wa;
+        group_wargs(ctx, bp, g, &wa);
+        unsigned* status = (unsigned*)(bp.bufs[G.pairs[0]].ctr + 4);
+        for (int f : {FLCT_FORM_FP32, FLCT_FORM_TC_FP16}) {
+            if (f != FLCT_FORM_FP32 && G.n != 32) continue;
+            flct_status s = prime_form(ctx, f, G.n);
+            if (s != FLCT_OK) return s;
+        }
+        flct_status s = tune_windows(ctx, find_win(G.n), G.n, wa, status, wa.nwork, bs);
+        if (s != FLCT_OK) return s;
+    }
+    CK(cudaStreamSynchronize(bs));
+    return FLCT_OK;
+}
+
+// Plans the batch, tunes what needs tuning, captures the whole batch as one
+// CUDA graph and instantiates it.
+flct_status rebuild_batch(flct_ctx* ctx, int npairs, const flct_pair* pairs, cudaStream_t st) {
+    // the previous batch's graph may still be running on the workspace
+    if (ctx->bdone) CK(cudaEventSynchronize(ctx->bdone));
+    if (ctx->gexec) {
+        cudaGraphExecDestroy(ctx->gexec);
+        ctx->gexec = nullptr;
+    }
+    ctx->gkey.clear();
+    for (int k = 0; k < flct_ctx::kBranches; ++k)
+        if (!ctx->bstream[k]) CK(cudaStreamCreateWithFlags(&ctx->bstream[k], cudaStreamNonBlocking));
+    for (auto& e : ctx->bev)
+        if (!e) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    if (!ctx->bdone) CK(cudaEventCreateWithFlags(&ctx->bdone, cudaEventDisableTiming));
+    BatchPlan bp;
+    flct_status s = plan_batch(ctx, npairs, pairs, &bp);
+    if (s != FLCT_OK) return s;
+    cudaStream_t bs = ctx->stream;
+    // the internal stream sees the caller's inputs before the tuning pass
+    CK(cudaEventRecord(ctx->bev[0], st));
+    CK(cudaStreamWaitEvent(bs, ctx->bev[0], 0));
+    s = tune_batch(ctx, bp, bs);
+    if (s != FLCT_OK) return s;
+    for (auto& G : bp.groups) {
+        resolved_config(ctx, G.req_form, G.n, &G.form, &G.grid_div);
+        s = prime_form(ctx, G.form, G.n);
+        if (s != FLCT_OK) return s;
+    }
+    CK(cudaStreamBeginCapture(bs, cudaStreamCaptureModeRelaxed));
+    int launches = 0;
+    s = enqueue_batch(ctx, bp, bs, true, &launches);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(bs, &graph);
+    if (s != FLCT_OK || ec != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();
+        if (s != FLCT_OK) return s;
+        return fail(ctx, FLCT_ERR_CUDA, "capturing the batch failed: %s", cudaGetErrorString(ec));
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&ctx->gexec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ei != cudaSuccess) {
+        ctx->gexec = nullptr;
+        return fail(ctx, FLCT_ERR_CUDA, "instantiating the batch graph failed: %s", cudaGetErrorString(ei));
+    }
+    ctx->gkey = batch_key(npairs, pairs);
+    ctx->batch_launches = launches;
+    ctx->batch_box = bp.groups.size() == 1 ? bp.groups[0].n : 0;
+    ctx->batch_form = bp.groups[0].form;
     return FLCT_OK;
 }
 
@@ -334,6 +1089,14 @@ flct_status flct_gpu_create(int device, flct_ctx** out) {
             flct_gpu_destroy(ctx);
             return FLCT_ERR_CUDA;
         }
+    for (auto& e : ctx->tev)
+        if (cudaEventCreate(&e) != cudaSuccess) {
+            flct_gpu_destroy(ctx);
+            return FLCT_ERR_CUDA;
+        }
+    ctx->device_name = prop.name;
+    if (const char* path = getenv("FLCT_AUTOTUNE_CACHE")) ctx->tune_path = path;
+    tune_load(ctx);
     *out = ctx;
     return FLCT_OK;
 }
@@ -342,10 +1105,21 @@ void flct_gpu_destroy(flct_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (auto& st : ctx->bstream)
+        if (st) cudaStreamSynchronize(st);
+    if (ctx->bdone) cudaEventSynchronize(ctx->bdone);
+    if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
     for (auto* b : ctx->all())
         if (b->p) cudaFree(b->p);
     for (auto& e : ctx->ev)
         if (e) cudaEventDestroy(e);
+    for (auto& e : ctx->tev)
+        if (e) cudaEventDestroy(e);
+    for (auto& e : ctx->bev)
+        if (e) cudaEventDestroy(e);
+    if (ctx->bdone) cudaEventDestroy(ctx->bdone);
+    for (auto& st : ctx->bstream)
+        if (st) cudaStreamDestroy(st);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -372,198 +1146,83 @@ flct_status flct_gpu_velocity_device(flct_ctx* ctx, const flct_params* p, const 
                                      const double* d_f2, int nx, int ny, double* d_vx, double* d_vy,
                                      double* d_vm, void* stream) {
     if (!ctx) return FLCT_ERR_ARG;
-    if (!p || !d_f1 || !d_f2 || !d_vx || !d_vy || !d_vm || nx < 1 || ny < 1)
-        return fail(ctx, FLCT_ERR_ARG, "null pointer or empty image (%d x %d)", nx, ny);
-    if ((long long)nx * ny >= (1ll << 31)) return fail(ctx, FLCT_ERR_UNSUPPORTED, "image larger than 2^31 pixels");
+    Job j;
+    flct_status s = plan_job(ctx, p, d_f1, d_f2, nx, ny, d_vx, d_vy, d_vm, &j);
+    if (s != FLCT_OK) return s;
     CK(cudaSetDevice(ctx->device));
     cudaStream_t st = (cudaStream_t)stream;  // NULL: the CUDA default stream
-    Derived d;
-    flct_status s = derive(ctx, p, nx, ny, &d);
-    if (s != FLCT_OK) return s;
-    if (d.global) return fail(ctx, FLCT_ERR_UNSUPPORTED, "sigma <= 0 (global-shift mode) is not available on the GPU path yet");
-    if (p->hires) return fail(ctx, FLCT_ERR_UNSUPPORTED, "-h (hires) is not available on the GPU path yet");
-    if (p->filter && !(p->kr > 0.)) return fail(ctx, FLCT_ERR_UNSUPPORTED, "-k with kr <= 0 is not available on the GPU path");
-    const int n = d.n;
-    const WinEntry* we = find_win(n);
-    if (!we) return fail(ctx, FLCT_ERR_UNSUPPORTED, "box size %d (sigma %g) has no GPU kernel", n, p->sigma);
+    const int n = j.n;
     int form = FLCT_FORM_FP32;
     s = pick_form(ctx, p->form, n, &form);
     if (s != FLCT_OK) return s;
 
-    const size_t npx = (size_t)nx * ny;
-    const int W = ny - n + 1, H = nx - n + 1;
-    ENSURE(ctx->b_s1, npx * sizeof(float2));
-    ENSURE(ctx->b_s2, npx * sizeof(float2));
-    ENSURE(ctx->b_work, npx * sizeof(int));
+    const JobSizes z = job_sizes(j);
+    ENSURE(ctx->b_s1, z.s);
+    ENSURE(ctx->b_s2, z.s);
+    ENSURE(ctx->b_work, z.work);
     ENSURE(ctx->b_ctr, 64);
-    ENSURE(ctx->b_r1, (size_t)nx * W * sizeof(double));
-    ENSURE(ctx->b_r2, (size_t)nx * W * sizeof(double));
-    ENSURE(ctx->b_b1, (size_t)H * W * sizeof(double));
-    ENSURE(ctx->b_b2, (size_t)H * W * sizeof(double));
-    ENSURE(ctx->b_means, npx * sizeof(float4));
-    ENSURE(ctx->b_peaks, npx * sizeof(PeakRec));
-    const bool interp = d.skip > 0 && p->interpolate;
-    if (interp) {
-        ENSURE(ctx->b_hrow, (size_t)(d.icnt + 2) * ny * (2 * sizeof(double) + 1));
-        ENSURE(ctx->b_gvx, (size_t)d.icnt * d.jcnt * sizeof(double));
-        ENSURE(ctx->b_gvy, (size_t)d.icnt * d.jcnt * sizeof(double));
-        ENSURE(ctx->b_ix, (size_t)nx * (4 * sizeof(double) + sizeof(int) + 1) + 64);
-        ENSURE(ctx->b_iy, (size_t)ny * (4 * sizeof(double) + sizeof(int) + 1) + 64);
+    ENSURE(ctx->b_r1, z.r);
+    ENSURE(ctx->b_r2, z.r);
+    ENSURE(ctx->b_b1, z.b);
+    ENSURE(ctx->b_b2, z.b);
+    ENSURE(ctx->b_means, z.means);
+    ENSURE(ctx->b_peaks, z.peaks);
+    if (j.interp) {
+        ENSURE(ctx->b_hrow, z.hrow);
+        ENSURE(ctx->b_gvx, z.gv);
+        ENSURE(ctx->b_gvy, z.gv);
+        ENSURE(ctx->b_ix, z.ix);
+        ENSURE(ctx->b_iy, z.iy);
     }
-    // counters: [0] nwork (int), [1] status (u32), [8..23] absmax (2 x u64), [24..31] thresh
-    unsigned char* ctr = (unsigned char*)ctx->b_ctr.p;
-    int* d_nwork = (int*)ctr;
-    unsigned* d_status = (unsigned*)(ctr + 4);
-    unsigned long long* d_absmax = (unsigned long long*)(ctr + 8);
-    double* d_thr = (double*)(ctr + 24);
+    JobBufs b;
+    b.s1 = (float2*)ctx->b_s1.p;
+    b.s2 = (float2*)ctx->b_s2.p;
+    b.work = (int*)ctx->b_work.p;
+    b.means = (float4*)ctx->b_means.p;
+    b.peaks = (PeakRec*)ctx->b_peaks.p;
+    b.r1 = (double*)ctx->b_r1.p;
+    b.r2 = (double*)ctx->b_r2.p;
+    b.b1 = (double*)ctx->b_b1.p;
+    b.b2 = (double*)ctx->b_b2.p;
+    b.ctr = (unsigned char*)ctx->b_ctr.p;
+    b.gvx = (double*)ctx->b_gvx.p;
+    b.gvy = (double*)ctx->b_gvy.p;
+    b.hrow = (unsigned char*)ctx->b_hrow.p;
+    b.ix = (unsigned char*)ctx->b_ix.p;
+    b.iy = (unsigned char*)ctx->b_iy.p;
+    unsigned* d_status = (unsigned*)(b.ctr + 4);
 
     int launches = 0;
+    ctx->batch_pending = 0;
     CK(cudaEventRecord(ctx->ev[0], st));
-    CK(cudaMemsetAsync(ctr, 0, 32, st));
-    if (d.rel_thresh) {
-        k_absmax<<<ctx->nsm * 4, 256, 0, st>>>(d_f1, d_f2, (long)npx, d_absmax);
-        k_thresh_final<<<1, 1, 0, st>>>(d_f1, d_f2, d_absmax, p->thresh, d_thr);
-        launches += 2;
+    s = enqueue_prepass(ctx, j, b, st, &launches);
+    if (s != FLCT_OK) return s;
+    WinArgs wa;
+    make_wargs(j, b, &wa);
+    // first FLCT_FORM_AUTO call for this box size: time the candidates on
+    // this work list (not possible inside a stream capture)
+    if (p->form == FLCT_FORM_AUTO && !ctx->tune.count(n) && !capturing(st)) {
+        for (int f : {FLCT_FORM_FP32, FLCT_FORM_TC_FP16}) {
+            if (f != FLCT_FORM_FP32 && n != 32) continue;
+            s = prime_form(ctx, f, n);
+            if (s != FLCT_OK) return s;
+        }
+        s = tune_windows(ctx, j.we, n, wa, d_status, (const int*)b.ctr, st);
+        if (s != FLCT_OK) return s;
     }
-    ClassifyArgs ca{};
-    ca.f1 = d_f1;
-    ca.f2 = d_f2;
-    ca.nx = nx;
-    ca.ny = ny;
-    ca.thr_val = p->thresh;
-    ca.thr_ptr = d.rel_thresh ? d_thr : nullptr;
-    ca.skip = d.skip;
-    ca.xoff = d.xoff;
-    ca.yoff = d.yoff;
-    ca.interpolate = interp;
-    ca.jcnt = d.jcnt;
-    ca.s1 = (float2*)ctx->b_s1.p;
-    ca.s2 = (float2*)ctx->b_s2.p;
-    ca.work = (int*)ctx->b_work.p;
-    ca.nwork = d_nwork;
-    ca.vx = d_vx;
-    ca.vy = d_vy;
-    ca.vm = d_vm;
-    ca.gvx = interp ? (double*)ctx->b_gvx.p : nullptr;
-    ca.gvy = interp ? (double*)ctx->b_gvy.p : nullptr;
-    ca.status = d_status;
-    {
-        long blocks = std::min<long>((long)(npx + 255) / 256, (long)ctx->nsm * 8);
-        k_classify<<<(int)std::max(1l, blocks), 256, 0, st>>>(ca);
-        ++launches;
-    }
-    {
-        const int nseg = (W + kSeg - 1) / kSeg;
-        long t = (long)nx * nseg;
-        k_rowsum<<<(int)((t + 127) / 128), 128, 0, st>>>(d_f1, d_f2, nx, ny, n, (double*)ctx->b_r1.p,
-                                                         (double*)ctx->b_r2.p);
-        const int hseg = (H + kSeg - 1) / kSeg;
-        t = (long)W * hseg;
-        k_colsum<<<(int)((t + 127) / 128), 128, 0, st>>>((double*)ctx->b_r1.p, (double*)ctx->b_r2.p, nx, W, n,
-                                                         (double*)ctx->b_b1.p, (double*)ctx->b_b2.p);
-        launches += 2;
-    }
-    {
-        // FP64 local means per work item, one window per lane
-        MeansArgs ma{};
-        ma.work = (const int*)ctx->b_work.p;
-        ma.nwork = d_nwork;
-        ma.nx = nx;
-        ma.ny = ny;
-        ma.nsize = d.nsize;
-        ma.bsw = W;
-        ma.bs1 = (const double*)ctx->b_b1.p;
-        ma.bs2 = (const double*)ctx->b_b2.p;
-        ma.inv_n2 = 1. / ((double)n * n);
-        ma.means = (float4*)ctx->b_means.p;
-        long blocks = std::min<long>((long)(npx + 255) / 256, (long)ctx->nsm * 8);
-        k_means<<<(int)std::max(1l, blocks), 256, 0, st>>>(ma);
-        ++launches;
-    }
-    CK(cudaGetLastError());
+    int grid_div = 1;
+    resolved_config(ctx, p->form, n, &form, &grid_div);
     CK(cudaEventRecord(ctx->ev[1], st));
-
-    WinArgs wa{};
-    fill_tables(p, n, wa.gauss, wa.filt2);
-    wa.use_filter = p->filter;
-    wa.s1 = (const float2*)ctx->b_s1.p;
-    wa.s2 = (const float2*)ctx->b_s2.p;
-    wa.means = (const float4*)ctx->b_means.p;
-    wa.work = (const int*)ctx->b_work.p;
-    wa.nwork = d_nwork;
-    wa.nx = nx;
-    wa.ny = ny;
-    wa.nsize = d.nsize;
-    wa.peaks = (PeakRec*)ctx->b_peaks.p;
-    s = launch_windows(ctx, form, we, n, wa, d_status, st);
+    s = launch_windows(ctx, form, j.we, n, wa, d_status, st, grid_div);
     if (s != FLCT_OK) return s;
     ++launches;
     CK(cudaEventRecord(ctx->ev[2], st));
-    {
-        FitArgs fa{};
-        fa.work = (const int*)ctx->b_work.p;
-        fa.nwork = d_nwork;
-        fa.peaks = (const PeakRec*)ctx->b_peaks.p;
-        fa.n = n;
-        fa.ny = ny;
-        fa.deltinv = 1. / p->deltat;  // flct.c:343
-        fa.deltas = p->deltas;
-        fa.skip = d.skip > 0 ? d.skip : 1;
-        fa.xoff = d.xoff;
-        fa.yoff = d.yoff;
-        fa.jcnt = d.jcnt;
-        fa.vx = d_vx;
-        fa.vy = d_vy;
-        fa.vm = d_vm;
-        fa.gvx = ca.gvx;
-        fa.gvy = ca.gvy;
-        long blocks = std::min<long>((long)(npx + 127) / 128, (long)ctx->nsm * 8);
-        k_fit<<<(int)std::max(1l, blocks), 128, 0, st>>>(fa);
-        ++launches;
-    }
-    CK(cudaGetLastError());
+    s = enqueue_fit(ctx, j, b, st, &launches);
+    if (s != FLCT_OK) return s;
     CK(cudaEventRecord(ctx->ev[7], st));
-
-    if (interp) {
-        unsigned char* ix = (unsigned char*)ctx->b_ix.p;
-        unsigned char* iy = (unsigned char*)ctx->b_iy.p;
-        double* wx = (double*)ix;
-        int* zx = (int*)(ix + (size_t)nx * 4 * sizeof(double));
-        unsigned char* okx = ix + (size_t)nx * (4 * sizeof(double) + sizeof(int));
-        double* wy = (double*)iy;
-        int* zy = (int*)(iy + (size_t)ny * 4 * sizeof(double));
-        unsigned char* oky = iy + (size_t)ny * (4 * sizeof(double) + sizeof(int));
-        k_interp_axis<<<(nx + 127) / 128, 128, 0, st>>>(nx, d.icnt, d.xoff, d.skip, nullptr, zx, wx, okx);
-        k_interp_axis<<<(ny + 127) / 128, 128, 0, st>>>(ny, d.jcnt, d.yoff, d.skip, nullptr, zy, wy, oky);
-        InterpArgs ia{};
-        ia.nx = nx;
-        ia.ny = ny;
-        ia.skip = d.skip;
-        ia.xoff = d.xoff;
-        ia.yoff = d.yoff;
-        ia.gx = d.icnt;
-        ia.gy = d.jcnt;
-        ia.gvx = ca.gvx;
-        ia.gvy = ca.gvy;
-        ia.zx = zx;
-        ia.wx = wx;
-        ia.okx = okx;
-        ia.zy = zy;
-        ia.wy = wy;
-        ia.oky = oky;
-        const size_t hn = (size_t)(d.icnt + 2) * ny;
-        ia.hx = (double*)ctx->b_hrow.p;
-        ia.hy = ia.hx + hn;
-        ia.hbad = (unsigned char*)(ia.hy + hn);
-        ia.vx = d_vx;
-        ia.vy = d_vy;
-        ia.vm = d_vm;
-        long rblocks = std::min<long>((long)(hn + 255) / 256, (long)ctx->nsm * 8);
-        k_interp_rows<<<(int)std::max(1l, rblocks), 256, 0, st>>>(ia);
-        long blocks = std::min<long>((long)(npx + 255) / 256, (long)ctx->nsm * 16);
-        k_interp<<<(int)std::max(1l, blocks), 256, 0, st>>>(ia);
-        launches += 4;
-        CK(cudaGetLastError());
+    if (j.interp) {
+        s = enqueue_interp(ctx, j, b, st, &launches);
+        if (s != FLCT_OK) return s;
     }
     CK(cudaEventRecord(ctx->ev[3], st));
     ctx->timing = flct_timing{};
@@ -579,16 +1238,36 @@ flct_status flct_gpu_velocity_device(flct_ctx* ctx, const flct_params* p, const 
 static flct_status collect_timing(flct_ctx* ctx) {
     ctx->pending = false;
     CK(cudaEventSynchronize(ctx->ev[3]));
-    unsigned char* ctr = (unsigned char*)ctx->b_ctr.p;
-    int nwork = 0;
+    long long nwork = 0;
     unsigned status = 0;
-    CK(cudaMemcpy(&nwork, ctr, sizeof(int), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(&status, ctr + 4, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    const bool batch = ctx->batch_pending > 0;
+    if (batch) {
+        // a batch: every pair's counters
+        std::vector<unsigned char> h((size_t)ctx->batch_pending * 64);
+        ctx->batch_pending = 0;
+        CK(cudaMemcpy(h.data(), ctx->bb_ctr.p, h.size(), cudaMemcpyDeviceToHost));
+        for (size_t k = 0; k < h.size(); k += 64) {
+            int w;
+            unsigned st;
+            memcpy(&w, h.data() + k, sizeof(int));
+            memcpy(&st, h.data() + k + 4, sizeof(unsigned));
+            nwork += w;
+            status |= st;
+        }
+    } else {
+        unsigned char* ctr = (unsigned char*)ctx->b_ctr.p;
+        int w = 0;
+        CK(cudaMemcpy(&w, ctr, sizeof(int), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(&status, ctr + 4, sizeof(unsigned), cudaMemcpyDeviceToHost));
+        nwork = w;
+    }
     ctx->timing.windows = nwork;
-    ctx->timing.ms_prepass = ev_ms(ctx->ev[0], ctx->ev[1]);
-    ctx->timing.ms_window = ev_ms(ctx->ev[1], ctx->ev[2]);
-    ctx->timing.ms_fit = ev_ms(ctx->ev[2], ctx->ev[7]);
-    ctx->timing.ms_interp = ev_ms(ctx->ev[7], ctx->ev[3]);
+    if (!batch) {  // a batch's graph has no per-stage events
+        ctx->timing.ms_prepass = ev_ms(ctx->ev[0], ctx->ev[1]);
+        ctx->timing.ms_window = ev_ms(ctx->ev[1], ctx->ev[2]);
+        ctx->timing.ms_fit = ev_ms(ctx->ev[2], ctx->ev[7]);
+        ctx->timing.ms_interp = ev_ms(ctx->ev[7], ctx->ev[3]);
+    }
     ctx->timing.ms_total = ev_ms(ctx->ev[0], ctx->ev[3]);
     if (status & kStatusRange)
         return fail(ctx, FLCT_ERR_UNSUPPORTED, "an input magnitude exceeds the FP32 range of the GPU kernels");
@@ -877,9 +1556,28 @@ flct_status flct_gpu_warp_frac2d(flct_ctx* ctx, const double* arr, const double*
 }
 
 flct_status flct_gpu_velocity_batch(flct_ctx* ctx, int npairs, const flct_pair* pairs, void* stream) {
-    (void)npairs; (void)pairs; (void)stream;
     if (!ctx) return FLCT_ERR_ARG;
-    return fail(ctx, FLCT_ERR_UNSUPPORTED, "batched velocity is not available yet");
+    if (npairs < 0 || (npairs > 0 && !pairs)) return fail(ctx, FLCT_ERR_ARG, "bad pair list (%d pairs)", npairs);
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    ctx->pending = false;
+    ctx->batch_pending = 0;
+    ctx->timing = flct_timing{};
+    if (npairs == 0) return FLCT_OK;
+    if (!ctx->gexec || ctx->gkey != batch_key(npairs, pairs)) {
+        flct_status s = rebuild_batch(ctx, npairs, pairs, st);
+        if (s != FLCT_OK) return s;
+    }
+    CK(cudaEventRecord(ctx->ev[0], st));
+    CK(cudaGraphLaunch(ctx->gexec, st));
+    CK(cudaEventRecord(ctx->ev[3], st));
+    CK(cudaEventRecord(ctx->bdone, st));
+    ctx->timing.launches = ctx->batch_launches;
+    ctx->timing.box = ctx->batch_box;
+    ctx->timing.form = ctx->batch_form;
+    ctx->pending = true;
+    ctx->batch_pending = npairs;
+    return FLCT_OK;
 }
 
 }  // extern "C"

@@ -73,4 +73,17 @@ __global__ void k_fit(FitArgs a) {
     }
 }
 
+__global__ void k_batch_starts(const unsigned char* ctr, const int* seg_pair, const int* first, int ngroups,
+                               int* start) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= ngroups) return;
+    int* st = start + first[g] + g;
+    int acc = 0;
+    st[0] = 0;
+    for (int k = first[g]; k < first[g + 1]; ++k) {
+        acc += *reinterpret_cast<const int*>(ctr + 64 * (size_t)seg_pair[k]);
+        st[k - first[g] + 1] = acc;
+    }
+}
+
 }  // namespace flct

@@ -51,7 +51,36 @@ struct FitArgs {
     double *shx, *shy;     // raw shifts per work item or null
 };
 
+// One image pair of a batched window launch.  The pair's work items,
+// means and peak records sit at [base, base + its work count) of the
+// batch's arrays; seg_start (device, prefix sums of the work counts, one
+// more entry than segments) maps a launch-wide item index to its pair.
+struct WinSeg {
+    const float2* s1;
+    const float2* s2;
+    int nx, ny;
+    int base;
+    int pad;
+};
+
+// Largest k in [0, nseg) with start[k] <= w (skips pairs without work).
+__device__ __forceinline__ int seg_find(const int* __restrict__ start, int nseg, int w) {
+    int lo = 0, hi = nseg - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(start + mid) <= w) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
 __global__ void k_means(MeansArgs a);
 __global__ void k_fit(FitArgs a);
+
+// Batched launches: for every group g, start[first[g] + g + k] (k = 0..nseg)
+// = prefix sums of the work counts (int at ctr + 64 * pair) of the group's
+// pairs seg_pair[first[g] .. first[g+1]).
+__global__ void k_batch_starts(const unsigned char* ctr, const int* seg_pair, const int* first, int ngroups,
+                               int* start);
 
 }  // namespace flct

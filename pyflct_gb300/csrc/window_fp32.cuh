@@ -34,6 +34,9 @@ struct WinArgs {
     int use_filter;       // -k given
     int direct;           // windows given directly: box w starts at row w*n, unit weights
     PeakRec* peaks;       // per work item: integer peak and its 3x3 |c| stencil
+    const WinSeg* segs;   // batched launch: the pairs (s1, s2, nx, ny unused), else null
+    const int* seg_start; // batched launch: [nseg + 1] item prefix sums; nwork = seg_start + nseg
+    int nseg;
     float gauss[2 * kMaxBox + 1];  // weight of offset d at d + n (separable Gaussian)
     float filt2[kMaxBox];          // squared k-space filter factor by frequency index
 };
@@ -77,34 +80,46 @@ k_window_fp32(WinArgs a) {
     for (int base = blockIdx.x * TEAMS; base < nwork; base += gridDim.x * TEAMS) {
         const int w = base + team;
         const bool valid = w < nwork;
-        const int wi = valid ? w : base;
-        const int pix = a.work[wi];
+        int gi = valid ? w : base;  // item index into work / means / peaks
+        const float2* f1s = a.s1;
+        const float2* f2s = a.s2;
+        int nx = a.nx, ny = a.ny;
+        if (a.nseg > 0) {
+            const int k = seg_find(a.seg_start, a.nseg, gi);
+            const WinSeg sg = a.segs[k];
+            f1s = sg.s1;
+            f2s = sg.s2;
+            nx = sg.nx;
+            ny = sg.ny;
+            gi = sg.base + (gi - __ldg(a.seg_start + k));
+        }
+        const int pix = a.work[gi];
         int i, j, imin, jmin;
         if (a.direct) {
-            imin = pix / a.ny;
+            imin = pix / ny;
             jmin = 0;
             i = imin;
             j = 0;
         } else {
-            i = pix / a.ny;
-            j = pix - i * a.ny;
-            imin = box_start(i, a.nx, a.nsize);
-            jmin = box_start(j, a.ny, a.nsize);
+            i = pix / ny;
+            j = pix - i * ny;
+            imin = box_start(i, nx, a.nsize);
+            jmin = box_start(j, ny, a.nsize);
         }
 
         // windowed, mean-subtracted column jj = ln of both frames: z = g1 + i g2
         float2 x[N];
         {
-            const float4 mm = a.means ? __ldg(a.means + wi) : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float4 mm = a.means ? __ldg(a.means + gi) : make_float4(0.f, 0.f, 0.f, 0.f);
             const float wc = s_g[ln + jmin - j + N];
-            const float2* p1 = a.s1 + (size_t)imin * a.ny + jmin + ln;
-            const float2* p2 = a.s2 + (size_t)imin * a.ny + jmin + ln;
+            const float2* p1 = f1s + (size_t)imin * ny + jmin + ln;
+            const float2* p2 = f2s + (size_t)imin * ny + jmin + ln;
             const float* gr = s_g + (imin - i + N);
             float mx1 = 0.f, mx2 = 0.f;
 #pragma unroll
             for (int ii = 0; ii < N; ++ii) {
-                const float2 u = __ldg(p1 + (size_t)ii * a.ny);
-                const float2 v = __ldg(p2 + (size_t)ii * a.ny);
+                const float2 u = __ldg(p1 + (size_t)ii * ny);
+                const float2 v = __ldg(p2 + (size_t)ii * ny);
                 const float wgt = wc * gr[ii];
                 const float d1 = (u.x - mm.x) + (u.y - mm.y);
                 const float d2 = (v.x - mm.z) + (v.y - mm.w);
@@ -219,7 +234,7 @@ k_window_fp32(WinArgs a) {
             const bool dofit = have && I > 0 && I < N - 1 && J > 0 && J < N - 1;
             if (valid) {
                 // 10 words per record; teams narrower than 10 lanes loop
-                float* rec = reinterpret_cast<float*>(a.peaks + w);
+                float* rec = reinterpret_cast<float*>(a.peaks + gi);
                 for (int k = ln; k < 10; k += N) {
                     if (k < 9) {
                         rec[k] = dofit ? ab[(I - 1 + k / 3) * N + (J - 1 + k % 3)] : 0.f;

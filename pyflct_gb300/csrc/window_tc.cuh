@@ -51,6 +51,9 @@ struct TcArgs {
     int direct;
     int use_filter;
     PeakRec* peaks;
+    const WinSeg* segs;   // batched launch (see WinArgs), else null
+    const int* seg_start;
+    int nseg;
     const float* b1;      // [c][j] 32 x 32: S1 matrix, row = output column c
     const float* b2;      // [n][k] 64 x 64: S2 matrix, n = (re/im, q), k = (re/im, i), kx = tc_kx(q)
     unsigned* status;
@@ -171,6 +174,9 @@ __global__ void __launch_bounds__(128) k_window_tc32(TcArgs a) {
     float4* s_mean = reinterpret_cast<float4*>(sm + TcSmem::off_misc + 512);  // 8
     uint64_t* s_mbar = reinterpret_cast<uint64_t*>(sm + TcSmem::off_misc + 640);
     uint32_t* s_tmem = reinterpret_cast<uint32_t*>(sm + TcSmem::off_misc + 648);
+    int* s_gi = reinterpret_cast<int*>(sm + TcSmem::off_misc + 656);                    // 8
+    const float2** s_src = reinterpret_cast<const float2**>(sm + TcSmem::off_misc + 704);  // 8 x 2
+    int2* s_dim = reinterpret_cast<int2*>(sm + TcSmem::off_misc + 832);                 // 8
 
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
 
@@ -242,7 +248,22 @@ __global__ void __launch_bounds__(128) k_window_tc32(TcArgs a) {
 
     for (int base = blockIdx.x * WIT; base < nwork && ok; base += gridDim.x * WIT) {
         if (t < WIT) {
-            const int w = min(base + t, nwork - 1);
+            int w = min(base + t, nwork - 1);
+            const float2* f1s = a.s1;
+            const float2* f2s = a.s2;
+            int2 dim = make_int2(a.nx, a.ny);
+            if (a.nseg > 0) {
+                const int k = seg_find(a.seg_start, a.nseg, w);
+                const WinSeg sg = a.segs[k];
+                f1s = sg.s1;
+                f2s = sg.s2;
+                dim = make_int2(sg.nx, sg.ny);
+                w = sg.base + (w - __ldg(a.seg_start + k));
+            }
+            s_gi[t] = w;
+            s_src[2 * t] = f1s;
+            s_src[2 * t + 1] = f2s;
+            s_dim[t] = dim;
             s_pix[t] = a.work[w];
             s_mean[t] = a.means ? a.means[w] : make_float4(0.f, 0.f, 0.f, 0.f);
         }
@@ -257,28 +278,29 @@ __global__ void __launch_bounds__(128) k_window_tc32(TcArgs a) {
             for (int tile = 0; tile < 4; ++tile) {
                 const int w = 2 * tile + wl;
                 const int pix = s_pix[w];
+                const int2 dim = s_dim[w];
                 int ic, jc, imin, jmin;
                 if (a.direct) {
-                    imin = pix / a.ny;
+                    imin = pix / dim.y;
                     jmin = 0;
                     ic = imin;
                     jc = 0;
                 } else {
-                    ic = pix / a.ny;
-                    jc = pix - ic * a.ny;
-                    imin = box_start(ic, a.nx, a.nsize);
-                    jmin = box_start(jc, a.ny, a.nsize);
+                    ic = pix / dim.y;
+                    jc = pix - ic * dim.y;
+                    imin = box_start(ic, dim.x, a.nsize);
+                    jmin = box_start(jc, dim.y, a.nsize);
                 }
                 const float4 mm = s_mean[w];
                 const float mh = img ? mm.z : mm.x, ml = img ? mm.w : mm.y;
-                const float2* src = (img ? a.s2 : a.s1) + (size_t)imin * a.ny + jmin + lane;
+                const float2* src = s_src[2 * w + img] + (size_t)imin * dim.y + jmin + lane;
                 const float* gr = s_g + (imin - ic + N);
                 const float gc = s_g[lane + jmin - jc + N];
                 float x[32];
                 float mx = 0.f;
 #pragma unroll
                 for (int i = 0; i < 32; ++i) {
-                    const float2 u = __ldg(src + (size_t)i * a.ny);
+                    const float2 u = __ldg(src + (size_t)i * dim.y);
                     x[i] = ((u.x - mh) + (u.y - ml)) * (gr[i] * gc);
                     mx = fmaxf(mx, fabsf(x[i]));
                 }
@@ -506,7 +528,7 @@ __global__ void __launch_bounds__(128) k_window_tc32(TcArgs a) {
                 }
                 const bool dofit = have && Ip > 0 && Ip < N - 1 && Jp > 0 && Jp < N - 1;
                 if (valid && lane < 10) {
-                    float* rec = reinterpret_cast<float*>(a.peaks + base + wg);
+                    float* rec = reinterpret_cast<float*>(a.peaks + s_gi[wg]);
                     if (lane < 9)
                         rec[lane] = dofit ? stage[(Ip - 1 + lane / 3) * 33 + (Jp - 1 + lane % 3)] : 0.f;
                     else

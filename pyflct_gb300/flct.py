@@ -18,7 +18,7 @@ from . import _lib
 from ._lib import FlctError, Params
 
 __all__ = ["flct", "make_params", "parse_skip", "parse_thresh", "cross_cor", "interpcc2d",
-           "shift_frac2d", "warp_frac2d", "warp", "FlctError"]
+           "shift_frac2d", "warp_frac2d", "warp", "FlctBatch", "flct_batch", "FlctError"]
 
 
 def parse_thresh(thresh) -> tuple[float, bool]:
@@ -186,3 +186,67 @@ def warp(arr, delx, dely, device=0):
     raise FlctError(_lib.ERR_WARP_DIMS,
                     f"warp: bad shift arrays: nx={a.shape[0]}, nxdel={dx.shape[0]}, "
                     f"ny={a.shape[1]}, nydel={dx.shape[1]}")
+
+
+class FlctBatch:
+    """Many frame pairs of uneven sizes and sigmas in one batched GPU call
+    (flct_gpu_velocity_batch): device-resident inputs and outputs, so that
+    repeated runs replay the library's captured CUDA graph.
+
+    shapes: sequence of (nx, ny); params: one flct_params per pair (from
+    make_params).  f1[k], f2[k] are float64 CUDA tensors [nx][ny] to fill;
+    run() computes vx[k], vy[k], vm[k] on the current torch stream."""
+
+    def __init__(self, shapes, params, device=0):
+        import torch
+        if len(shapes) != len(params):
+            raise FlctError(_lib.ERR_ARG, "one params entry per pair is required")
+        # a context of its own: the captured graph and its workspace stay
+        # valid while other calls use the shared context
+        self.ctx = _lib.Context(device)
+        dev = torch.device("cuda", device)
+        self.device = dev
+        z = lambda s: torch.zeros(s, dtype=torch.float64, device=dev)
+        self.f1 = [z(tuple(s)) for s in shapes]
+        self.f2 = [z(tuple(s)) for s in shapes]
+        self.vx = [z(tuple(s)) for s in shapes]
+        self.vy = [z(tuple(s)) for s in shapes]
+        self.vm = [z(tuple(s)) for s in shapes]
+        self.pairs = (_lib.Pair * max(1, len(shapes)))()
+        for k, ((nx, ny), p) in enumerate(zip(shapes, params)):
+            q = self.pairs[k]
+            q.f1, q.f2 = self.f1[k].data_ptr(), self.f2[k].data_ptr()
+            q.nx, q.ny = int(nx), int(ny)
+            q.params = p
+            q.vx, q.vy, q.vm = self.vx[k].data_ptr(), self.vy[k].data_ptr(), self.vm[k].data_ptr()
+        self.npairs = len(shapes)
+
+    def load(self, frames):
+        """Copy (f1, f2) arrays of each pair into the device inputs."""
+        import torch
+        for k, (a, b) in enumerate(frames):
+            self.f1[k].copy_(torch.as_tensor(_f64(a)), non_blocking=False)
+            self.f2[k].copy_(torch.as_tensor(_f64(b)), non_blocking=False)
+
+    def run(self, stream=None):
+        import torch
+        st = stream if stream is not None else torch.cuda.current_stream(self.device)
+        self.ctx.check(self.ctx.lib.flct_gpu_velocity_batch(self.ctx.h, self.npairs, self.pairs,
+                                                             C.c_void_p(st.cuda_stream)))
+
+    def timing(self):
+        return self.ctx.timing()
+
+
+def flct_batch(frames, params, device=0):
+    """Velocity fields of many pairs [(f1, f2), ...] (numpy arrays [nx][ny])
+    with one params per pair, in one batched GPU call.  Returns a list of
+    (vx, vy, vm) numpy arrays."""
+    shapes = [np.shape(a) for a, _ in frames]
+    b = FlctBatch(shapes, params, device)
+    b.load(frames)
+    b.run()
+    import torch
+    torch.cuda.synchronize(b.device)
+    return [(b.vx[k].cpu().numpy(), b.vy[k].cpu().numpy(), b.vm[k].cpu().numpy())
+            for k in range(len(frames))]

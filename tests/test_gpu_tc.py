@@ -93,7 +93,9 @@ def test_auto_form_and_unsupported_box():
     rng = np.random.default_rng(9)
     a = rng.standard_normal((60, 60))
     got = run(a, a, "auto", sigma=8.0)
-    assert _lib.context(0).timing().form == _lib.FORMS["tc_fp16"]
+    # the autotuner measured the candidates on this call's work list and
+    # chose one of the FP32-accurate forms
+    assert _lib.context(0).timing().form in (_lib.FORMS["fp32"], _lib.FORMS["tc_fp16"])
     assert np.all(got[2] == 1)
     with pytest.raises(FlctError) as e:
         run(a, a, "tc_fp16", sigma=4.0)
