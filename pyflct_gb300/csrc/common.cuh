@@ -7,6 +7,7 @@ namespace flct {
 
 // Missing-value marker of the reference (flct.c:279).
 constexpr double kXmiss = -999999.;
+constexpr float kXmissF = -999999.f;  // exact in FP32
 
 // Status bits a kernel may raise in the context's device status word.
 enum : unsigned {
@@ -28,6 +29,44 @@ __device__ __forceinline__ float2 split_double(double a) {
     float hi = __double2float_rn(a);
     float lo = __double2float_rn(__dsub_rn(a, (double)hi));
     return make_float2(hi, lo);
+}
+
+// split_double with integer operations on the normal-range path (GB300's
+// FP64 pipe is narrow, and conversions to and from double run on it).
+// Bit-identical to split_double except that a zero remainder is +0:
+//   hi = x rounded to 24 bits (ties to even), D = the signed 29-bit rest of
+//   the mantissa, lo = float(D) * 2^(e-52) (exact: a power-of-two scale of
+//   a normal float).  Exponents outside [-74, 126], zeros' signs and
+//   non-finite values take the FP64 path.
+__device__ __forceinline__ float2 split_double_fast(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7ffu) - 1023;
+    if (e < -74 || e > 126) {
+        if ((b << 1) == 0ull) return make_float2(__int_as_float((int)((b >> 32) & 0x80000000u)), 0.0f);
+        return split_double(x);
+    }
+    const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+    const unsigned long long mi = (b & 0xfffffffffffffull) | (1ull << 52);
+    unsigned top = (unsigned)(mi >> 29);             // 24 bits with the implicit one
+    const unsigned rem = (unsigned)(mi & 0x1fffffffu);
+    const bool up = rem > 0x10000000u || (rem == 0x10000000u && (top & 1u));
+    top += up ? 1u : 0u;                             // 2^24 carries into the exponent below
+    const float hi = __uint_as_float(sign | ((unsigned)(e + 126) << 23) + top);
+    const int D = (int)rem - (up ? (1 << 29) : 0);
+    const float lo = (D == 0) ? 0.0f : __int2float_rn(D) * __uint_as_float(sign | ((unsigned)(e - 52 + 127) << 23));
+    return make_float2(hi, lo);
+}
+
+// Exact float -> double with integer operations for normal floats and
+// zeros; subnormals, infinities and NaN take the conversion instruction.
+__device__ __forceinline__ double f2d(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned E = (u >> 23) & 0xffu;
+    const unsigned long long s = (unsigned long long)(u >> 31) << 63;
+    if (E == 0u && (u & 0x7fffffu) == 0u) return __longlong_as_double((long long)s);
+    if (E == 0u || E == 255u) return (double)f;
+    return __longlong_as_double(
+        (long long)(s | ((unsigned long long)(E + 896u) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29)));
 }
 
 // Power-of-two factor bringing a non-negative float (given as its bits) into

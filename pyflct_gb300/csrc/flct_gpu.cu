@@ -84,11 +84,11 @@ struct flct_ctx {
         size_t n = 0;
     };
     Buf b_s1, b_s2, b_work, b_ctr, b_r1, b_r2, b_b1, b_b2, b_gvx, b_gvy, b_ix, b_iy;
-    Buf b_f1, b_f2, b_vx, b_vy, b_vm, b_aux1, b_aux2, b_means, b_peaks, b_hrow;
+    Buf b_f1, b_f2, b_vx, b_vy, b_vm, b_aux1, b_aux2, b_means, b_peaks, b_grid;
     std::vector<Buf*> all() {
         return {&b_s1,   &b_s2,   &b_work,   &b_ctr,    &b_r1,     &b_r2,     &b_b1,     &b_b2,
                 &b_gvx,  &b_gvy,  &b_ix,     &b_iy,     &b_f1,     &b_f2,     &b_vx,     &b_vy,
-                &b_vm,   &b_aux1, &b_aux2,   &b_means,  &b_peaks,  &b_hrow,   &b_tc,     &bb_arena,
+                &b_vm,   &b_aux1, &b_aux2,   &b_means,  &b_peaks,  &b_grid,   &b_tc,     &bb_arena,
                 &bb_work, &bb_means, &bb_peaks, &bb_ctr, &bb_meta};
     }
     int bps[sizeof(kWin) / sizeof(kWin[0])] = {0};
@@ -428,6 +428,9 @@ struct Job {
     int n = 0;
     const WinEntry* we = nullptr;
     bool interp = false;
+    // window grid: pixel (xo + q gs, yo + m gs), q < gi, m < gj (every
+    // pixel without -s)
+    int gs = 1, xo = 0, yo = 0, gi = 0, gj = 0;
 };
 
 flct_status plan_job(flct_ctx* ctx, const flct_params* p, const double* f1, const double* f2, int nx, int ny,
@@ -454,6 +457,16 @@ flct_status plan_job(flct_ctx* ctx, const flct_params* p, const double* f1, cons
     j->nx = nx;
     j->ny = ny;
     j->interp = j->d.skip > 0 && p->interpolate;
+    if (j->d.skip > 0) {
+        j->gs = j->d.skip;
+        j->xo = j->d.xoff;
+        j->yo = j->d.yoff;
+        j->gi = grid_count(nx, j->xo, j->gs);
+        j->gj = grid_count(ny, j->yo, j->gs);
+    } else {
+        j->gi = nx;
+        j->gj = ny;
+    }
     return FLCT_OK;
 }
 
@@ -465,41 +478,31 @@ struct JobBufs {
     int* work = nullptr;
     float4* means = nullptr;
     PeakRec* peaks = nullptr;
-    double* r1 = nullptr;
+    double* r1 = nullptr;  // row sums [gj][nx]
     double* r2 = nullptr;
-    double* b1 = nullptr;
+    double* b1 = nullptr;  // box sums [gi][gj]
     double* b2 = nullptr;
     // 64 bytes: [0] work count (int), [4] status bits, [8..23] |f1|,|f2|
     // maxima, [24..31] relative threshold
     unsigned char* ctr = nullptr;
-    double* gvx = nullptr;
-    double* gvy = nullptr;
-    unsigned char* hrow = nullptr;
-    unsigned char* ix = nullptr;
-    unsigned char* iy = nullptr;
+    float2* grid = nullptr;  // skip-grid (vx, vy) [gi][gj] for the interpolation
 };
 
 // Bytes of each workspace region of a job.
 struct JobSizes {
-    size_t s = 0, work = 0, means = 0, peaks = 0, r = 0, b = 0, gv = 0, hrow = 0, ix = 0, iy = 0;
+    size_t s = 0, work = 0, means = 0, peaks = 0, r = 0, b = 0, grid = 0;
 };
 
 JobSizes job_sizes(const Job& j) {
     const size_t npx = (size_t)j.nx * j.ny;
-    const int W = j.ny - j.n + 1, H = j.nx - j.n + 1;
     JobSizes z;
     z.s = npx * sizeof(float2);
     z.work = npx * sizeof(int);
     z.means = npx * sizeof(float4);
     z.peaks = npx * sizeof(PeakRec);
-    z.r = (size_t)j.nx * W * sizeof(double);
-    z.b = (size_t)H * W * sizeof(double);
-    if (j.interp) {
-        z.gv = (size_t)j.d.icnt * j.d.jcnt * sizeof(double);
-        z.hrow = (size_t)(j.d.icnt + 2) * j.ny * (2 * sizeof(double) + 1);
-        z.ix = (size_t)j.nx * (4 * sizeof(double) + sizeof(int) + 1) + 64;
-        z.iy = (size_t)j.ny * (4 * sizeof(double) + sizeof(int) + 1) + 64;
-    }
+    z.r = (size_t)j.gj * j.nx * sizeof(double);
+    z.b = (size_t)j.gi * j.gj * sizeof(double);
+    if (j.interp) z.grid = (size_t)j.gi * j.gj * sizeof(float2);
     return z;
 }
 
@@ -539,21 +542,36 @@ flct_status enqueue_prepass(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaS
     ca.vx = j.vx;
     ca.vy = j.vy;
     ca.vm = j.vm;
-    ca.gvx = j.interp ? b.gvx : nullptr;
-    ca.gvy = j.interp ? b.gvy : nullptr;
+    ca.grid = j.interp ? b.grid : nullptr;
     ca.status = d_status;
     {
-        long blocks = std::min<long>((long)(npx + 255) / 256, (long)ctx->nsm * 8);
-        k_classify<<<(int)std::max(1l, blocks), 256, 0, st>>>(ca);
+        const long tiles = (long)nx * ((ny + 255) / 256);
+        k_classify<<<(int)std::min<long>(tiles, (long)ctx->nsm * 8), 256, 0, st>>>(ca);
         ++*launches;
     }
     {
-        const int nseg = (W + kSeg - 1) / kSeg;
-        long t = (long)nx * nseg;
-        k_rowsum<<<(int)((t + 127) / 128), 128, 0, st>>>(j.f1, j.f2, nx, ny, n, b.r1, b.r2);
-        const int hseg = (H + kSeg - 1) / kSeg;
-        t = (long)W * hseg;
-        k_colsum<<<(int)((t + 127) / 128), 128, 0, st>>>(b.r1, b.r2, nx, W, n, b.b1, b.b2);
+        // FP64 box sums at the boxes of the window grid
+        BoxArgs ba{};
+        ba.f1 = j.f1;
+        ba.f2 = j.f2;
+        ba.nx = nx;
+        ba.ny = ny;
+        ba.n = n;
+        ba.nsize = j.d.nsize;
+        ba.gs = j.gs;
+        ba.xo = j.xo;
+        ba.yo = j.yo;
+        ba.gi = j.gi;
+        ba.gj = j.gj;
+        ba.seg = std::max(8, n / j.gs);
+        ba.rt1 = b.r1;
+        ba.rt2 = b.r2;
+        ba.b1 = b.b1;
+        ba.b2 = b.b2;
+        long t = (long)nx * ((j.gj + ba.seg - 1) / ba.seg);
+        k_box_rows<<<(int)((t + 127) / 128), 128, 0, st>>>(ba);
+        t = (long)j.gj * ((j.gi + ba.seg - 1) / ba.seg);
+        k_box_cols<<<(int)((t + 127) / 128), 128, 0, st>>>(ba);
         *launches += 2;
     }
     {
@@ -561,10 +579,11 @@ flct_status enqueue_prepass(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaS
         MeansArgs ma{};
         ma.work = b.work;
         ma.nwork = d_nwork;
-        ma.nx = nx;
         ma.ny = ny;
-        ma.nsize = j.d.nsize;
-        ma.bsw = W;
+        ma.gs = j.gs;
+        ma.xo = j.xo;
+        ma.yo = j.yo;
+        ma.gj = j.gj;
         ma.bs1 = b.b1;
         ma.bs2 = b.b2;
         ma.inv_n2 = 1. / ((double)n * n);
@@ -609,8 +628,7 @@ flct_status enqueue_fit(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaStrea
     fa.vx = j.vx;
     fa.vy = j.vy;
     fa.vm = j.vm;
-    fa.gvx = j.interp ? b.gvx : nullptr;
-    fa.gvy = j.interp ? b.gvy : nullptr;
+    fa.grid = j.interp ? b.grid : nullptr;
     const size_t npx = (size_t)j.nx * j.ny;
     long blocks = std::min<long>((long)(npx + 127) / 128, (long)ctx->nsm * 8);
     k_fit<<<(int)std::max(1l, blocks), 128, 0, st>>>(fa);
@@ -619,47 +637,25 @@ flct_status enqueue_fit(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaStrea
     return FLCT_OK;
 }
 
-// Cubic-convolution interpolation of the skip grid onto the skipped pixels
-// (flct.c:958-1133).
+// Cubic-convolution interpolation of the skip grid onto the skipped pixels,
+// mask and xmiss reset (flct.c:958-1133).
 flct_status enqueue_interp(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaStream_t st, int* launches) {
-    const int nx = j.nx, ny = j.ny;
-    const size_t npx = (size_t)nx * ny;
-    double* wx = (double*)b.ix;
-    int* zx = (int*)(b.ix + (size_t)nx * 4 * sizeof(double));
-    unsigned char* okx = b.ix + (size_t)nx * (4 * sizeof(double) + sizeof(int));
-    double* wy = (double*)b.iy;
-    int* zy = (int*)(b.iy + (size_t)ny * 4 * sizeof(double));
-    unsigned char* oky = b.iy + (size_t)ny * (4 * sizeof(double) + sizeof(int));
-    k_interp_axis<<<(nx + 127) / 128, 128, 0, st>>>(nx, j.d.icnt, j.d.xoff, j.d.skip, nullptr, zx, wx, okx);
-    k_interp_axis<<<(ny + 127) / 128, 128, 0, st>>>(ny, j.d.jcnt, j.d.yoff, j.d.skip, nullptr, zy, wy, oky);
     InterpArgs ia{};
-    ia.nx = nx;
-    ia.ny = ny;
+    ia.nx = j.nx;
+    ia.ny = j.ny;
     ia.skip = j.d.skip;
     ia.xoff = j.d.xoff;
     ia.yoff = j.d.yoff;
     ia.gx = j.d.icnt;
     ia.gy = j.d.jcnt;
-    ia.gvx = b.gvx;
-    ia.gvy = b.gvy;
-    ia.zx = zx;
-    ia.wx = wx;
-    ia.okx = okx;
-    ia.zy = zy;
-    ia.wy = wy;
-    ia.oky = oky;
-    const size_t hn = (size_t)(j.d.icnt + 2) * ny;
-    ia.hx = (double*)b.hrow;
-    ia.hy = ia.hx + hn;
-    ia.hbad = (unsigned char*)(ia.hy + hn);
+    ia.grid = b.grid;
     ia.vx = j.vx;
     ia.vy = j.vy;
     ia.vm = j.vm;
-    long rblocks = std::min<long>((long)(hn + 255) / 256, (long)ctx->nsm * 8);
-    k_interp_rows<<<(int)std::max(1l, rblocks), 256, 0, st>>>(ia);
-    long blocks = std::min<long>((long)(npx + 255) / 256, (long)ctx->nsm * 16);
-    k_interp<<<(int)std::max(1l, blocks), 256, 0, st>>>(ia);
-    *launches += 4;
+    const int bx = std::min(4, (j.ny + 255) / 256);
+    const int by = std::min(j.nx, std::max(1, ctx->nsm * 8 / bx));
+    k_interp_grid<<<dim3(bx, by), 256, 0, st>>>(ia);
+    ++*launches;
     CK(cudaGetLastError());
     return FLCT_OK;
 }
@@ -791,7 +787,7 @@ flct_status plan_batch(flct_ctx* ctx, int npairs, const flct_pair* pairs, BatchP
     }
     // workspace: per-pair arena slices, item-indexed arrays shared by all pairs
     struct Off {
-        size_t s1, s2, r1, r2, b1, b2, gvx, gvy, hrow, ix, iy;
+        size_t s1, s2, r1, r2, b1, b2, grid;
         long long base;
     };
     std::vector<Off> off(npairs);
@@ -811,11 +807,7 @@ flct_status plan_batch(flct_ctx* ctx, int npairs, const flct_pair* pairs, BatchP
         o.r2 = take(z.r);
         o.b1 = take(z.b);
         o.b2 = take(z.b);
-        o.gvx = take(z.gv);
-        o.gvy = take(z.gv);
-        o.hrow = take(z.hrow);
-        o.ix = take(z.ix);
-        o.iy = take(z.iy);
+        o.grid = take(z.grid);
         o.base = items;
         items += (long long)bp->jobs[k].nx * bp->jobs[k].ny;
     }
@@ -842,11 +834,7 @@ flct_status plan_batch(flct_ctx* ctx, int npairs, const flct_pair* pairs, BatchP
         b.r2 = (double*)(A + o.r2);
         b.b1 = (double*)(A + o.b1);
         b.b2 = (double*)(A + o.b2);
-        b.gvx = (double*)(A + o.gvx);
-        b.gvy = (double*)(A + o.gvy);
-        b.hrow = A + o.hrow;
-        b.ix = A + o.ix;
-        b.iy = A + o.iy;
+        b.grid = (float2*)(A + o.grid);
         b.work = (int*)ctx->bb_work.p + o.base;
         b.means = (float4*)ctx->bb_means.p + o.base;
         b.peaks = (PeakRec*)ctx->bb_peaks.p + o.base;
@@ -1168,11 +1156,7 @@ flct_status flct_gpu_velocity_device(flct_ctx* ctx, const flct_params* p, const 
     ENSURE(ctx->b_means, z.means);
     ENSURE(ctx->b_peaks, z.peaks);
     if (j.interp) {
-        ENSURE(ctx->b_hrow, z.hrow);
-        ENSURE(ctx->b_gvx, z.gv);
-        ENSURE(ctx->b_gvy, z.gv);
-        ENSURE(ctx->b_ix, z.ix);
-        ENSURE(ctx->b_iy, z.iy);
+        ENSURE(ctx->b_grid, z.grid);
     }
     JobBufs b;
     b.s1 = (float2*)ctx->b_s1.p;
@@ -1185,11 +1169,7 @@ flct_status flct_gpu_velocity_device(flct_ctx* ctx, const flct_params* p, const 
     b.b1 = (double*)ctx->b_b1.p;
     b.b2 = (double*)ctx->b_b2.p;
     b.ctr = (unsigned char*)ctx->b_ctr.p;
-    b.gvx = (double*)ctx->b_gvx.p;
-    b.gvy = (double*)ctx->b_gvy.p;
-    b.hrow = (unsigned char*)ctx->b_hrow.p;
-    b.ix = (unsigned char*)ctx->b_ix.p;
-    b.iy = (unsigned char*)ctx->b_iy.p;
+    b.grid = (float2*)ctx->b_grid.p;
     unsigned* d_status = (unsigned*)(b.ctr + 4);
 
     int launches = 0;

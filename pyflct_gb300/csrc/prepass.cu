@@ -5,11 +5,14 @@
 //                               float hi+lo split of both frames, and the
 //                               final values of pixels without a window
 //                               (flct.c:721-755, 918-930, 1125-1133)
-//   k_rowsum / k_colsum         FP64 box sums for the local means
-//                               (flct.c:815-827) as sliding sums
-//   k_interp                    skip-grid cubic-convolution interpolation
+//   k_box_rows / k_box_cols     FP64 box sums for the local means
+//                               (flct.c:815-827) as sliding sums, at the
+//                               boxes the skip grid needs
+//   k_interp_grid               skip-grid cubic-convolution interpolation
 //                               (flct.c:958-1120 with interpcc2d,
 //                               flct.c:2226-2463) and the xmiss reset
+//   k_interp_axis / k_interp_general   interpcc2d itself (FP64, reference
+//                               order) for the standalone entry points
 #include "prepass.cuh"
 
 namespace flct {
@@ -59,48 +62,72 @@ __global__ void k_thresh_final(const double* __restrict__ f1, const double* __re
 
 // ------------------------------------------------------- classify ----
 
-__global__ void k_classify(ClassifyArgs a) {
-    const long n = (long)a.nx * a.ny;
+// One tile = 256 consecutive pixels of one row, one per thread.  The work
+// list grows by one atomic per tile (block-wide ballot counts); the float
+// split of both frames uses integer operations, and the threshold test
+// 0.5*|f1+f2| < thresh (flct.c:721-722) needs one FP64 add only when the
+// threshold is positive (otherwise no pixel is below it).
+__global__ void __launch_bounds__(256) k_classify(ClassifyArgs a) {
+    __shared__ int s_cnt[8];
+    __shared__ int s_base;
     const double thr = a.thr_ptr ? *a.thr_ptr : a.thr_val;
-    const int lane = threadIdx.x & 31;
-    const long stride = (long)gridDim.x * blockDim.x;
-    // whole warps iterate together so the ballot sees every lane
-    for (long base = blockIdx.x * (long)blockDim.x + (threadIdx.x & ~31); base < n; base += stride) {
-        const long k = base + lane;
-        const bool act = k < n;
+    const unsigned long long tb = (unsigned long long)__double_as_longlong(thr);
+    // thr in (0, +inf]: compare |s|/2 with it as bit patterns
+    const bool thr_pos = (long long)tb > 0ll && tb <= 0x7ff0000000000000ull;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int tpr = (a.ny + 255) >> 8;  // tiles per row
+    const long ntile = (long)a.nx * tpr;
+    for (long t = blockIdx.x; t < ntile; t += gridDim.x) {
+        const int i = (int)(t / tpr);
+        const int j = (int)(t - (long)i * tpr) * 256 + threadIdx.x;
+        const bool act = j < a.ny;
+        const size_t k = (size_t)i * a.ny + j;
         bool comp = false, grid = false;
-        int i = 0, j = 0;
         if (act) {
             const double fa = a.f1[k], fb = a.f2[k];
-            const float2 sa = split_double(fa), sb = split_double(fb);
+            const float2 sa = split_double_fast(fa), sb = split_double_fast(fb);
             a.s1[k] = sa;
             a.s2[k] = sb;
             if ((isinf(sa.x) && !isinf(fa)) || (isinf(sb.x) && !isinf(fb))) atomicOr(a.status, kStatusRange);
-            i = (int)(k / a.ny);
-            j = (int)(k - (long)i * a.ny);
-            // 0.5*|f1+f2| < thresh in FP64 (flct.c:721-722)
-            const bool below = __dmul_rn(0.5, fabs(__dadd_rn(fa, fb))) < thr;
+            bool below = false;
+            if (thr_pos) {
+                const unsigned long long sb2 =
+                    (unsigned long long)__double_as_longlong(__dadd_rn(fa, fb)) & 0x7fffffffffffffffull;
+                const unsigned E = (unsigned)(sb2 >> 52);
+                if (E >= 2u && E < 0x7ffu) below = (sb2 - (1ull << 52)) < tb;  // exact halving
+                else if (E == 0x7ffu) below = sb2 < tb;                         // inf / NaN
+                else below = __dmul_rn(0.5, __longlong_as_double((long long)sb2)) < thr;
+            }
             grid = (a.skip > 0) ? (!((i - a.xoff) % a.skip) && !((j - a.yoff) % a.skip)) : true;
             comp = !below && grid;
         }
         const unsigned m = __ballot_sync(0xffffffffu, comp);
-        int slot = 0;
-        if (lane == 0 && m) slot = atomicAdd(a.nwork, __popc(m));
-        slot = __shfl_sync(0xffffffffu, slot, 0);
+        if (lane == 0) s_cnt[warp] = __popc(m);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int tot = 0;
+#pragma unroll
+            for (int w = 0; w < 8; ++w) {
+                const int c = s_cnt[w];
+                s_cnt[w] = tot;
+                tot += c;
+            }
+            s_base = tot ? atomicAdd(a.nwork, tot) : 0;
+        }
+        __syncthreads();
         if (comp) {
-            a.work[slot + __popc(m & ((1u << lane) - 1u))] = (int)k;
+            a.work[s_base + s_cnt[warp] + __popc(m & ((1u << lane) - 1u))] = (int)k;
         } else if (act) {
             // pixels without a window: (xmiss, xmiss, 0) then the reset gives
             // (0, 0, 0); skipped pixels that will be interpolated are left to
-            // k_interp.
+            // the interpolation.
             if (grid) {
                 a.vx[k] = 0.;
                 a.vy[k] = 0.;
                 a.vm[k] = 0.;
-                if (a.gvx) {
+                if (a.grid) {
                     const int ic = (i - a.xoff) / a.skip, jc = (j - a.yoff) / a.skip;
-                    a.gvx[(size_t)ic * a.jcnt + jc] = kXmiss;
-                    a.gvy[(size_t)ic * a.jcnt + jc] = kXmiss;
+                    a.grid[(size_t)ic * a.jcnt + jc] = make_float2(kXmissF, kXmissF);
                 }
             } else if (!a.interpolate) {
                 a.vx[k] = 0.;
@@ -108,6 +135,7 @@ __global__ void k_classify(ClassifyArgs a) {
                 a.vm[k] = 0.;
             }
         }
+        __syncthreads();  // s_cnt / s_base are rewritten by the next tile
     }
 }
 
@@ -129,59 +157,67 @@ __device__ __forceinline__ double slide(double sum, double in, double out, int n
     return t;
 }
 
-// R[i][s] = sum_{jj<n} f[i][s+jj] for s in [0, ny-n]; one thread per row
-// segment of kSeg outputs: n adds to start, then two per step.
-__global__ void k_rowsum(const double* __restrict__ f1, const double* __restrict__ f2, int nx,
-                         int ny, int n, double* __restrict__ r1, double* __restrict__ r2) {
-    const int W = ny - n + 1;
-    const int nseg = (W + kSeg - 1) / kSeg;
+// Row sums RT[m][i] = sum_{jj<n} f[i][s_m + jj] at the grid's box columns
+// s_m = box_start(yo + m gs).  One thread per (row, run of `seg` grid
+// columns): n adds for the first box, then one column step (an add and a
+// subtract) per column between consecutive boxes.  Consecutive threads take
+// consecutive rows, so the transposed stores are coalesced.
+__global__ void k_box_rows(BoxArgs a) {
+    const int nseg = (a.gj + a.seg - 1) / a.seg;
     const long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (idx >= (long)nx * nseg) return;
-    const int i = (int)(idx / nseg);
-    const int s0 = (int)(idx - (long)i * nseg) * kSeg;
-    const int s1 = min(s0 + kSeg, W);
-    const double* a = f1 + (size_t)i * ny;
-    const double* b = f2 + (size_t)i * ny;
+    if (idx >= (long)a.nx * nseg) return;
+    const int sg = (int)(idx / a.nx);
+    const int i = (int)(idx - (long)sg * a.nx);
+    const int m0 = sg * a.seg, m1 = min(m0 + a.seg, a.gj);
+    const double* f = a.f1 + (size_t)i * a.ny;
+    const double* g = a.f2 + (size_t)i * a.ny;
+    int s = box_start(a.yo + m0 * a.gs, a.ny, a.nsize);
     double sa = 0., sb = 0.;
-    for (int jj = 0; jj < n; ++jj) {
-        sa = __dadd_rn(sa, a[s0 + jj]);
-        sb = __dadd_rn(sb, b[s0 + jj]);
+    for (int jj = 0; jj < a.n; ++jj) {
+        sa = __dadd_rn(sa, f[s + jj]);
+        sb = __dadd_rn(sb, g[s + jj]);
     }
-    r1[(size_t)i * W + s0] = sa;
-    r2[(size_t)i * W + s0] = sb;
-    for (int s = s0 + 1; s < s1; ++s) {
-        sa = slide(sa, a[s + n - 1], a[s - 1], n, [&](int q) { return a[s + q]; });
-        sb = slide(sb, b[s + n - 1], b[s - 1], n, [&](int q) { return b[s + q]; });
-        r1[(size_t)i * W + s] = sa;
-        r2[(size_t)i * W + s] = sb;
+    a.rt1[(size_t)m0 * a.nx + i] = sa;
+    a.rt2[(size_t)m0 * a.nx + i] = sb;
+    for (int m = m0 + 1; m < m1; ++m) {
+        const int s1 = box_start(a.yo + m * a.gs, a.ny, a.nsize);
+        for (; s < s1; ++s) {
+            sa = slide(sa, f[s + a.n], f[s], a.n, [&](int q) { return f[s + 1 + q]; });
+            sb = slide(sb, g[s + a.n], g[s], a.n, [&](int q) { return g[s + 1 + q]; });
+        }
+        a.rt1[(size_t)m * a.nx + i] = sa;
+        a.rt2[(size_t)m * a.nx + i] = sb;
     }
 }
 
-// S[t][s] = sum_{ii<n} R[t+ii][s] for t in [0, nx-n]; consecutive threads
-// take consecutive columns s (coalesced), each a segment of kSeg rows.
-__global__ void k_colsum(const double* __restrict__ r1, const double* __restrict__ r2, int nx,
-                         int W, int n, double* __restrict__ b1, double* __restrict__ b2) {
-    const int H = nx - n + 1;
-    const int nseg = (H + kSeg - 1) / kSeg;
+// Box sums B[q][m] = sum_{ii<n} RT[m][t_q + ii] at the grid's box rows
+// t_q = box_start(xo + q gs); one thread per (grid column, run of `seg`
+// grid rows), consecutive threads on consecutive columns.
+__global__ void k_box_cols(BoxArgs a) {
+    const int nseg = (a.gi + a.seg - 1) / a.seg;
     const long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (idx >= (long)W * nseg) return;
-    const int seg = (int)(idx / W);
-    const int s = (int)(idx - (long)seg * W);
-    const int t0 = seg * kSeg, t1 = min(t0 + kSeg, H);
+    if (idx >= (long)a.gj * nseg) return;
+    const int sg = (int)(idx / a.gj);
+    const int m = (int)(idx - (long)sg * a.gj);
+    const int q0 = sg * a.seg, q1 = min(q0 + a.seg, a.gi);
+    const double* r = a.rt1 + (size_t)m * a.nx;
+    const double* u = a.rt2 + (size_t)m * a.nx;
+    int t = box_start(a.xo + q0 * a.gs, a.nx, a.nsize);
     double sa = 0., sb = 0.;
-    for (int ii = 0; ii < n; ++ii) {
-        sa = __dadd_rn(sa, r1[(size_t)(t0 + ii) * W + s]);
-        sb = __dadd_rn(sb, r2[(size_t)(t0 + ii) * W + s]);
+    for (int ii = 0; ii < a.n; ++ii) {
+        sa = __dadd_rn(sa, r[t + ii]);
+        sb = __dadd_rn(sb, u[t + ii]);
     }
-    b1[(size_t)t0 * W + s] = sa;
-    b2[(size_t)t0 * W + s] = sb;
-    for (int t = t0 + 1; t < t1; ++t) {
-        sa = slide(sa, r1[(size_t)(t + n - 1) * W + s], r1[(size_t)(t - 1) * W + s], n,
-                   [&](int q) { return r1[(size_t)(t + q) * W + s]; });
-        sb = slide(sb, r2[(size_t)(t + n - 1) * W + s], r2[(size_t)(t - 1) * W + s], n,
-                   [&](int q) { return r2[(size_t)(t + q) * W + s]; });
-        b1[(size_t)t * W + s] = sa;
-        b2[(size_t)t * W + s] = sb;
+    a.b1[(size_t)q0 * a.gj + m] = sa;
+    a.b2[(size_t)q0 * a.gj + m] = sb;
+    for (int q = q0 + 1; q < q1; ++q) {
+        const int t1 = box_start(a.xo + q * a.gs, a.nx, a.nsize);
+        for (; t < t1; ++t) {
+            sa = slide(sa, r[t + a.n], r[t], a.n, [&](int k) { return r[t + 1 + k]; });
+            sb = slide(sb, u[t + a.n], u[t], a.n, [&](int k) { return u[t + 1 + k]; });
+        }
+        a.b1[(size_t)q * a.gj + m] = sa;
+        a.b2[(size_t)q * a.gj + m] = sb;
     }
 }
 
@@ -269,75 +305,107 @@ __device__ __forceinline__ double interp_one(const double* __restrict__ g, int g
     return bad ? xmiss : acc;
 }
 
-// Separable form of the velocity pipeline's interpolation.  Every output in
-// column j contracts the same cdata rows with the same ry weights, so
-//   H[a][j] = sum_q cdata[a][jz(j)+q] ry_j[q]      (k_interp_rows, once)
-//   out[i][j] = sum_p rx_i[p] H[iz(i)+p][j]          (k_interp, per pixel)
-// which is the reference's 4x4 sum regrouped (equal up to the last bits of
-// the FP64 rounding); the xmiss test is the same set of 16 comparisons,
-// split the same way, so the mask is exact.
-__global__ void k_interp_rows(InterpArgs a) {
-    const long n = (long)(a.gx + 2) * a.ny;
-    for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
-        const int r = (int)(k / a.ny), j = (int)(k - (long)(k / a.ny) * a.ny);
-        if (!a.oky[j]) continue;  // out of range: every output of column j is xmiss
-        const int jz = a.zy[j];
-        double hx = 0., hy = 0.;
-        unsigned char bad = 0;
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const double ry = a.wy[(size_t)j * 4 + q];
-            const int b = jz + q;
-            double cx, cy;
-            if (r >= 1 && r <= a.gx && b >= 1 && b <= a.gy) {
-                cx = a.gvx[(size_t)(r - 1) * a.gy + (b - 1)];
-                cy = a.gvy[(size_t)(r - 1) * a.gy + (b - 1)];
-            } else {
-                cx = cdata_at(a.gvx, a.gx, a.gy, r, b);
-                cy = cdata_at(a.gvy, a.gx, a.gy, r, b);
-            }
-            hx = fma(cx, ry, hx);
-            hy = fma(cy, ry, hy);
-            bad |= (cx == kXmiss ? 1 : 0) | (cy == kXmiss ? 2 : 0);
-        }
-        a.hx[k] = hx;
-        a.hy[k] = hy;
-        a.hbad[k] = bad;
-    }
+// The velocity pipeline's interpolation of the skip grid onto the skipped
+// pixels (flct.c:958-1120 with interpcc2d, flct.c:2226-2463), the mask 0.5
+// and the final xmiss reset (flct.c:1125-1133), fused in one pass with FP32
+// arithmetic (velocities interpolate to ~1e-7 relative; the FP64 reference
+// order is kept by the standalone interpcc2d entry point instead).
+//
+// The range test and izero come from integer arithmetic on (i - offset)
+// and skip, exactly as the reference's xwant = (i - offset)/skip gives
+// them; a stencil holding xmiss yields xmiss (so the mask is exact).
+
+// Keys kernel, a = -0.5 (flct.c:2398-2419).
+__device__ __forceinline__ float keys_f(float t) {
+    return (t >= 1.0f) ? ((-0.5f * t + 2.5f) * t - 4.0f) * t + 2.0f : (1.5f * t - 2.5f) * t * t + 1.0f;
 }
 
-__global__ void k_interp(InterpArgs a) {
-    const long n = (long)a.nx * a.ny;
-    for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
-        const int i = (int)(k / a.ny), j = (int)(k - (long)(k / a.ny) * a.ny);
-        const bool gi = !((i - a.xoff) % a.skip), gj = !((j - a.yoff) % a.skip);
-        if (gi && gj) continue;  // grid points keep their computed value
-        double vx = kXmiss, vy = kXmiss;
-        if (a.okx[i] && a.oky[j]) {
-            const int iz = a.zx[i];
-            double sx = 0., sy = 0.;
-            unsigned char bad = 0;
+// cdata[a][b] of the border-extended grid (flct.c:2257-2336) for one of the
+// two components (c = 0: vx, 1: vy).
+__device__ __forceinline__ float cdata_f(const float2* __restrict__ g, int gx, int gy, int a, int b, int c) {
+    auto F = [&](int p, int q) -> float {
+        const float2 v = g[(size_t)p * gy + q];
+        return c ? v.y : v.x;
+    };
+    auto row_edge = [&](int p, int q) -> float {  // interior row p, border column q
+        if (q == 0) return (F(p, 2) - 3.f * F(p, 1)) + 3.f * F(p, 0);
+        return (F(p, gy - 3) - 3.f * F(p, gy - 2)) + 3.f * F(p, gy - 1);
+    };
+    auto col_edge = [&](int p, int q) -> float {  // border row p, interior column q
+        if (p == 0) return (F(2, q) - 3.f * F(1, q)) + 3.f * F(0, q);
+        return (F(gx - 3, q) - 3.f * F(gx - 2, q)) + 3.f * F(gx - 1, q);
+    };
+    const bool ra = (a >= 1 && a <= gx), rb = (b >= 1 && b <= gy);
+    if (ra && rb) return F(a - 1, b - 1);
+    if (ra) return row_edge(a - 1, b);
+    if (rb) return col_edge(a, b - 1);
+    // corners: (0, gy+1) from the top border row, the others from the
+    // border columns, as the reference extrapolates them
+    if (a == 0 && b == gy + 1)
+        return (3.f * col_edge(0, gy - 1) - 3.f * col_edge(0, gy - 2)) + col_edge(0, gy - 3);
+    const int qb = (b == 0) ? 0 : gy + 1;
+    const int p0 = (a == 0) ? 1 : gx, p1 = (a == 0) ? 2 : gx - 1, p2 = (a == 0) ? 3 : gx - 2;
+    return (3.f * row_edge(p0 - 1, qb) - 3.f * row_edge(p1 - 1, qb)) + row_edge(p2 - 1, qb);
+}
+
+__global__ void __launch_bounds__(256) k_interp_grid(InterpArgs a) {
+    for (int i = blockIdx.y; i < a.nx; i += gridDim.y) {
+        const int di = i - a.xoff;
+        const bool gi = (di % a.skip) == 0;
+        // xwant = di / skip in [0, gx - 1], izero = min((int)xwant, gx - 2)
+        const bool okx = di >= 0 && di <= (a.gx - 1) * a.skip;
+        int iz = 0;
+        float rx[4] = {0.f, 0.f, 0.f, 0.f};
+        if (okx) {
+            iz = min(di / a.skip, a.gx - 2);
 #pragma unroll
-            for (int p = 0; p < 4; ++p) {
-                const double rx = a.wx[(size_t)i * 4 + p];
-                const size_t h = (size_t)(iz + p) * a.ny + j;
-                sx = fma(rx, a.hx[h], sx);
-                sy = fma(rx, a.hy[h], sy);
-                bad |= a.hbad[h];
+            for (int p = 0; p < 4; ++p)
+                rx[p] = keys_f(fabsf((float)(di - (iz + p - 1) * a.skip) / (float)a.skip));
+        }
+        for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < a.ny; j += gridDim.x * blockDim.x) {
+            const int dj = j - a.yoff;
+            if (gi && (dj % a.skip) == 0) continue;  // grid points keep their computed value
+            const bool ok = okx && dj >= 0 && dj <= (a.gy - 1) * a.skip;
+            bool badx = true, bady = true;
+            float sx = 0.f, sy = 0.f;
+            if (ok) {
+                const int jz = min(dj / a.skip, a.gy - 2);
+                float ry[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    ry[q] = keys_f(fabsf((float)(dj - (jz + q - 1) * a.skip) / (float)a.skip));
+                badx = bady = false;
+                // cdata rows iz..iz+3, columns jz..jz+3 (cdata index = grid index + 1)
+                const bool inner = iz >= 1 && iz + 3 <= a.gx && jz >= 1 && jz + 3 <= a.gy;
+#pragma unroll
+                for (int p = 0; p < 4; ++p) {
+                    float hx = 0.f, hy = 0.f;
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        float cx, cy;
+                        if (inner) {
+                            const float2 v = __ldg(a.grid + (size_t)(iz + p - 1) * a.gy + (jz + q - 1));
+                            cx = v.x;
+                            cy = v.y;
+                        } else {
+                            cx = cdata_f(a.grid, a.gx, a.gy, iz + p, jz + q, 0);
+                            cy = cdata_f(a.grid, a.gx, a.gy, iz + p, jz + q, 1);
+                        }
+                        badx |= cx == kXmissF;
+                        bady |= cy == kXmissF;
+                        hx = fmaf(cx, ry[q], hx);
+                        hy = fmaf(cy, ry[q], hy);
+                    }
+                    sx = fmaf(rx[p], hx, sx);
+                    sy = fmaf(rx[p], hy, sy);
+                }
             }
-            vx = (bad & 1) ? kXmiss : sx;
-            vy = (bad & 2) ? kXmiss : sy;
+            const size_t k = (size_t)i * a.ny + j;
+            // xmiss reset: a missing vx clears the mask, a missing vy only vy
+            a.vx[k] = badx ? 0. : f2d(sx);
+            a.vy[k] = bady ? 0. : f2d(sy);
+            a.vm[k] = badx ? 0. : 0.5;
         }
-        double vm = 0.5;
-        // the final xmiss reset (flct.c:1125-1133)
-        if (vx == kXmiss) {
-            vm = 0.;
-            vx = 0.;
-        }
-        if (vy == kXmiss) vy = 0.;
-        a.vx[k] = vx;
-        a.vy[k] = vy;
-        a.vm[k] = vm;
     }
 }
 

@@ -4,8 +4,6 @@
 
 namespace flct {
 
-constexpr int kSeg = 32;  // outputs per thread in the sliding box sums
-
 struct ClassifyArgs {
     const double* f1;
     const double* f2;
@@ -18,23 +16,28 @@ struct ClassifyArgs {
     int* work;
     int* nwork;
     double *vx, *vy, *vm;
-    double *gvx, *gvy;
+    float2* grid;             // skip-grid (vx, vy) for the interpolation, or null
     unsigned* status;
 };
 
+// Local-mean box sums for the boxes the grid needs.  Grid point (q, m) is
+// pixel (xo + q gs, yo + m gs) (gs = 1, xo = yo = 0 without -s); its box
+// starts at (box_start(xo + q gs), box_start(yo + m gs)).
+struct BoxArgs {
+    const double* f1;
+    const double* f2;
+    int nx, ny, n, nsize;
+    int gs, xo, yo, gi, gj;   // grid step, offsets and counts (slow, fast axis)
+    int seg;                  // outputs per thread
+    double *rt1, *rt2;        // row sums [gj][nx]
+    double *b1, *b2;          // box sums [gi][gj]
+};
+
+// The velocity pipeline's skip-grid interpolation (FP32 arithmetic).
 struct InterpArgs {
     int nx, ny, skip, xoff, yoff;
     int gx, gy;               // grid counts along the slow / fast axis
-    const double* gvx;
-    const double* gvy;
-    const int* zx;
-    const double* wx;
-    const unsigned char* okx;
-    const int* zy;
-    const double* wy;
-    const unsigned char* oky;
-    double *hx, *hy;          // row contractions [(gx+2) x ny]
-    unsigned char* hbad;      // xmiss flags of those rows (bit 0: vx, bit 1: vy)
+    const float2* grid;       // (vx, vy) per grid point [gx][gy]
     double *vx, *vy, *vm;
 };
 
@@ -42,12 +45,11 @@ __global__ void k_absmax(const double* f1, const double* f2, long n, unsigned lo
 __global__ void k_thresh_final(const double* f1, const double* f2, const unsigned long long* mx,
                                double thresh, double* thr);
 __global__ void k_classify(ClassifyArgs a);
-__global__ void k_rowsum(const double* f1, const double* f2, int nx, int ny, int n, double* r1, double* r2);
-__global__ void k_colsum(const double* r1, const double* r2, int nx, int W, int n, double* b1, double* b2);
+__global__ void k_box_rows(BoxArgs a);
+__global__ void k_box_cols(BoxArgs a);
 __global__ void k_interp_axis(int n, int gcount, int off, int skip, const double* want, int* zero,
                               double* wts, unsigned char* ok);
-__global__ void k_interp_rows(InterpArgs a);
-__global__ void k_interp(InterpArgs a);
+__global__ void k_interp_grid(InterpArgs a);
 __global__ void k_interp_general(const double* f, int gx, int gy, double xmiss, const int* zx,
                                  const double* wx, const unsigned char* okx, int nxi, const int* zy,
                                  const double* wy, const unsigned char* oky, int nyi, double* out);

@@ -12,10 +12,9 @@ __global__ void k_means(MeansArgs a) {
     for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < nw; w += gridDim.x * blockDim.x) {
         const int pix = a.work[w];
         const int i = pix / a.ny, j = pix - (pix / a.ny) * a.ny;
-        const int imin = box_start(i, a.nx, a.nsize), jmin = box_start(j, a.ny, a.nsize);
-        const size_t b = (size_t)imin * a.bsw + jmin;
-        const float2 m1 = split_double(dm(a.bs1[b], a.inv_n2));
-        const float2 m2 = split_double(dm(a.bs2[b], a.inv_n2));
+        const size_t b = (size_t)((i - a.xo) / a.gs) * a.gj + (j - a.yo) / a.gs;
+        const float2 m1 = split_double_fast(dm(a.bs1[b], a.inv_n2));
+        const float2 m2 = split_double_fast(dm(a.bs2[b], a.inv_n2));
         a.means[w] = make_float4(m1.x, m1.y, m2.x, m2.y);
     }
 }
@@ -32,7 +31,7 @@ __global__ void k_fit(FitArgs a) {
         if (r.meta >> 16) {
             double v[9];
 #pragma unroll
-            for (int k = 0; k < 9; ++k) v[k] = (double)r.v[k];
+            for (int k = 0; k < 9; ++k) v[k] = f2d(r.v[k]);
             // v[3p+q] = |c| at (I-1+p, J-1+q)
             const double fx = dm(0.5, ds(v[7], v[1]));
             const double fy = dm(0.5, ds(v[5], v[3]));
@@ -56,10 +55,9 @@ __global__ void k_fit(FitArgs a) {
             double vxx = dm(dm(shy, a.deltinv), a.deltas);
             double vyy = dm(dm(shx, a.deltinv), a.deltas);
             double vmm = 1.;
-            if (a.gvx) {
+            if (a.grid) {
                 const int ic = (i - a.xoff) / a.skip, jc = (j - a.yoff) / a.skip;
-                a.gvx[(size_t)ic * a.jcnt + jc] = vxx;
-                a.gvy[(size_t)ic * a.jcnt + jc] = vyy;
+                a.grid[(size_t)ic * a.jcnt + jc] = make_float2((float)vxx, (float)vyy);
             }
             if (vxx == kXmiss) {
                 vmm = 0.;

@@ -31,7 +31,8 @@ __host__ __device__ __forceinline__ unsigned peak_meta(int I, int J, bool dofit)
 struct MeansArgs {
     const int* work;
     const int* nwork;
-    int nx, ny, nsize, bsw;
+    int ny;
+    int gs, xo, yo, gj;   // grid step and offsets; box sums are [grid row][grid column]
     const double* bs1;
     const double* bs2;
     double inv_n2;
@@ -47,7 +48,7 @@ struct FitArgs {
     double deltinv, deltas;
     int skip, xoff, yoff, jcnt;
     double *vx, *vy, *vm;  // outputs [nx*ny] or null (window-only calls)
-    double *gvx, *gvy;     // skip-grid copies or null
+    float2* grid;          // skip-grid (vx, vy) for the interpolation, or null
     double *shx, *shy;     // raw shifts per work item or null
 };
 
