@@ -72,7 +72,9 @@ def build(force: bool = False, jobs: int | None = None, verbose: bool = False) -
             for s in ex.map(run, todo):
                 if verbose:
                     print("compiled", os.path.basename(s))
-    if todo or force or not os.path.exists(LIB):
+    # relink when any object is newer than the library (also after a failed link)
+    stale_lib = not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs)
+    if todo or force or stale_lib:
         tmp = LIB + ".tmp"
         cmd = [cc] + ARCH + ["-shared", "-cudart", "static", "-o", tmp] + objs + ["-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)

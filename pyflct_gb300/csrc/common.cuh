@@ -38,13 +38,19 @@ __device__ __forceinline__ float2 split_double(double a) {
 //   the mantissa, lo = float(D) * 2^(e-52) (exact: a power-of-two scale of
 //   a normal float).  Exponents outside [-74, 126], zeros' signs and
 //   non-finite values take the FP64 path.
+// (The rare paths are out of line so the compiler cannot execute their
+// FP64 instructions speculatively on every call.)
+static __device__ __noinline__ float2 split_double_slow(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    if ((b << 1) == 0ull) return make_float2(__int_as_float((int)((b >> 32) & 0x80000000u)), 0.0f);
+    return split_double(x);
+}
+static __device__ __noinline__ double f2d_slow(float f) { return (double)f; }
+
 __device__ __forceinline__ float2 split_double_fast(double x) {
     const unsigned long long b = (unsigned long long)__double_as_longlong(x);
     const int e = (int)((b >> 52) & 0x7ffu) - 1023;
-    if (e < -74 || e > 126) {
-        if ((b << 1) == 0ull) return make_float2(__int_as_float((int)((b >> 32) & 0x80000000u)), 0.0f);
-        return split_double(x);
-    }
+    if (e < -74 || e > 126) return split_double_slow(x);
     const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
     const unsigned long long mi = (b & 0xfffffffffffffull) | (1ull << 52);
     unsigned top = (unsigned)(mi >> 29);             // 24 bits with the implicit one
@@ -64,7 +70,7 @@ __device__ __forceinline__ double f2d(float f) {
     const unsigned E = (u >> 23) & 0xffu;
     const unsigned long long s = (unsigned long long)(u >> 31) << 63;
     if (E == 0u && (u & 0x7fffffu) == 0u) return __longlong_as_double((long long)s);
-    if (E == 0u || E == 255u) return (double)f;
+    if (E == 0u || E == 255u) return f2d_slow(f);
     return __longlong_as_double(
         (long long)(s | ((unsigned long long)(E + 896u) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29)));
 }

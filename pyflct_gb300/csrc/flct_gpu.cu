@@ -563,14 +563,22 @@ flct_status enqueue_prepass(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaS
         ba.yo = j.yo;
         ba.gi = j.gi;
         ba.gj = j.gj;
-        ba.seg = std::max(8, n / j.gs);
+        // runs per line chosen for ~24K threads per pass: the FP64 pipe, not
+        // the thread count, bounds these passes, and longer runs add less
+        // per-run start-up
+        constexpr long kThreads = 16384;
+        const long T = (2l * nx + kBoxLines - 1) / kBoxLines, T2 = (2l * j.gj + kBoxLines - 1) / kBoxLines;
+        const int nseg = (int)std::min<long>(j.gj, std::max(1l, (kThreads + T - 1) / T));
+        const int nseg2 = (int)std::min<long>(j.gi, std::max(1l, (kThreads + T2 - 1) / T2));
+        ba.seg = (j.gj + nseg - 1) / nseg;
+        ba.seg2 = (j.gi + nseg2 - 1) / nseg2;
         ba.rt1 = b.r1;
         ba.rt2 = b.r2;
         ba.b1 = b.b1;
         ba.b2 = b.b2;
-        long t = (long)nx * ((j.gj + ba.seg - 1) / ba.seg);
+        long t = T * ((j.gj + ba.seg - 1) / ba.seg);
         k_box_rows<<<(int)((t + 127) / 128), 128, 0, st>>>(ba);
-        t = (long)j.gj * ((j.gi + ba.seg - 1) / ba.seg);
+        t = T2 * ((j.gi + ba.seg2 - 1) / ba.seg2);
         k_box_cols<<<(int)((t + 127) / 128), 128, 0, st>>>(ba);
         *launches += 2;
     }
@@ -652,9 +660,8 @@ flct_status enqueue_interp(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaSt
     ia.vx = j.vx;
     ia.vy = j.vy;
     ia.vm = j.vm;
-    const int bx = std::min(4, (j.ny + 255) / 256);
-    const int by = std::min(j.nx, std::max(1, ctx->nsm * 8 / bx));
-    k_interp_grid<<<dim3(bx, by), 256, 0, st>>>(ia);
+    const long tiles = (long)((j.nx + 7) / 8) * ((j.ny + 31) / 32);
+    k_interp_grid<<<(int)std::min<long>(tiles, (long)ctx->nsm * 8), 256, 0, st>>>(ia);
     ++*launches;
     CK(cudaGetLastError());
     return FLCT_OK;

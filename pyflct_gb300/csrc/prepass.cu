@@ -62,6 +62,12 @@ __global__ void k_thresh_final(const double* __restrict__ f1, const double* __re
 
 // ------------------------------------------------------- classify ----
 
+// Finite test on the bit pattern (integer ops only).
+__device__ __forceinline__ bool finite_bits(double x) {
+    return ((__double_as_longlong(x) >> 52) & 0x7ff) != 0x7ff;
+}
+
+
 // One tile = 256 consecutive pixels of one row, one per thread.  The work
 // list grows by one atomic per tile (block-wide ballot counts); the float
 // split of both frames uses integer operations, and the threshold test
@@ -88,7 +94,10 @@ __global__ void __launch_bounds__(256) k_classify(ClassifyArgs a) {
             const float2 sa = split_double_fast(fa), sb = split_double_fast(fb);
             a.s1[k] = sa;
             a.s2[k] = sb;
-            if ((isinf(sa.x) && !isinf(fa)) || (isinf(sb.x) && !isinf(fb))) atomicOr(a.status, kStatusRange);
+            // a finite value beyond the FP32 range (integer tests on the bits)
+            if (((__float_as_uint(sa.x) & 0x7fffffffu) == 0x7f800000u && finite_bits(fa)) ||
+                ((__float_as_uint(sb.x) & 0x7fffffffu) == 0x7f800000u && finite_bits(fb)))
+                atomicOr(a.status, kStatusRange);
             bool below = false;
             if (thr_pos) {
                 const unsigned long long sb2 =
@@ -141,84 +150,136 @@ __global__ void __launch_bounds__(256) k_classify(ClassifyArgs a) {
 
 // ------------------------------------------------------- box sums ----
 
-// Finite test on the bit pattern (integer ops only).
-__device__ __forceinline__ bool finite_bits(double x) {
-    return ((__double_as_longlong(x) >> 52) & 0x7ff) != 0x7ff;
-}
-
-// Running-sum step with the reference's direct-sum semantics for NaN and
-// infinities: whenever a non-finite value enters, leaves, or is in the sum,
-// the box is summed again directly, so a NaN taints only boxes holding it.
-template <class Get>
-__device__ __forceinline__ double slide(double sum, double in, double out, int n, Get get) {
-    if (finite_bits(sum) && finite_bits(in) && finite_bits(out)) return __dsub_rn(__dadd_rn(sum, in), out);
-    double t = 0.;
-    for (int q = 0; q < n; ++q) t = __dadd_rn(t, get(q));
-    return t;
+// One thread's runs of box sums along kBoxLines lines v[l][0..len) (frame
+// rows, or columns of row sums) that share their box starts: outputs
+// k = k0..k1-1 are out(l, k) = sum_{d<n} v[l][start(k) + d], start()
+// non-decreasing.  The first box is summed directly (n adds), every later
+// one by sliding column steps (an add and a subtract each), with the loads
+// of four steps issued before their adds.  A non-finite value anywhere in
+// the run switches the run to direct sums, so a NaN or an infinity taints
+// only the boxes holding it (the reference sums each box directly,
+// flct.c:815-827).  n is a multiple of 4; a null o[l] marks a padding line
+// (read from a valid line, stored nowhere).
+template <class Start>
+__device__ __forceinline__ void box_lines(const double* const (&v)[kBoxLines], double* const (&o)[kBoxLines],
+                                          long ks, int n, int k0, int k1, Start start) {
+    constexpr int L = kBoxLines;
+    double P[L];
+    bool fin = true;
+    const int s0 = start(k0);
+#pragma unroll
+    for (int l = 0; l < L; ++l) P[l] = 0.;
+    for (int d = 0; d < n; d += 4) {
+        double x[4][L];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int l = 0; l < L; ++l) x[u][l] = v[l][s0 + d + u];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int l = 0; l < L; ++l) {
+                fin &= finite_bits(x[u][l]);
+                P[l] = __dadd_rn(P[l], x[u][l]);
+            }
+    }
+    int k = k0;
+    int kn = s0;  // start(k) of the next output to store
+    while (k < k1 && kn == s0) {
+#pragma unroll
+        for (int l = 0; l < L; ++l)
+            if (o[l]) o[l][k * ks] = P[l];
+        if (++k < k1) kn = start(k);
+    }
+    const int cend = start(k1 - 1);
+    for (int c = s0; c < cend; c += 4) {
+        double xi[4][L], xo[4][L];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const bool ok = c + u < cend;
+#pragma unroll
+            for (int l = 0; l < L; ++l) {
+                xi[u][l] = ok ? v[l][c + u + n] : 0.;
+                xo[u][l] = ok ? v[l][c + u] : 0.;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            if (c + u < cend) {
+#pragma unroll
+                for (int l = 0; l < L; ++l) {
+                    fin &= finite_bits(xi[u][l]) & finite_bits(xo[u][l]);
+                    P[l] = __dsub_rn(__dadd_rn(P[l], xi[u][l]), xo[u][l]);
+                }
+                while (k < k1 && kn == c + u + 1) {
+#pragma unroll
+                    for (int l = 0; l < L; ++l)
+                        if (o[l]) o[l][k * ks] = P[l];
+                    if (++k < k1) kn = start(k);
+                }
+            }
+        }
+    }
+    if (!fin) {
+        for (int kk = k0; kk < k1; ++kk) {
+            const int s = start(kk);
+            for (int l = 0; l < L; ++l) {
+                if (!o[l]) continue;
+                double t = 0.;
+                for (int d = 0; d < n; ++d) t = __dadd_rn(t, v[l][s + d]);
+                o[l][kk * ks] = t;
+            }
+        }
+    }
 }
 
 // Row sums RT[m][i] = sum_{jj<n} f[i][s_m + jj] at the grid's box columns
-// s_m = box_start(yo + m gs).  One thread per (row, run of `seg` grid
-// columns): n adds for the first box, then one column step (an add and a
-// subtract) per column between consecutive boxes.  Consecutive threads take
-// consecutive rows, so the transposed stores are coalesced.
+// s_m = box_start(yo + m gs).  Lines are (frame, row) pairs; thread t of a
+// run takes lines t, t + T, t + 2T, t + 3T (T = lines / 4, rounded up), so
+// consecutive threads store consecutive rows (coalesced).
 __global__ void k_box_rows(BoxArgs a) {
-    const int nseg = (a.gj + a.seg - 1) / a.seg;
+    const int lines = 2 * a.nx;
+    const int T = (lines + kBoxLines - 1) / kBoxLines;
     const long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (idx >= (long)a.nx * nseg) return;
-    const int sg = (int)(idx / a.nx);
-    const int i = (int)(idx - (long)sg * a.nx);
+    const int nseg = (a.gj + a.seg - 1) / a.seg;
+    if (idx >= (long)T * nseg) return;
+    const int sg = (int)(idx / T), t = (int)(idx - (long)sg * T);
     const int m0 = sg * a.seg, m1 = min(m0 + a.seg, a.gj);
-    const double* f = a.f1 + (size_t)i * a.ny;
-    const double* g = a.f2 + (size_t)i * a.ny;
-    int s = box_start(a.yo + m0 * a.gs, a.ny, a.nsize);
-    double sa = 0., sb = 0.;
-    for (int jj = 0; jj < a.n; ++jj) {
-        sa = __dadd_rn(sa, f[s + jj]);
-        sb = __dadd_rn(sb, g[s + jj]);
+    const double* v[kBoxLines];
+    double* o[kBoxLines];
+#pragma unroll
+    for (int l = 0; l < kBoxLines; ++l) {
+        const int lam = t + l * T;
+        const bool ok = lam < lines;
+        const int img = (ok ? lam : 0) >= a.nx, i = (ok ? lam : 0) - img * a.nx;
+        v[l] = (img ? a.f2 : a.f1) + (size_t)i * a.ny;
+        o[l] = ok ? (img ? a.rt2 : a.rt1) + i : nullptr;
     }
-    a.rt1[(size_t)m0 * a.nx + i] = sa;
-    a.rt2[(size_t)m0 * a.nx + i] = sb;
-    for (int m = m0 + 1; m < m1; ++m) {
-        const int s1 = box_start(a.yo + m * a.gs, a.ny, a.nsize);
-        for (; s < s1; ++s) {
-            sa = slide(sa, f[s + a.n], f[s], a.n, [&](int q) { return f[s + 1 + q]; });
-            sb = slide(sb, g[s + a.n], g[s], a.n, [&](int q) { return g[s + 1 + q]; });
-        }
-        a.rt1[(size_t)m * a.nx + i] = sa;
-        a.rt2[(size_t)m * a.nx + i] = sb;
-    }
+    box_lines(v, o, a.nx, a.n, m0, m1, [&](int m) { return box_start(a.yo + m * a.gs, a.ny, a.nsize); });
 }
 
 // Box sums B[q][m] = sum_{ii<n} RT[m][t_q + ii] at the grid's box rows
-// t_q = box_start(xo + q gs); one thread per (grid column, run of `seg`
-// grid rows), consecutive threads on consecutive columns.
+// t_q = box_start(xo + q gs).  Lines are (frame, grid column) pairs, spread
+// over threads as in k_box_rows.
 __global__ void k_box_cols(BoxArgs a) {
-    const int nseg = (a.gi + a.seg - 1) / a.seg;
+    const int lines = 2 * a.gj;
+    const int T = (lines + kBoxLines - 1) / kBoxLines;
     const long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (idx >= (long)a.gj * nseg) return;
-    const int sg = (int)(idx / a.gj);
-    const int m = (int)(idx - (long)sg * a.gj);
-    const int q0 = sg * a.seg, q1 = min(q0 + a.seg, a.gi);
-    const double* r = a.rt1 + (size_t)m * a.nx;
-    const double* u = a.rt2 + (size_t)m * a.nx;
-    int t = box_start(a.xo + q0 * a.gs, a.nx, a.nsize);
-    double sa = 0., sb = 0.;
-    for (int ii = 0; ii < a.n; ++ii) {
-        sa = __dadd_rn(sa, r[t + ii]);
-        sb = __dadd_rn(sb, u[t + ii]);
+    const int nseg = (a.gi + a.seg2 - 1) / a.seg2;
+    if (idx >= (long)T * nseg) return;
+    const int sg = (int)(idx / T), t = (int)(idx - (long)sg * T);
+    const int q0 = sg * a.seg2, q1 = min(q0 + a.seg2, a.gi);
+    const double* v[kBoxLines];
+    double* o[kBoxLines];
+#pragma unroll
+    for (int l = 0; l < kBoxLines; ++l) {
+        const int lam = t + l * T;
+        const bool ok = lam < lines;
+        const int img = (ok ? lam : 0) >= a.gj, m = (ok ? lam : 0) - img * a.gj;
+        v[l] = (img ? a.rt2 : a.rt1) + (size_t)m * a.nx;
+        o[l] = ok ? (img ? a.b2 : a.b1) + m : nullptr;
     }
-    a.b1[(size_t)q0 * a.gj + m] = sa;
-    a.b2[(size_t)q0 * a.gj + m] = sb;
-    for (int q = q0 + 1; q < q1; ++q) {
-        const int t1 = box_start(a.xo + q * a.gs, a.nx, a.nsize);
-        for (; t < t1; ++t) {
-            sa = slide(sa, r[t + a.n], r[t], a.n, [&](int k) { return r[t + 1 + k]; });
-            sb = slide(sb, u[t + a.n], u[t], a.n, [&](int k) { return u[t + 1 + k]; });
-        }
-        a.b1[(size_t)q * a.gj + m] = sa;
-        a.b2[(size_t)q * a.gj + m] = sb;
-    }
+    box_lines(v, o, a.gj, a.n, q0, q1, [&](int q) { return box_start(a.xo + q * a.gs, a.nx, a.nsize); });
 }
 
 // --------------------------------------------------- interpolation ----
@@ -320,20 +381,23 @@ __device__ __forceinline__ float keys_f(float t) {
     return (t >= 1.0f) ? ((-0.5f * t + 2.5f) * t - 4.0f) * t + 2.0f : (1.5f * t - 2.5f) * t * t + 1.0f;
 }
 
-// cdata[a][b] of the border-extended grid (flct.c:2257-2336) for one of the
-// two components (c = 0: vx, 1: vy).
-__device__ __forceinline__ float cdata_f(const float2* __restrict__ g, int gx, int gy, int a, int b, int c) {
-    auto F = [&](int p, int q) -> float {
-        const float2 v = g[(size_t)p * gy + q];
-        return c ? v.y : v.x;
+// cdata[a][b] of the border-extended grid (flct.c:2257-2336), both
+// components.  Out of line: only stencils at the grid's border use it.
+__device__ __noinline__ float2 cdata_f(const float2* __restrict__ g, int gx, int gy, int a, int b) {
+    auto F = [&](int p, int q) -> float2 { return g[(size_t)p * gy + q]; };
+    auto ext = [](float2 f0, float2 f1, float2 f2) -> float2 {  // 3 f0 - 3 f1 + f2 in the reference's order
+        return make_float2((f2.x - 3.f * f1.x) + 3.f * f0.x, (f2.y - 3.f * f1.y) + 3.f * f0.y);
     };
-    auto row_edge = [&](int p, int q) -> float {  // interior row p, border column q
-        if (q == 0) return (F(p, 2) - 3.f * F(p, 1)) + 3.f * F(p, 0);
-        return (F(p, gy - 3) - 3.f * F(p, gy - 2)) + 3.f * F(p, gy - 1);
+    auto ext3 = [](float2 f0, float2 f1, float2 f2) -> float2 {  // corners: 3 c0 - 3 c1 + c2
+        return make_float2((3.f * f0.x - 3.f * f1.x) + f2.x, (3.f * f0.y - 3.f * f1.y) + f2.y);
     };
-    auto col_edge = [&](int p, int q) -> float {  // border row p, interior column q
-        if (p == 0) return (F(2, q) - 3.f * F(1, q)) + 3.f * F(0, q);
-        return (F(gx - 3, q) - 3.f * F(gx - 2, q)) + 3.f * F(gx - 1, q);
+    auto row_edge = [&](int p, int q) -> float2 {  // interior row p, border column q
+        if (q == 0) return ext(F(p, 0), F(p, 1), F(p, 2));
+        return ext(F(p, gy - 1), F(p, gy - 2), F(p, gy - 3));
+    };
+    auto col_edge = [&](int p, int q) -> float2 {  // border row p, interior column q
+        if (p == 0) return ext(F(0, q), F(1, q), F(2, q));
+        return ext(F(gx - 1, q), F(gx - 2, q), F(gx - 3, q));
     };
     const bool ra = (a >= 1 && a <= gx), rb = (b >= 1 && b <= gy);
     if (ra && rb) return F(a - 1, b - 1);
@@ -341,71 +405,111 @@ __device__ __forceinline__ float cdata_f(const float2* __restrict__ g, int gx, i
     if (rb) return col_edge(a, b - 1);
     // corners: (0, gy+1) from the top border row, the others from the
     // border columns, as the reference extrapolates them
-    if (a == 0 && b == gy + 1)
-        return (3.f * col_edge(0, gy - 1) - 3.f * col_edge(0, gy - 2)) + col_edge(0, gy - 3);
+    if (a == 0 && b == gy + 1) return ext3(col_edge(0, gy - 1), col_edge(0, gy - 2), col_edge(0, gy - 3));
     const int qb = (b == 0) ? 0 : gy + 1;
-    const int p0 = (a == 0) ? 1 : gx, p1 = (a == 0) ? 2 : gx - 1, p2 = (a == 0) ? 3 : gx - 2;
-    return (3.f * row_edge(p0 - 1, qb) - 3.f * row_edge(p1 - 1, qb)) + row_edge(p2 - 1, qb);
+    if (a == 0) return ext3(row_edge(0, qb), row_edge(1, qb), row_edge(2, qb));
+    return ext3(row_edge(gx - 1, qb), row_edge(gx - 2, qb), row_edge(gx - 3, qb));
 }
 
-__global__ void __launch_bounds__(256) k_interp_grid(InterpArgs a) {
-    for (int i = blockIdx.y; i < a.nx; i += gridDim.y) {
-        const int di = i - a.xoff;
-        const bool gi = (di % a.skip) == 0;
-        // xwant = di / skip in [0, gx - 1], izero = min((int)xwant, gx - 2)
-        const bool okx = di >= 0 && di <= (a.gx - 1) * a.skip;
-        int iz = 0;
-        float rx[4] = {0.f, 0.f, 0.f, 0.f};
-        if (okx) {
-            iz = min(di / a.skip, a.gx - 2);
-#pragma unroll
-            for (int p = 0; p < 4; ++p)
-                rx[p] = keys_f(fabsf((float)(di - (iz + p - 1) * a.skip) / (float)a.skip));
+// A block interpolates a tile of kTileR x kTileC pixels in three steps
+// separated by barriers: stage the cdata patch the tile's stencils touch
+// (interior grid values, and the border extrapolations where the tile
+// reaches the grid's edge) in shared memory; contract the patch along x for
+// every tile row, V[r][b] = sum_p rx_r[p] patch[izr + p][b] (with per-column
+// y stencils tabulated alongside); then each pixel contracts four V values
+// with its y weights.  xmiss flags travel with the values (bit 0: vx,
+// bit 1: vy).
+constexpr int kTileR = 8, kTileC = 32;
+constexpr int kPatchR = kTileR + 4, kPatchC = kTileC + 4;  // cdata rows / columns at skip 1
+
+__global__ void __launch_bounds__(kTileR * kTileC) k_interp_grid(InterpArgs a) {
+    __shared__ float2 s_p[kPatchR * kPatchC];
+    __shared__ unsigned char s_pb[kPatchR * kPatchC];
+    __shared__ float2 s_v[kTileR * kPatchC];
+    __shared__ unsigned char s_vb[kTileR * kPatchC];
+    __shared__ float s_ry[kTileC][4];
+    __shared__ int s_jz[kTileC];       // izero along y, -1 out of range
+    __shared__ unsigned char s_gj[kTileC];  // grid column
+    const int ntc = (a.ny + kTileC - 1) / kTileC;
+    const int ntr = (a.nx + kTileR - 1) / kTileR;
+    const float inv = 1.0f / (float)a.skip;
+    const int imax = (a.gx - 1) * a.skip, jmax = (a.gy - 1) * a.skip;
+    const int ti = threadIdx.x / kTileC, tj = threadIdx.x - (threadIdx.x / kTileC) * kTileC;
+    for (int tile = blockIdx.x; tile < ntr * ntc; tile += gridDim.x) {
+        const int i0 = (tile / ntc) * kTileR, j0 = (tile - (tile / ntc) * ntc) * kTileC;
+        // cdata rows / columns the tile's in-range pixels use
+        const int dlo = max(i0 - a.xoff, 0), dhi = min(min(i0 + kTileR, a.nx) - 1 - a.xoff, imax);
+        const int elo = max(j0 - a.yoff, 0), ehi = min(min(j0 + kTileC, a.ny) - 1 - a.yoff, jmax);
+        const bool any = dlo <= dhi && elo <= ehi;
+        const int r0 = any ? min(dlo / a.skip, a.gx - 2) : 0, r1 = any ? min(dhi / a.skip, a.gx - 2) + 3 : -1;
+        const int c0 = any ? min(elo / a.skip, a.gy - 2) : 0, c1 = any ? min(ehi / a.skip, a.gy - 2) + 3 : -1;
+        const int pw = c1 - c0 + 1, pn = (r1 - r0 + 1) * pw;
+        __syncthreads();  // the previous tile's tables are consumed
+        for (int e = threadIdx.x; e < pn; e += blockDim.x) {
+            const int ra = r0 + e / pw, cb = c0 + (e - (e / pw) * pw);
+            const float2 v = (ra >= 1 && ra <= a.gx && cb >= 1 && cb <= a.gy)
+                                 ? __ldg(a.grid + (size_t)(ra - 1) * a.gy + (cb - 1))
+                                 : cdata_f(a.grid, a.gx, a.gy, ra, cb);
+            s_p[e] = v;
+            s_pb[e] = (v.x == kXmissF ? 1 : 0) | (v.y == kXmissF ? 2 : 0);
         }
-        for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < a.ny; j += gridDim.x * blockDim.x) {
-            const int dj = j - a.yoff;
-            if (gi && (dj % a.skip) == 0) continue;  // grid points keep their computed value
-            const bool ok = okx && dj >= 0 && dj <= (a.gy - 1) * a.skip;
-            bool badx = true, bady = true;
-            float sx = 0.f, sy = 0.f;
-            if (ok) {
-                const int jz = min(dj / a.skip, a.gy - 2);
-                float ry[4];
+        if (threadIdx.x < kTileC) {
+            const int dj = j0 + threadIdx.x - a.yoff;
+            const bool okj = dj >= 0 && dj <= jmax;
+            const int jz = okj ? min(dj / a.skip, a.gy - 2) : -1;
+            s_jz[threadIdx.x] = jz;
+            s_gj[threadIdx.x] = (dj % a.skip) == 0;
 #pragma unroll
-                for (int q = 0; q < 4; ++q)
-                    ry[q] = keys_f(fabsf((float)(dj - (jz + q - 1) * a.skip) / (float)a.skip));
-                badx = bady = false;
-                // cdata rows iz..iz+3, columns jz..jz+3 (cdata index = grid index + 1)
-                const bool inner = iz >= 1 && iz + 3 <= a.gx && jz >= 1 && jz + 3 <= a.gy;
+            for (int q = 0; q < 4; ++q)
+                s_ry[threadIdx.x][q] = okj ? keys_f(fabsf((float)(dj - (jz + q - 1) * a.skip) * inv)) : 0.f;
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < kTileR * pw; e += blockDim.x) {
+            const int r = e / pw, b = e - (e / pw) * pw;
+            const int di = i0 + r - a.xoff;
+            float2 v = make_float2(0.f, 0.f);
+            unsigned char bad = 3;
+            if (i0 + r < a.nx && di >= 0 && di <= imax) {
+                const int iz = min(di / a.skip, a.gx - 2);
+                bad = 0;
 #pragma unroll
                 for (int p = 0; p < 4; ++p) {
-                    float hx = 0.f, hy = 0.f;
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        float cx, cy;
-                        if (inner) {
-                            const float2 v = __ldg(a.grid + (size_t)(iz + p - 1) * a.gy + (jz + q - 1));
-                            cx = v.x;
-                            cy = v.y;
-                        } else {
-                            cx = cdata_f(a.grid, a.gx, a.gy, iz + p, jz + q, 0);
-                            cy = cdata_f(a.grid, a.gx, a.gy, iz + p, jz + q, 1);
-                        }
-                        badx |= cx == kXmissF;
-                        bady |= cy == kXmissF;
-                        hx = fmaf(cx, ry[q], hx);
-                        hy = fmaf(cy, ry[q], hy);
-                    }
-                    sx = fmaf(rx[p], hx, sx);
-                    sy = fmaf(rx[p], hy, sy);
+                    const float rx = keys_f(fabsf((float)(di - (iz + p - 1) * a.skip) * inv));
+                    const int pe = (iz - r0 + p) * pw + b;
+                    const float2 c = s_p[pe];
+                    bad |= s_pb[pe];
+                    v.x = fmaf(rx, c.x, v.x);
+                    v.y = fmaf(rx, c.y, v.y);
                 }
             }
-            const size_t k = (size_t)i * a.ny + j;
-            // xmiss reset: a missing vx clears the mask, a missing vy only vy
-            a.vx[k] = badx ? 0. : f2d(sx);
-            a.vy[k] = bady ? 0. : f2d(sy);
-            a.vm[k] = badx ? 0. : 0.5;
+            s_v[r * kPatchC + b] = v;
+            s_vb[r * kPatchC + b] = bad;
         }
+        __syncthreads();
+        const int i = i0 + ti, j = j0 + tj;
+        if (i >= a.nx || j >= a.ny) continue;
+        const int di = i - a.xoff;
+        if (s_gj[tj] && (di % a.skip) == 0) continue;  // grid points keep their computed value
+        const int jz = s_jz[tj];
+        float sx = 0.f, sy = 0.f;
+        unsigned bad = 3;
+        if (jz >= 0 && di >= 0 && di <= imax) {  // (V is not built when no tile row is in range)
+            bad = 0;
+            const int vb = ti * kPatchC + (jz - c0);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const float ry = s_ry[tj][q];
+                const float2 v = s_v[vb + q];
+                bad |= s_vb[vb + q];
+                sx = fmaf(ry, v.x, sx);
+                sy = fmaf(ry, v.y, sy);
+            }
+        }
+        const size_t k = (size_t)i * a.ny + j;
+        // xmiss reset: a missing vx clears the mask, a missing vy only vy
+        a.vx[k] = (bad & 1) ? 0. : f2d(sx);
+        a.vy[k] = (bad & 2) ? 0. : f2d(sy);
+        a.vm[k] = (bad & 1) ? 0. : 0.5;
     }
 }
 

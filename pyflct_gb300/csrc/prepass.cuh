@@ -20,6 +20,8 @@ struct ClassifyArgs {
     unsigned* status;
 };
 
+constexpr int kBoxLines = 4;  // independent lines (FP64 add chains) per box-sum thread
+
 // Local-mean box sums for the boxes the grid needs.  Grid point (q, m) is
 // pixel (xo + q gs, yo + m gs) (gs = 1, xo = yo = 0 without -s); its box
 // starts at (box_start(xo + q gs), box_start(yo + m gs)).
@@ -28,7 +30,7 @@ struct BoxArgs {
     const double* f2;
     int nx, ny, n, nsize;
     int gs, xo, yo, gi, gj;   // grid step, offsets and counts (slow, fast axis)
-    int seg;                  // outputs per thread
+    int seg, seg2;            // outputs per thread of the row / column pass
     double *rt1, *rt2;        // row sums [gj][nx]
     double *b1, *b2;          // box sums [gi][gj]
 };
