@@ -84,12 +84,12 @@ struct flct_ctx {
         size_t n = 0;
     };
     Buf b_s1, b_s2, b_work, b_ctr, b_r1, b_r2, b_b1, b_b2, b_gvx, b_gvy, b_ix, b_iy;
-    Buf b_f1, b_f2, b_vx, b_vy, b_vm, b_aux1, b_aux2, b_means, b_peaks, b_grid;
+    Buf b_f1, b_f2, b_vx, b_vy, b_vm, b_aux1, b_aux2, b_means, b_peaks, b_grid, b_peaks_h;
     std::vector<Buf*> all() {
         return {&b_s1,   &b_s2,   &b_work,   &b_ctr,    &b_r1,     &b_r2,     &b_b1,     &b_b2,
                 &b_gvx,  &b_gvy,  &b_ix,     &b_iy,     &b_f1,     &b_f2,     &b_vx,     &b_vy,
                 &b_vm,   &b_aux1, &b_aux2,   &b_means,  &b_peaks,  &b_grid,   &b_tc,     &bb_arena,
-                &bb_work, &bb_means, &bb_peaks, &bb_ctr, &bb_meta};
+                &bb_work, &bb_means, &bb_peaks, &bb_ctr, &bb_meta, &b_peaks_h, &bb_peaks_h};
     }
     int bps[sizeof(kWin) / sizeof(kWin[0])] = {0};
     int bps_tc[2] = {0, 0};
@@ -109,7 +109,7 @@ struct flct_ctx {
     // at it), branch streams of the captured graph, the instantiated graph
     // of the last batch and the pairs it was built for
     static constexpr int kBranches = 8;
-    Buf bb_arena, bb_work, bb_means, bb_peaks, bb_ctr, bb_meta;
+    Buf bb_arena, bb_work, bb_means, bb_peaks, bb_peaks_h, bb_ctr, bb_meta;
     cudaStream_t bstream[kBranches] = {};
     cudaEvent_t bev[kBranches + 1] = {};
     cudaEvent_t bdone = nullptr;  // recorded after each batch launch
@@ -299,6 +299,7 @@ flct_status launch_windows(flct_ctx* ctx, int form, const WinEntry* we, int n, c
     ta.direct = wa.direct;
     ta.use_filter = wa.use_filter;
     ta.peaks = wa.peaks;
+    ta.peaks_h = wa.peaks_h;
     ta.segs = wa.segs;
     ta.seg_start = wa.seg_start;
     ta.nseg = wa.nseg;
@@ -442,7 +443,6 @@ flct_status plan_job(flct_ctx* ctx, const flct_params* p, const double* f1, cons
     if (s != FLCT_OK) return s;
     if (j->d.global)
         return fail(ctx, FLCT_ERR_UNSUPPORTED, "sigma <= 0 (global-shift mode) is not available on the GPU path yet");
-    if (p->hires) return fail(ctx, FLCT_ERR_UNSUPPORTED, "-h (hires) is not available on the GPU path yet");
     if (p->filter && !(p->kr > 0.))
         return fail(ctx, FLCT_ERR_UNSUPPORTED, "-k with kr <= 0 is not available on the GPU path");
     j->n = j->d.n;
@@ -478,6 +478,7 @@ struct JobBufs {
     int* work = nullptr;
     float4* means = nullptr;
     PeakRec* peaks = nullptr;
+    PeakRecH* peaks_h = nullptr;  // -h only
     double* r1 = nullptr;  // row sums [gj][nx]
     double* r2 = nullptr;
     double* b1 = nullptr;  // box sums [gi][gj]
@@ -490,7 +491,7 @@ struct JobBufs {
 
 // Bytes of each workspace region of a job.
 struct JobSizes {
-    size_t s = 0, work = 0, means = 0, peaks = 0, r = 0, b = 0, grid = 0;
+    size_t s = 0, work = 0, means = 0, peaks = 0, peaks_h = 0, r = 0, b = 0, grid = 0;
 };
 
 JobSizes job_sizes(const Job& j) {
@@ -500,6 +501,7 @@ JobSizes job_sizes(const Job& j) {
     z.work = npx * sizeof(int);
     z.means = npx * sizeof(float4);
     z.peaks = npx * sizeof(PeakRec);
+    if (j.p->hires) z.peaks_h = npx * sizeof(PeakRecH);
     z.r = (size_t)j.gj * j.nx * sizeof(double);
     z.b = (size_t)j.gi * j.gj * sizeof(double);
     if (j.interp) z.grid = (size_t)j.gi * j.gj * sizeof(float2);
@@ -617,6 +619,7 @@ void make_wargs(const Job& j, const JobBufs& b, WinArgs* wa) {
     wa->ny = j.ny;
     wa->nsize = j.d.nsize;
     wa->peaks = b.peaks;
+    wa->peaks_h = j.p->hires ? b.peaks_h : nullptr;
 }
 
 // 3x3 fit, velocity, mask and skip-grid copy per work item (flct.c:901-942).
@@ -638,8 +641,14 @@ flct_status enqueue_fit(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaStrea
     fa.vm = j.vm;
     fa.grid = j.interp ? b.grid : nullptr;
     const size_t npx = (size_t)j.nx * j.ny;
-    long blocks = std::min<long>((long)(npx + 127) / 128, (long)ctx->nsm * 8);
-    k_fit<<<(int)std::max(1l, blocks), 128, 0, st>>>(fa);
+    if (j.p->hires) {
+        fa.peaks_h = b.peaks_h;
+        long blocks = std::min<long>((long)(npx + 3) / 4, (long)ctx->nsm * 16);
+        k_fit_hires<<<(int)std::max(1l, blocks), 128, 0, st>>>(fa);
+    } else {
+        long blocks = std::min<long>((long)(npx + 127) / 128, (long)ctx->nsm * 8);
+        k_fit<<<(int)std::max(1l, blocks), 128, 0, st>>>(fa);
+    }
     ++*launches;
     CK(cudaGetLastError());
     return FLCT_OK;
@@ -708,6 +717,7 @@ struct BatchGroup {
     int n = 0;
     int req_form = 0;
     int use_filter = 0;
+    int hires = 0;
     float gauss[2 * kMaxBox + 1] = {};
     float filt2[kMaxBox] = {};
     std::vector<int> pairs;
@@ -778,10 +788,11 @@ flct_status plan_batch(flct_ctx* ctx, int npairs, const flct_pair* pairs, BatchP
         g.n = j.n;
         g.req_form = j.p->form;
         g.use_filter = j.p->filter ? 1 : 0;
+        g.hires = j.p->hires ? 1 : 0;
         fill_tables(j.p, j.n, g.gauss, g.filt2);
         bool found = false;
         for (auto& G : bp->groups)
-            if (G.n == g.n && G.req_form == g.req_form && G.use_filter == g.use_filter &&
+            if (G.n == g.n && G.req_form == g.req_form && G.use_filter == g.use_filter && G.hires == g.hires &&
                 !memcmp(G.gauss, g.gauss, sizeof(g.gauss)) && !memcmp(G.filt2, g.filt2, sizeof(g.filt2))) {
                 G.pairs.push_back(k);
                 found = true;
@@ -828,6 +839,9 @@ flct_status plan_batch(flct_ctx* ctx, int npairs, const flct_pair* pairs, BatchP
     ENSURE(ctx->bb_work, (size_t)items * sizeof(int));
     ENSURE(ctx->bb_means, (size_t)items * sizeof(float4));
     ENSURE(ctx->bb_peaks, (size_t)items * sizeof(PeakRec));
+    bool any_hires = false;
+    for (const auto& G : bp->groups) any_hires |= G.hires != 0;
+    if (any_hires) ENSURE(ctx->bb_peaks_h, (size_t)items * sizeof(PeakRecH));
     ENSURE(ctx->bb_ctr, (size_t)npairs * 64);
     ENSURE(ctx->bb_meta, seg_bytes + start_bytes + pair_bytes + first_bytes);
     unsigned char* A = (unsigned char*)ctx->bb_arena.p;
@@ -845,6 +859,7 @@ flct_status plan_batch(flct_ctx* ctx, int npairs, const flct_pair* pairs, BatchP
         b.work = (int*)ctx->bb_work.p + o.base;
         b.means = (float4*)ctx->bb_means.p + o.base;
         b.peaks = (PeakRec*)ctx->bb_peaks.p + o.base;
+        b.peaks_h = any_hires ? (PeakRecH*)ctx->bb_peaks_h.p + o.base : nullptr;
         b.ctr = (unsigned char*)ctx->bb_ctr.p + 64 * (size_t)k;
     }
     // segment tables, group-major
@@ -888,6 +903,7 @@ void group_wargs(flct_ctx* ctx, const BatchPlan& bp, int g, WinArgs* wa) {
     wa->means = (const float4*)ctx->bb_means.p;
     wa->work = (const int*)ctx->bb_work.p;
     wa->peaks = (PeakRec*)ctx->bb_peaks.p;
+    wa->peaks_h = G.hires ? (PeakRecH*)ctx->bb_peaks_h.p : nullptr;
     wa->nsize = G.n / 2;
     wa->nseg = bp.h_first[g + 1] - bp.h_first[g];
     wa->segs = bp.segs + bp.h_first[g];
@@ -1162,6 +1178,7 @@ flct_status flct_gpu_velocity_device(flct_ctx* ctx, const flct_params* p, const 
     ENSURE(ctx->b_b2, z.b);
     ENSURE(ctx->b_means, z.means);
     ENSURE(ctx->b_peaks, z.peaks);
+    if (z.peaks_h) ENSURE(ctx->b_peaks_h, z.peaks_h);
     if (j.interp) {
         ENSURE(ctx->b_grid, z.grid);
     }
@@ -1171,6 +1188,7 @@ flct_status flct_gpu_velocity_device(flct_ctx* ctx, const flct_params* p, const 
     b.work = (int*)ctx->b_work.p;
     b.means = (float4*)ctx->b_means.p;
     b.peaks = (PeakRec*)ctx->b_peaks.p;
+    b.peaks_h = (PeakRecH*)ctx->b_peaks_h.p;
     b.r1 = (double*)ctx->b_r1.p;
     b.r2 = (double*)ctx->b_r2.p;
     b.b1 = (double*)ctx->b_b1.p;

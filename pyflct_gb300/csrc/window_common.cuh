@@ -24,6 +24,16 @@ struct PeakRec {
     unsigned meta;  // I | J << 8 | dofit << 16
 };
 
+// The -h (hires) form of PeakRec: |c| on the 6x6 patch rows I-2..I+3,
+// columns J-2..J+3 around the integer peak (0 outside the box), which holds
+// every value the reference's 21x21 cubic-convolution zoom around the peak
+// reads, border extrapolations included (flct.c:1564-1600, 2257-2336).
+constexpr int kHiresPatch = 6;
+struct PeakRecH {
+    float v[kHiresPatch * kHiresPatch];
+    unsigned meta;  // I | J << 8 | have << 16
+};
+
 __host__ __device__ __forceinline__ unsigned peak_meta(int I, int J, bool dofit) {
     return (unsigned)I | ((unsigned)J << 8) | ((dofit ? 1u : 0u) << 16);
 }
@@ -50,6 +60,7 @@ struct FitArgs {
     double *vx, *vy, *vm;  // outputs [nx*ny] or null (window-only calls)
     float2* grid;          // skip-grid (vx, vy) for the interpolation, or null
     double *shx, *shy;     // raw shifts per work item or null
+    const PeakRecH* peaks_h;  // -h: patches instead of peaks (k_fit_hires)
 };
 
 // One image pair of a batched window launch.  The pair's work items,
@@ -77,6 +88,7 @@ __device__ __forceinline__ int seg_find(const int* __restrict__ start, int nseg,
 
 __global__ void k_means(MeansArgs a);
 __global__ void k_fit(FitArgs a);
+__global__ void k_fit_hires(FitArgs a);
 
 // Batched launches: for every group g, start[first[g] + g + k] (k = 0..nseg)
 // = prefix sums of the work counts (int at ctr + 64 * pair) of the group's

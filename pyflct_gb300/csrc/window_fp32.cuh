@@ -34,6 +34,7 @@ struct WinArgs {
     int use_filter;       // -k given
     int direct;           // windows given directly: box w starts at row w*n, unit weights
     PeakRec* peaks;       // per work item: integer peak and its 3x3 |c| stencil
+    PeakRecH* peaks_h;    // -h: the 6x6 patch records instead (null otherwise)
     const WinSeg* segs;   // batched launch: the pairs (s1, s2, nx, ny unused), else null
     const int* seg_start; // batched launch: [nseg + 1] item prefix sums; nwork = seg_start + nseg
     int nseg;
@@ -232,7 +233,18 @@ k_window_fp32(WinArgs a) {
                 J = have ? (int)(L % N) : N / 2;
             }
             const bool dofit = have && I > 0 && I < N - 1 && J > 0 && J < N - 1;
-            if (valid) {
+            if (valid && a.peaks_h) {
+                // -h: the 6x6 patch around the peak, 37 words
+                float* rec = reinterpret_cast<float*>(a.peaks_h + gi);
+                for (int k = ln; k < kHiresPatch * kHiresPatch + 1; k += N) {
+                    if (k < kHiresPatch * kHiresPatch) {
+                        const int r = I - 2 + k / kHiresPatch, c = J - 2 + k % kHiresPatch;
+                        rec[k] = (r >= 0 && r < N && c >= 0 && c < N) ? ab[r * N + c] : 0.f;
+                    } else {
+                        rec[k] = __uint_as_float(peak_meta(I, J, have));
+                    }
+                }
+            } else if (valid) {
                 // 10 words per record; teams narrower than 10 lanes loop
                 float* rec = reinterpret_cast<float*>(a.peaks + gi);
                 for (int k = ln; k < 10; k += N) {

@@ -51,6 +51,7 @@ struct TcArgs {
     int direct;
     int use_filter;
     PeakRec* peaks;
+    PeakRecH* peaks_h;    // -h patch records, else null
     const WinSeg* segs;   // batched launch (see WinArgs), else null
     const int* seg_start;
     int nseg;
@@ -527,7 +528,18 @@ __global__ void __launch_bounds__(128) k_window_tc32(TcArgs a) {
                     Jp = have ? (int)(L % 32) : H;
                 }
                 const bool dofit = have && Ip > 0 && Ip < N - 1 && Jp > 0 && Jp < N - 1;
-                if (valid && lane < 10) {
+                if (valid && a.peaks_h) {
+                    // -h: the 6x6 patch around the peak, 37 words
+                    float* rec = reinterpret_cast<float*>(a.peaks_h + s_gi[wg]);
+                    for (int k = lane; k < kHiresPatch * kHiresPatch + 1; k += 32) {
+                        if (k < kHiresPatch * kHiresPatch) {
+                            const int r = Ip - 2 + k / kHiresPatch, cc = Jp - 2 + k % kHiresPatch;
+                            rec[k] = (r >= 0 && r < N && cc >= 0 && cc < N) ? stage[r * 33 + cc] : 0.f;
+                        } else {
+                            rec[k] = __uint_as_float(peak_meta(Ip, Jp, have));
+                        }
+                    }
+                } else if (valid && lane < 10) {
                     float* rec = reinterpret_cast<float*>(a.peaks + s_gi[wg]);
                     if (lane < 9)
                         rec[lane] = dofit ? stage[(Ip - 1 + lane / 3) * 33 + (Jp - 1 + lane % 3)] : 0.f;

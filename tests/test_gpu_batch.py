@@ -37,6 +37,7 @@ SPECS = [
      dict(sigma=6, skip=5, interpolate=True, thresh=0.4, thresh_abs=True)),
     ((70, 96), dict(sigma=5), dict(sigma=5)),
     ((128, 100), dict(sigma=8, kr=0.5), dict(sigma=8, kr=0.5)),
+    ((80, 76), dict(sigma=5, hires=True), dict(sigma=5, hires=True)),
 ]
 
 

@@ -43,7 +43,7 @@ def test_golden_windows_n32(form):
 @pytest.mark.parametrize("form", ["tc_fp16", "tc_bf16"])
 @pytest.mark.parametrize("seed,shape,extra", [
     (1, (96, 100), {}), (2, (128, 80), {"kr": 0.5}), (3, (140, 150), {"skip": "3p1q2i"}),
-    (4, (100, 104), {"thresh": 0.3}),
+    (4, (100, 104), {"thresh": 0.3}), (5, (90, 96), {"hires": True}),
 ])
 def test_random_fields_sigma8(form, seed, shape, extra):
     from pyflct_gb300 import synth
@@ -54,7 +54,7 @@ def test_random_fields_sigma8(form, seed, shape, extra):
     got = run(f1, f2, form, sigma=8.0, **extra)
     args = [1, 1, 8]
     for k, v in extra.items():
-        args += {"kr": ["-k", v], "skip": ["-s", v], "thresh": ["-t", v]}[k]
+        args += {"kr": ["-k", v], "skip": ["-s", v], "thresh": ["-t", v], "hires": ["-h"]}[k]
     kw = parse_cli_args(args)
     rep = compare(f1, f2, got, po.velocity(f1, f2, **kw), kw, tol=TOL[form])
     print(form, shape, extra, rep)

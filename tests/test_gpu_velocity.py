@@ -68,8 +68,8 @@ def test_cli_case(case):
             gpu_flct(f1, f2, kw)
         assert e.value.code == ERR[name]
         return
-    if kw.get("hires") or kw["sigma"] <= 0:
-        pytest.skip("-h and sigma=0 are not on the GPU path yet")
+    if kw["sigma"] <= 0:
+        pytest.skip("sigma=0 is not on the GPU path yet")
     got = gpu_flct(f1, f2, kw)
     ref = po.velocity(f1, f2, **kw)
     rep = compare(f1, f2, got, ref, kw)
@@ -114,6 +114,8 @@ def test_config1_blobs_128():
     ((200, 210), 15, {"kr": 0.5}), ((50, 60), 7, {}), ((70, 66), 9, {"thresh": 0.3}),
     ((80, 84), 4, {"skip": 3, "poffset": 2, "qoffset": -1, "interpolate": True}),
     ((90, 90), 6, {"skip": 5, "interpolate": True, "thresh": 0.4, "thresh_abs": True}),
+    ((72, 80), 5, {"hires": True}), ((64, 70), 8, {"hires": True, "kr": 0.5}),
+    ((66, 64), 4, {"hires": True, "skip": 3, "interpolate": True}), ((40, 44), 2, {"hires": True}),
 ])
 def test_random_fields(shape, sigma, extra):
     from pyflct_gb300 import synth
