@@ -23,6 +23,11 @@ __host__ __device__ __forceinline__ int box_start(int i, int n, int nsize) {
     return (hi0 == n - 1) ? n - 1 - (2 * nsize - 1) : lo0;
 }
 
+// Finite test on a double's bit pattern (integer operations only).
+__device__ __forceinline__ bool finite_d(double x) {
+    return ((__double_as_longlong(x) >> 52) & 0x7ff) != 0x7ff;
+}
+
 // Split a double into float hi + float lo (hi = nearest float, lo = nearest
 // float to the remainder): a - (hi + lo) is below 2^-48 |a|.
 __device__ __forceinline__ float2 split_double(double a) {

@@ -19,6 +19,7 @@
 #include <string>
 #include <vector>
 
+#include "global.cuh"
 #include "prepass.cuh"
 #include "warp.cuh"
 #include "window_fp32.cuh"
@@ -441,13 +442,19 @@ flct_status plan_job(flct_ctx* ctx, const flct_params* p, const double* f1, cons
     if ((long long)nx * ny >= (1ll << 31)) return fail(ctx, FLCT_ERR_UNSUPPORTED, "image larger than 2^31 pixels");
     flct_status s = derive(ctx, p, nx, ny, &j->d);
     if (s != FLCT_OK) return s;
-    if (j->d.global)
-        return fail(ctx, FLCT_ERR_UNSUPPORTED, "sigma <= 0 (global-shift mode) is not available on the GPU path yet");
+    if (j->d.global && (nx > kMaxGlobalAxis || ny > kMaxGlobalAxis))
+        return fail(ctx, FLCT_ERR_UNSUPPORTED, "sigma <= 0 correlates whole frames of at most %d per side",
+                    kMaxGlobalAxis);
+    if (j->d.global && p->hires && (nx < 3 || ny < 3))
+        return fail(ctx, FLCT_ERR_UNSUPPORTED, "sigma <= 0 with -h needs frames of at least 3 x 3");
+    if (j->d.global && p->filter && (nx < 2 || ny < 2))
+        return fail(ctx, FLCT_ERR_UNSUPPORTED, "sigma <= 0 with -k needs frames of at least 2 x 2");
     if (p->filter && !(p->kr > 0.))
         return fail(ctx, FLCT_ERR_UNSUPPORTED, "-k with kr <= 0 is not available on the GPU path");
     j->n = j->d.n;
-    j->we = find_win(j->n);
-    if (!j->we) return fail(ctx, FLCT_ERR_UNSUPPORTED, "box size %d (sigma %g) has no GPU kernel", j->n, p->sigma);
+    j->we = j->d.global ? nullptr : find_win(j->n);
+    if (!j->d.global && !j->we)
+        return fail(ctx, FLCT_ERR_UNSUPPORTED, "box size %d (sigma %g) has no GPU kernel", j->n, p->sigma);
     j->p = p;
     j->f1 = f1;
     j->f2 = f2;
@@ -709,6 +716,143 @@ void resolved_config(flct_ctx* ctx, int requested, int n, int* form, int* grid_d
     *grid_div = it->second.grid_div;
 }
 
+// ------------------------------------------------------ sigma <= 0 --
+
+// make_freq (flct.c:1651-1690): 0..n/2-1, n/2 (and -n/2 for odd n), then
+// the negative frequencies.
+std::vector<double> make_freq(int n) {
+    std::vector<double> k(n);
+    const int n21 = n / 2 - 1;
+    int i = 0;
+    for (; i < n21 + 1; ++i) k[i] = (double)i;
+    int inext = n21 + 1;
+    if ((n / 2) * 2 != n) {
+        if (inext < n) k[inext] = (double)(n / 2);
+        ++inext;
+        if (inext < n) k[inext] = -(double)(n / 2);
+        ++inext;
+    } else {
+        if (inext < n) k[inext] = (double)(n / 2);
+        ++inext;
+    }
+    for (i = inext; i < n; ++i) k[i] = -(double)(n21 - (i - inext));
+    return k;
+}
+
+// The whole-frame correlation of the sigma <= 0 mode: FP64 means, FP32
+// batched DFTs, the same fits as the sliding windows (flct.c:802-942 with
+// init = 2).  Output: one (vx, vy, vm).
+flct_status velocity_global(flct_ctx* ctx, const Job& j, cudaStream_t st) {
+    const flct_params* p = j.p;
+    const int nx = j.nx, ny = j.ny;
+    const long n = (long)nx * ny;
+    ENSURE(ctx->b_s1, (size_t)n * sizeof(float2));
+    ENSURE(ctx->b_s2, (size_t)n * sizeof(float2));
+    ENSURE(ctx->b_ctr, 64);
+    ENSURE(ctx->b_aux2, (size_t)kGsumBlocks * 2 * sizeof(double));
+    ENSURE(ctx->b_b1, (size_t)(nx + ny) * (sizeof(float2) + sizeof(float)) + 64);
+    ENSURE(ctx->b_work, 64);
+    ENSURE(ctx->b_peaks, sizeof(PeakRec));
+    if (p->hires) ENSURE(ctx->b_peaks_h, sizeof(PeakRecH));
+    // twiddles e^{-2 pi i m / L} per axis and the squared -k filter factors
+    // exp(-2 (k / (kr k[L/2]))^2) (flct.c:1694-1715, applied to both spectra)
+    std::vector<unsigned char> tab((size_t)(nx + ny) * (sizeof(float2) + sizeof(float)));
+    float2* twx = (float2*)tab.data();
+    float2* twy = twx + nx;
+    float* fx2 = (float*)(twy + ny);
+    float* fy2 = fx2 + nx;
+    auto fill = [&](int L, float2* tw, float* f2) {
+        for (int m = 0; m < L; ++m) {
+            const double a = 2.0 * 3.14159265358979323846 * (double)m / (double)L;
+            tw[m] = make_float2((float)std::cos(a), (float)-std::sin(a));
+        }
+        const std::vector<double> k = make_freq(L);
+        const double roll = p->kr * k[L / 2];
+        for (int m = 0; m < L; ++m) {
+            const double ax = k[m] / roll;
+            f2[m] = p->filter ? (float)std::exp(-2.0 * ax * ax) : 1.0f;
+        }
+    };
+    fill(nx, twx, fx2);
+    fill(ny, twy, fy2);
+    unsigned char* dtab = (unsigned char*)ctx->b_b1.p;
+    CK(cudaMemcpyAsync(dtab, tab.data(), tab.size(), cudaMemcpyHostToDevice, st));
+    const float2* d_twx = (const float2*)dtab;
+    const float2* d_twy = d_twx + nx;
+    const float* d_fx2 = (const float*)(d_twy + ny);
+    const float* d_fy2 = d_fx2 + nx;
+    // counters: [0] nwork, [4] status, [8] peak key, [16] |g| maxima, [24] means
+    unsigned char* ctr = (unsigned char*)ctx->b_ctr.p;
+    int* d_nwork = (int*)ctr;
+    unsigned* d_status = (unsigned*)(ctr + 4);
+    unsigned long long* d_key = (unsigned long long*)(ctr + 8);
+    unsigned* d_max = (unsigned*)(ctr + 16);
+    double* d_means = (double*)(ctr + 24);
+    float2* A = (float2*)ctx->b_s1.p;
+    float2* B = (float2*)ctx->b_s2.p;
+    int launches = 0;
+    ctx->batch_pending = 0;
+    CK(cudaEventRecord(ctx->ev[0], st));
+    CK(cudaMemsetAsync(ctr, 0, 64, st));
+    k_gsum_part<<<kGsumBlocks, 256, 0, st>>>(j.f1, j.f2, n, (double*)ctx->b_aux2.p);
+    k_gsum_final<<<1, 256, 0, st>>>((const double*)ctx->b_aux2.p, kGsumBlocks, (double)nx * ny, d_means);
+    const int eblocks = (int)std::min<long>((n + 255) / 256, (long)ctx->nsm * 8);
+    k_gz<<<eblocks, 256, 0, st>>>(j.f1, j.f2, n, d_means, A, d_max, d_status);
+    launches += 3;
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ctx->ev[1], st));
+    auto dft = [&](bool inverse, const float2* in, float2* out, int L, int lines, const float2* tw,
+                   const unsigned* sc) {
+        launch_dft_rows(inverse, in, out, L, lines, tw, sc, st);
+        ++launches;
+    };
+    auto transpose = [&](const float2* in, float2* out, int R, int C) {
+        k_transpose<<<dim3((C + 31) / 32, (R + 31) / 32), dim3(32, 8), 0, st>>>(in, out, R, C);
+        ++launches;
+    };
+    dft(false, A, B, ny, nx, d_twy, d_max);  // along the fast axis, with the power-of-two scales
+    transpose(B, A, nx, ny);                 // [ky][i]
+    dft(false, A, B, nx, ny, d_twx, nullptr);  // Zt[ky][kx]
+    k_gprod<<<eblocks, 256, 0, st>>>(B, A, nx, ny, d_fx2, d_fy2);
+    ++launches;
+    dft(true, A, B, nx, ny, d_twx, nullptr);
+    transpose(B, A, ny, nx);
+    dft(true, A, B, ny, nx, d_twy, nullptr);  // c[i][j] (real part)
+    k_gpeak<<<eblocks, 256, 0, st>>>(B, nx, ny, d_key);
+    PeakRec* rec = (PeakRec*)ctx->b_peaks.p;
+    PeakRecH* rech = p->hires ? (PeakRecH*)ctx->b_peaks_h.p : nullptr;
+    k_gpatch<<<1, 64, 0, st>>>(B, nx, ny, d_key, rec, rech, (int*)ctx->b_work.p, d_nwork);
+    launches += 2;
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ctx->ev[2], st));
+    FitArgs fa{};
+    fa.work = (const int*)ctx->b_work.p;
+    fa.nwork = d_nwork;
+    fa.peaks = rec;
+    fa.peaks_h = rech;
+    fa.n = nx;
+    fa.n1 = ny;
+    fa.ny = 1;
+    fa.deltinv = 1. / p->deltat;
+    fa.deltas = p->deltas;
+    fa.skip = 1;
+    fa.vx = j.vx;
+    fa.vy = j.vy;
+    fa.vm = j.vm;
+    if (rech) k_fit_hires<<<1, 128, 0, st>>>(fa);
+    else k_fit<<<1, 32, 0, st>>>(fa);
+    ++launches;
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ctx->ev[7], st));
+    CK(cudaEventRecord(ctx->ev[3], st));
+    ctx->timing = flct_timing{};
+    ctx->timing.launches = launches;
+    ctx->timing.box = 0;
+    ctx->timing.form = FLCT_FORM_FP32;
+    ctx->pending = true;
+    return FLCT_OK;
+}
+
 // ------------------------------------------------------------- batches --
 
 // Pairs sharing a box size, requested form and window tables run through
@@ -777,6 +921,8 @@ flct_status plan_batch(flct_ctx* ctx, int npairs, const flct_pair* pairs, BatchP
         const flct_pair& q = pairs[k];
         flct_status s = plan_job(ctx, &q.params, q.f1, q.f2, q.nx, q.ny, q.vx, q.vy, q.vm, &bp->jobs[k]);
         if (s != FLCT_OK) return pair_fail(ctx, s, k);
+        if (bp->jobs[k].d.global)
+            return pair_fail(ctx, fail(ctx, FLCT_ERR_UNSUPPORTED, "sigma <= 0 frames are not batched"), k);
         int form = 0;
         s = pick_form(ctx, q.params.form, bp->jobs[k].n, &form);  // rejects forms without a kernel for n
         if (s != FLCT_OK) return pair_fail(ctx, s, k);
@@ -1162,6 +1308,7 @@ flct_status flct_gpu_velocity_device(flct_ctx* ctx, const flct_params* p, const 
     if (s != FLCT_OK) return s;
     CK(cudaSetDevice(ctx->device));
     cudaStream_t st = (cudaStream_t)stream;  // NULL: the CUDA default stream
+    if (j.d.global) return velocity_global(ctx, j, st);
     const int n = j.n;
     int form = FLCT_FORM_FP32;
     s = pick_form(ctx, p->form, n, &form);

@@ -64,18 +64,18 @@ __device__ __forceinline__ void fit3x3(const double* v, double* sx, double* sy) 
 
 __global__ void k_fit(FitArgs a) {
     const int nw = *a.nwork;
-    const int half = a.n / 2;
+    const int half = a.n / 2, half1 = (a.n1 ? a.n1 : a.n) / 2;
     for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < nw; w += gridDim.x * blockDim.x) {
         const PeakRec r = a.peaks[w];
-        const int I = (int)(r.meta & 0xffu), J = (int)((r.meta >> 8) & 0xffu);
+        const int I = meta_I(r.meta), J = meta_J(r.meta);
         double sx = 0., sy = 0.;
-        if (r.meta >> 16) {
+        if (meta_flag(r.meta)) {
             double v[9];
 #pragma unroll
             for (int k = 0; k < 9; ++k) v[k] = f2d(r.v[k]);
             fit3x3(v, &sx, &sy);
         }
-        store_shift(a, w, ds(da((double)I, sx), (double)half), ds(da((double)J, sy), (double)half));
+        store_shift(a, w, ds(da((double)I, sx), (double)half), ds(da((double)J, sy), (double)half1));
     }
 }
 
@@ -86,26 +86,26 @@ __device__ __forceinline__ float keys32(float t) {
     return (t >= 1.0f) ? ((-0.5f * t + 2.5f) * t - 4.0f) * t + 2.0f : (1.5f * t - 2.5f) * t * t + 1.0f;
 }
 
-// cdata of the 6x6 patch p (array rows I-2.., columns J-2..) at array
-// coordinates (r, c) in [-1, n]: interior values, or the one-cell border
+// cdata of the 6x6 patch p (array rows I-2.., columns J-2..) of an n x m
+// array at array coordinates (r, c) in [-1, n] x [-1, m]: interior values, or the one-cell border
 // extrapolations 3 f0 - 3 f1 + f2 (corners from the border columns, the
 // top-right one from the top border row), as interpcc2d builds them
 // (flct.c:2257-2336).
-__device__ __forceinline__ float patch_cdata(const float* p, int I, int J, int n, int r, int c) {
+__device__ __forceinline__ float patch_cdata(const float* p, int I, int J, int n, int m, int r, int c) {
     auto F = [&](int rr, int cc) { return p[(rr - I + 2) * kHiresPatch + (cc - J + 2)]; };
     auto ext = [](float f0, float f1, float f2) { return (f2 - 3.f * f1) + 3.f * f0; };
     auto ext3 = [](float c0, float c1, float c2) { return (3.f * c0 - 3.f * c1) + c2; };
     auto row_edge = [&](int rr, int cc) {  // interior row rr, border column cc
-        return cc < 0 ? ext(F(rr, 0), F(rr, 1), F(rr, 2)) : ext(F(rr, n - 1), F(rr, n - 2), F(rr, n - 3));
+        return cc < 0 ? ext(F(rr, 0), F(rr, 1), F(rr, 2)) : ext(F(rr, m - 1), F(rr, m - 2), F(rr, m - 3));
     };
     auto col_edge = [&](int rr, int cc) {  // border row rr, interior column cc
         return rr < 0 ? ext(F(0, cc), F(1, cc), F(2, cc)) : ext(F(n - 1, cc), F(n - 2, cc), F(n - 3, cc));
     };
-    const bool ri = r >= 0 && r < n, ci = c >= 0 && c < n;
+    const bool ri = r >= 0 && r < n, ci = c >= 0 && c < m;
     if (ri && ci) return F(r, c);
     if (ri) return row_edge(r, c);
     if (ci) return col_edge(r, c);
-    if (r < 0 && c >= n) return ext3(col_edge(-1, n - 1), col_edge(-1, n - 2), col_edge(-1, n - 3));
+    if (r < 0 && c >= m) return ext3(col_edge(-1, m - 1), col_edge(-1, m - 2), col_edge(-1, m - 3));
     if (r < 0) return ext3(row_edge(0, c), row_edge(1, c), row_edge(2, c));
     return ext3(row_edge(n - 1, c), row_edge(n - 2, c), row_edge(n - 3, c));
 }
@@ -132,13 +132,13 @@ __global__ void __launch_bounds__(128) k_fit_hires(FitArgs a) {
     __shared__ int s_iz[4][NI];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nw = *a.nwork;
-    const int n = a.n;
+    const int n = a.n, m = a.n1 ? a.n1 : a.n;
     for (int w = blockIdx.x * 4 + warp; w < nw; w += gridDim.x * 4) {
         const PeakRecH& r = a.peaks_h[w];
         s_p[warp][lane] = r.v[lane];
         if (lane < P * P - 32) s_p[warp][32 + lane] = r.v[32 + lane];
         const unsigned meta = r.meta;
-        const int I = (int)(meta & 0xffu), J = (int)((meta >> 8) & 0xffu);
+        const int I = meta_I(meta), J = meta_J(meta);
         // zoom coordinate of index t: (t * 2)/20 - 1 + peak (exact at t = 0, 10, 20)
         int jz = 0;
         bool okj = false;
@@ -151,8 +151,8 @@ __global__ void __launch_bounds__(128) k_fit_hires(FitArgs a) {
             s_iz[warp][lane] = okx ? iz : -1;
 #pragma unroll
             for (int q = 0; q < 4; ++q) s_rx[warp][lane][q] = keys32(fabsf(x - (float)(iz + q - 1)));
-            okj = !(y < 0.f || y > (float)(n - 1));
-            jz = min(max((int)y, 0), n - 2);
+            okj = !(y < 0.f || y > (float)(m - 1));
+            jz = min(max((int)y, 0), m - 2);
 #pragma unroll
             for (int q = 0; q < 4; ++q) ry[q] = keys32(fabsf(y - (float)(jz + q - 1)));
         }
@@ -167,7 +167,7 @@ __global__ void __launch_bounds__(128) k_fit_hires(FitArgs a) {
                 if (rr >= -1 && rr <= n) {
 #pragma unroll
                     for (int q = 0; q < 4; ++q) {
-                        const float c = patch_cdata(s_p[warp], I, J, n, rr, jz + q - 1);
+                        const float c = patch_cdata(s_p[warp], I, J, n, m, rr, jz + q - 1);
                         bad |= c == 0.f;
                         h = fmaf(c, ry[q], h);
                     }
@@ -210,8 +210,8 @@ __global__ void __launch_bounds__(128) k_fit_hires(FitArgs a) {
         __syncwarp();
         if (lane == 0) {
             // a NaN first element stays the maximum of a sequential scan
-            const int m = (s_pk[warp][0] != s_pk[warp][0]) ? 0 : (int)(0xffffffffu - (unsigned)(best & 0xffffffffull));
-            const int ixx = m / NI, iyy = m - (m / NI) * NI;
+            const int mi = (s_pk[warp][0] != s_pk[warp][0]) ? 0 : (int)(0xffffffffu - (unsigned)(best & 0xffffffffull));
+            const int ixx = mi / NI, iyy = mi - (mi / NI) * NI;
             double ssx = 0., ssy = 0.;
             if (ixx > 0 && ixx < NI - 1 && iyy > 0 && iyy < NI - 1) {
                 double v[9];
@@ -224,7 +224,7 @@ __global__ void __launch_bounds__(128) k_fit_hires(FitArgs a) {
             }
             const double xw = ds(dm((double)ixx, 2.) / 20., 1.) + (double)I;
             const double yw = ds(dm((double)iyy, 2.) / 20., 1.) + (double)J;
-            store_shift(a, w, ds(da(xw, ssx), (double)(n / 2)), ds(da(yw, ssy), (double)(n / 2)));
+            store_shift(a, w, ds(da(xw, ssx), (double)(n / 2)), ds(da(yw, ssy), (double)(m / 2)));
         }
         __syncwarp();
     }

@@ -21,7 +21,7 @@ constexpr int kMaxBox = 64;  // largest box side with a compiled window kernel
 // integer peak (half-shifted frame, row-major) and the peak itself.
 struct PeakRec {
     float v[9];
-    unsigned meta;  // I | J << 8 | dofit << 16
+    unsigned meta;  // peak_meta(I, J, dofit)
 };
 
 // The -h (hires) form of PeakRec: |c| on the 6x6 patch rows I-2..I+3,
@@ -31,12 +31,18 @@ struct PeakRec {
 constexpr int kHiresPatch = 6;
 struct PeakRecH {
     float v[kHiresPatch * kHiresPatch];
-    unsigned meta;  // I | J << 8 | have << 16
+    unsigned meta;  // peak_meta(I, J, have)
 };
 
-__host__ __device__ __forceinline__ unsigned peak_meta(int I, int J, bool dofit) {
-    return (unsigned)I | ((unsigned)J << 8) | ((dofit ? 1u : 0u) << 16);
+// I and J take 15 bits each (the sigma-0 mode correlates whole frames of up
+// to kMaxGlobalAxis per side), the flag bit 30.
+constexpr int kMaxGlobalAxis = 32767;
+__host__ __device__ __forceinline__ unsigned peak_meta(int I, int J, bool flag) {
+    return (unsigned)I | ((unsigned)J << 15) | ((flag ? 1u : 0u) << 30);
 }
+__host__ __device__ __forceinline__ int meta_I(unsigned m) { return (int)(m & 0x7fffu); }
+__host__ __device__ __forceinline__ int meta_J(unsigned m) { return (int)((m >> 15) & 0x7fffu); }
+__host__ __device__ __forceinline__ bool meta_flag(unsigned m) { return (m >> 30) & 1u; }
 
 struct MeansArgs {
     const int* work;
@@ -53,7 +59,8 @@ struct FitArgs {
     const int* work;
     const int* nwork;
     const PeakRec* peaks;
-    int n;                 // box side
+    int n;                 // box side (square boxes)
+    int n1;                // fast-axis side when the box is not square (sigma 0), else 0
     int ny;
     double deltinv, deltas;
     int skip, xoff, yoff, jcnt;

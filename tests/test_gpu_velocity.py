@@ -68,8 +68,6 @@ def test_cli_case(case):
             gpu_flct(f1, f2, kw)
         assert e.value.code == ERR[name]
         return
-    if kw["sigma"] <= 0:
-        pytest.skip("sigma=0 is not on the GPU path yet")
     got = gpu_flct(f1, f2, kw)
     ref = po.velocity(f1, f2, **kw)
     rep = compare(f1, f2, got, ref, kw)
@@ -194,3 +192,24 @@ def test_repeat_calls_are_identical():
     b = gpu_flct(f1, f2, kw)
     for x, y in zip(a, b):
         assert np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("shape,extra", [
+    ((50, 40), {}), ((128, 96), {"kr": 0.4}), ((201, 101), {}), ((97, 130), {"hires": True}),
+    ((256, 256), {"kr": 0.5, "hires": True}), ((33, 35), {"thresh": 0.5}),
+])
+def test_sigma0_global_shift(shape, extra):
+    """sigma = 0: one correlation of the whole frames (arbitrary sizes, odd
+    and prime sides included) against the oracle."""
+    from pyflct_gb300 import synth
+    rng = np.random.default_rng(sum(shape))
+    f1 = synth.kfield(shape, rng) + 3.0  # a mean to subtract
+    d = rng.uniform(-2.5, 2.5, 2)
+    f2 = synth.fourier_shift(f1, *d)
+    kw = dict(sigma=0, **extra)
+    got = gpu_flct(f1, f2, kw)
+    ref = po.velocity(f1, f2, **kw)
+    assert got[0].shape == (1, 1) and np.array_equal(got[2], ref[2])
+    dv = max(abs(got[0][0, 0] - ref[0][0, 0]), abs(got[1][0, 0] - ref[1][0, 0]))
+    assert dv <= TOL, (dv, got, ref)
+    print(shape, extra, "dv", dv, "v", got[0][0, 0], got[1][0, 0])
