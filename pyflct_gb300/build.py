@@ -81,7 +81,42 @@ def build(force: bool = False, jobs: int | None = None, verbose: bool = False) -
         if r.returncode != 0:
             raise RuntimeError("link failed:\n" + r.stderr)
         os.replace(tmp, LIB)
+    build_cli(verbose)
     return LIB
+
+
+CLI = os.path.join(PKG, "cli")
+BIN = os.path.join(PKG, "bin")
+
+
+def cc() -> str:
+    for cand in (os.environ.get("CC"), shutil.which("gcc"), shutil.which("cc")):
+        if cand and shutil.which(cand):
+            return cand
+    raise RuntimeError("a C compiler (gcc) is required to build the flct / warp programs")
+
+
+def build_cli(verbose: bool = False) -> list[str]:
+    """The `flct` and `warp` programs (C over the C ABI) in pyflct_gb300/bin,
+    linked against libflctgpu.so with an rpath to it."""
+    os.makedirs(BIN, exist_ok=True)
+    out = []
+    srcs = [os.path.join(CLI, "vcio.c")]
+    deps = srcs + [os.path.join(CLI, "vcio.h"), os.path.join(ROOT, "include", "flct_gpu.h"), LIB]
+    for prog in ("flct", "warp"):
+        main_c = os.path.join(CLI, f"{prog}_main.c")
+        exe = os.path.join(BIN, prog)
+        out.append(exe)
+        if os.path.exists(exe) and all(os.path.getmtime(exe) >= os.path.getmtime(d) for d in deps + [main_c]):
+            continue
+        cmd = [cc(), "-std=c11", "-O2", "-Wall", "-I", os.path.join(ROOT, "include"), main_c] + srcs + \
+              ["-L", PKG, "-lflctgpu", "-Wl,-rpath,$ORIGIN/..", "-o", exe]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"building {prog} failed:\n{r.stderr}")
+        if verbose and r.stderr.strip():
+            print(r.stderr)
+    return out
 
 
 def main(argv=None):
