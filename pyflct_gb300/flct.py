@@ -227,6 +227,7 @@ class FlctBatch:
         for k, (a, b) in enumerate(frames):
             self.f1[k].copy_(torch.as_tensor(_f64(a)), non_blocking=False)
             self.f2[k].copy_(torch.as_tensor(_f64(b)), non_blocking=False)
+        return self
 
     def run(self, stream=None):
         import torch
