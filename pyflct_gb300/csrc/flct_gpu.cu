@@ -119,6 +119,7 @@ struct flct_ctx {
     int batch_pending = 0;        // pairs of the batch whose timing awaits collection
     int batch_launches = 0;
     int batch_box = 0, batch_form = 0;
+    unsigned char* hctr = nullptr;  // page-locked copy of a call's work count and status
 };
 
 namespace {
@@ -515,30 +516,18 @@ JobSizes job_sizes(const Job& j) {
     return z;
 }
 
-// Threshold, classification / work list, FP64 box sums and local means
-// (flct.c:684-827).  Zeroes the job's counters first.
-flct_status enqueue_prepass(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaStream_t st, int* launches) {
-    const flct_params* p = j.p;
-    const int nx = j.nx, ny = j.ny, n = j.n;
-    const size_t npx = (size_t)nx * ny;
-    const int W = ny - n + 1, H = nx - n + 1;
-    int* d_nwork = (int*)b.ctr;
-    unsigned* d_status = (unsigned*)(b.ctr + 4);
-    unsigned long long* d_absmax = (unsigned long long*)(b.ctr + 8);
-    double* d_thr = (double*)(b.ctr + 24);
-    CK(cudaMemsetAsync(b.ctr, 0, 32, st));
-    if (j.d.rel_thresh) {
-        k_absmax<<<ctx->nsm * 4, 256, 0, st>>>(j.f1, j.f2, (long)npx, d_absmax);
-        k_thresh_final<<<1, 1, 0, st>>>(j.f1, j.f2, d_absmax, p->thresh, d_thr);
-        *launches += 2;
-    }
+// Classification of frame rows [r0, r1): threshold test, skip grid, the
+// float split, the work list (b.work / b.ctr: the windows of those rows)
+// and the final values of pixels without a window (flct.c:684-755).
+flct_status enqueue_classify(flct_ctx* ctx, const Job& j, const JobBufs& b, int r0, int r1, const double* d_thr,
+                             cudaStream_t st, int* launches) {
     ClassifyArgs ca{};
     ca.f1 = j.f1;
     ca.f2 = j.f2;
-    ca.nx = nx;
-    ca.ny = ny;
-    ca.thr_val = p->thresh;
-    ca.thr_ptr = j.d.rel_thresh ? d_thr : nullptr;
+    ca.nx = j.nx;
+    ca.ny = j.ny;
+    ca.thr_val = j.p->thresh;
+    ca.thr_ptr = d_thr;
     ca.skip = j.d.skip;
     ca.xoff = j.d.xoff;
     ca.yoff = j.d.yoff;
@@ -547,70 +536,120 @@ flct_status enqueue_prepass(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaS
     ca.s1 = b.s1;
     ca.s2 = b.s2;
     ca.work = b.work;
-    ca.nwork = d_nwork;
+    ca.nwork = (int*)b.ctr;
     ca.vx = j.vx;
     ca.vy = j.vy;
     ca.vm = j.vm;
     ca.grid = j.interp ? b.grid : nullptr;
-    ca.status = d_status;
-    {
-        const long tiles = (long)nx * ((ny + 255) / 256);
-        k_classify<<<(int)std::min<long>(tiles, (long)ctx->nsm * 8), 256, 0, st>>>(ca);
-        ++*launches;
-    }
-    {
-        // FP64 box sums at the boxes of the window grid
-        BoxArgs ba{};
-        ba.f1 = j.f1;
-        ba.f2 = j.f2;
-        ba.nx = nx;
-        ba.ny = ny;
-        ba.n = n;
-        ba.nsize = j.d.nsize;
-        ba.gs = j.gs;
-        ba.xo = j.xo;
-        ba.yo = j.yo;
-        ba.gi = j.gi;
-        ba.gj = j.gj;
-        // runs per line chosen for ~24K threads per pass: the FP64 pipe, not
-        // the thread count, bounds these passes, and longer runs add less
-        // per-run start-up
-        constexpr long kThreads = 16384;
-        const long T = (2l * nx + kBoxLines - 1) / kBoxLines, T2 = (2l * j.gj + kBoxLines - 1) / kBoxLines;
-        const int nseg = (int)std::min<long>(j.gj, std::max(1l, (kThreads + T - 1) / T));
-        const int nseg2 = (int)std::min<long>(j.gi, std::max(1l, (kThreads + T2 - 1) / T2));
-        ba.seg = (j.gj + nseg - 1) / nseg;
-        ba.seg2 = (j.gi + nseg2 - 1) / nseg2;
-        ba.rt1 = b.r1;
-        ba.rt2 = b.r2;
-        ba.b1 = b.b1;
-        ba.b2 = b.b2;
-        long t = T * ((j.gj + ba.seg - 1) / ba.seg);
-        k_box_rows<<<(int)((t + 127) / 128), 128, 0, st>>>(ba);
-        t = T2 * ((j.gi + ba.seg2 - 1) / ba.seg2);
-        k_box_cols<<<(int)((t + 127) / 128), 128, 0, st>>>(ba);
-        *launches += 2;
-    }
-    {
-        // FP64 local means per work item, one window per lane
-        MeansArgs ma{};
-        ma.work = b.work;
-        ma.nwork = d_nwork;
-        ma.ny = ny;
-        ma.gs = j.gs;
-        ma.xo = j.xo;
-        ma.yo = j.yo;
-        ma.gj = j.gj;
-        ma.bs1 = b.b1;
-        ma.bs2 = b.b2;
-        ma.inv_n2 = 1. / ((double)n * n);
-        ma.means = b.means;
-        long blocks = std::min<long>((long)(npx + 255) / 256, (long)ctx->nsm * 8);
-        k_means<<<(int)std::max(1l, blocks), 256, 0, st>>>(ma);
-        ++*launches;
-    }
+    ca.status = (unsigned*)(b.ctr + 4);
+    ca.r0 = r0;
+    ca.r1 = r1;
+    const long tiles = (long)(r1 - r0) * ((j.ny + 255) / 256);
+    k_classify<<<(int)std::max(1l, std::min<long>(tiles, (long)ctx->nsm * 8)), 256, 0, st>>>(ca);
+    ++*launches;
     CK(cudaGetLastError());
     return FLCT_OK;
+}
+
+BoxArgs box_args(const Job& j, const JobBufs& b) {
+    BoxArgs ba{};
+    ba.f1 = j.f1;
+    ba.f2 = j.f2;
+    ba.nx = j.nx;
+    ba.ny = j.ny;
+    ba.n = j.n;
+    ba.nsize = j.d.nsize;
+    ba.gs = j.gs;
+    ba.xo = j.xo;
+    ba.yo = j.yo;
+    ba.gi = j.gi;
+    ba.gj = j.gj;
+    ba.rt1 = b.r1;
+    ba.rt2 = b.r2;
+    ba.b1 = b.b1;
+    ba.b2 = b.b2;
+    return ba;
+}
+
+// Runs per line chosen for ~16K threads per pass: the FP64 pipe, not the
+// thread count, bounds these passes, and longer runs add less start-up.
+constexpr long kBoxThreads = 16384;
+
+// FP64 row sums of frame rows [r0, r1) at the grid's box columns.
+flct_status enqueue_box_rows(flct_ctx* ctx, const Job& j, const JobBufs& b, int r0, int r1, cudaStream_t st,
+                             int* launches) {
+    if (r1 <= r0) return FLCT_OK;
+    BoxArgs ba = box_args(j, b);
+    ba.r0 = r0;
+    ba.r1 = r1;
+    // run length from the whole frame's line count
+    const long Tf = (2l * j.nx + kBoxLines - 1) / kBoxLines, T = (2l * (r1 - r0) + kBoxLines - 1) / kBoxLines;
+    const int nseg = (int)std::min<long>(j.gj, std::max(1l, (kBoxThreads + Tf - 1) / Tf));
+    ba.seg = (j.gj + nseg - 1) / nseg;
+    const long t = T * ((j.gj + ba.seg - 1) / ba.seg);
+    k_box_rows<<<(int)((t + 127) / 128), 128, 0, st>>>(ba);
+    ++*launches;
+    CK(cudaGetLastError());
+    return FLCT_OK;
+}
+
+// FP64 box sums of grid rows [q0, q1) (their row sums must be complete).
+flct_status enqueue_box_cols(flct_ctx* ctx, const Job& j, const JobBufs& b, int q0, int q1, cudaStream_t st,
+                             int* launches) {
+    if (q1 <= q0) return FLCT_OK;
+    BoxArgs ba = box_args(j, b);
+    ba.q0 = q0;
+    ba.q1 = q1;
+    const long T2 = (2l * j.gj + kBoxLines - 1) / kBoxLines;
+    const int nseg2 = (int)std::min<long>(j.gi, std::max(1l, (kBoxThreads + T2 - 1) / T2));
+    ba.seg2 = (j.gi + nseg2 - 1) / nseg2;  // run length from the whole frame
+    const long t = T2 * ((q1 - q0 + ba.seg2 - 1) / ba.seg2);
+    k_box_cols<<<(int)((t + 127) / 128), 128, 0, st>>>(ba);
+    ++*launches;
+    CK(cudaGetLastError());
+    return FLCT_OK;
+}
+
+// FP64 local means of the work list b.work / b.ctr (flct.c:815-827), one
+// window per lane.
+flct_status enqueue_means(flct_ctx* ctx, const Job& j, const JobBufs& b, long max_items, cudaStream_t st,
+                          int* launches) {
+    MeansArgs ma{};
+    ma.work = b.work;
+    ma.nwork = (const int*)b.ctr;
+    ma.ny = j.ny;
+    ma.gs = j.gs;
+    ma.xo = j.xo;
+    ma.yo = j.yo;
+    ma.gj = j.gj;
+    ma.bs1 = b.b1;
+    ma.bs2 = b.b2;
+    ma.inv_n2 = 1. / ((double)j.n * j.n);
+    ma.means = b.means;
+    long blocks = std::min<long>((max_items + 255) / 256, (long)ctx->nsm * 8);
+    k_means<<<(int)std::max(1l, blocks), 256, 0, st>>>(ma);
+    ++*launches;
+    CK(cudaGetLastError());
+    return FLCT_OK;
+}
+
+// The whole-frame prepass: counters, relative threshold (flct.c:594-629),
+// classification, box sums and means.
+flct_status enqueue_prepass(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaStream_t st, int* launches) {
+    const size_t npx = (size_t)j.nx * j.ny;
+    unsigned long long* d_absmax = (unsigned long long*)(b.ctr + 8);
+    double* d_thr = (double*)(b.ctr + 24);
+    CK(cudaMemsetAsync(b.ctr, 0, 32, st));
+    if (j.d.rel_thresh) {
+        k_absmax<<<ctx->nsm * 4, 256, 0, st>>>(j.f1, j.f2, (long)npx, d_absmax);
+        k_thresh_final<<<1, 1, 0, st>>>(j.f1, j.f2, d_absmax, j.p->thresh, d_thr);
+        *launches += 2;
+    }
+    flct_status s = enqueue_classify(ctx, j, b, 0, j.nx, j.d.rel_thresh ? d_thr : nullptr, st, launches);
+    if (s == FLCT_OK) s = enqueue_box_rows(ctx, j, b, 0, j.nx, st, launches);
+    if (s == FLCT_OK) s = enqueue_box_cols(ctx, j, b, 0, j.gi, st, launches);
+    if (s == FLCT_OK) s = enqueue_means(ctx, j, b, (long)npx, st, launches);
+    return s;
 }
 
 void make_wargs(const Job& j, const JobBufs& b, WinArgs* wa) {
@@ -663,7 +702,10 @@ flct_status enqueue_fit(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaStrea
 
 // Cubic-convolution interpolation of the skip grid onto the skipped pixels,
 // mask and xmiss reset (flct.c:958-1133).
-flct_status enqueue_interp(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaStream_t st, int* launches) {
+flct_status enqueue_interp(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaStream_t st, int* launches,
+                           int i0 = 0, int i1 = -1) {
+    if (i1 < 0) i1 = j.nx;
+    if (i1 <= i0) return FLCT_OK;
     InterpArgs ia{};
     ia.nx = j.nx;
     ia.ny = j.ny;
@@ -676,7 +718,9 @@ flct_status enqueue_interp(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaSt
     ia.vx = j.vx;
     ia.vy = j.vy;
     ia.vm = j.vm;
-    const long tiles = (long)((j.nx + 7) / 8) * ((j.ny + 31) / 32);
+    ia.i0 = i0;
+    ia.i1 = i1;
+    const long tiles = (long)((i1 - i0 + 7) / 8) * ((j.ny + 31) / 32);
     k_interp_grid<<<(int)std::min<long>(tiles, (long)ctx->nsm * 8), 256, 0, st>>>(ia);
     ++*launches;
     CK(cudaGetLastError());
@@ -844,6 +888,7 @@ flct_status velocity_global(flct_ctx* ctx, const Job& j, cudaStream_t st) {
     ++launches;
     CK(cudaGetLastError());
     CK(cudaEventRecord(ctx->ev[7], st));
+    CK(cudaMemcpyAsync(ctx->hctr, ctr, 8, cudaMemcpyDeviceToHost, st));
     CK(cudaEventRecord(ctx->ev[3], st));
     ctx->timing = flct_timing{};
     ctx->timing.launches = launches;
@@ -1251,6 +1296,11 @@ flct_status flct_gpu_create(int device, flct_ctx** out) {
             flct_gpu_destroy(ctx);
             return FLCT_ERR_CUDA;
         }
+    if (cudaHostAlloc((void**)&ctx->hctr, 64, cudaHostAllocDefault) != cudaSuccess) {
+        ctx->hctr = nullptr;
+        flct_gpu_destroy(ctx);
+        return FLCT_ERR_ALLOC;
+    }
     ctx->device_name = prop.name;
     if (const char* path = getenv("FLCT_AUTOTUNE_CACHE")) ctx->tune_path = path;
     tune_load(ctx);
@@ -1274,6 +1324,7 @@ void flct_gpu_destroy(flct_ctx* ctx) {
         if (e) cudaEventDestroy(e);
     for (auto& e : ctx->bev)
         if (e) cudaEventDestroy(e);
+    if (ctx->hctr) cudaFreeHost(ctx->hctr);
     if (ctx->bdone) cudaEventDestroy(ctx->bdone);
     for (auto& st : ctx->bstream)
         if (st) cudaStreamDestroy(st);
@@ -1376,6 +1427,8 @@ flct_status flct_gpu_velocity_device(flct_ctx* ctx, const flct_params* p, const 
         s = enqueue_interp(ctx, j, b, st, &launches);
         if (s != FLCT_OK) return s;
     }
+    // work count and status to page-locked memory, complete with ev[3]
+    CK(cudaMemcpyAsync(ctx->hctr, b.ctr, 8, cudaMemcpyDeviceToHost, st));
     CK(cudaEventRecord(ctx->ev[3], st));
     ctx->timing = flct_timing{};
     ctx->timing.launches = launches;
@@ -1407,10 +1460,9 @@ static flct_status collect_timing(flct_ctx* ctx) {
             status |= st;
         }
     } else {
-        unsigned char* ctr = (unsigned char*)ctx->b_ctr.p;
         int w = 0;
-        CK(cudaMemcpy(&w, ctr, sizeof(int), cudaMemcpyDeviceToHost));
-        CK(cudaMemcpy(&status, ctr + 4, sizeof(unsigned), cudaMemcpyDeviceToHost));
+        memcpy(&w, ctx->hctr, sizeof(int));
+        memcpy(&status, ctx->hctr + 4, sizeof(unsigned));
         nwork = w;
     }
     ctx->timing.windows = nwork;
@@ -1514,6 +1566,8 @@ flct_status flct_gpu_cross_cor_batch(flct_ctx* ctx, const double* g1, const doub
     ca.nwork = (int*)(ctr + 32);
     ca.vx = ca.vy = ca.vm = nullptr;
     ca.status = (unsigned*)(ctr + 4);
+    ca.r0 = 0;
+    ca.r1 = nwin * n;
     CK(cudaEventRecord(ctx->ev[0], st));
     k_classify<<<ctx->nsm * 8, 256, 0, st>>>(ca);
     CK(cudaMemcpyAsync(ctr, &nwin, sizeof(int), cudaMemcpyHostToDevice, st));

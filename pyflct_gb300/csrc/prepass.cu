@@ -82,10 +82,10 @@ __global__ void __launch_bounds__(256) k_classify(ClassifyArgs a) {
     const bool thr_pos = (long long)tb > 0ll && tb <= 0x7ff0000000000000ull;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int tpr = (a.ny + 255) >> 8;  // tiles per row
-    const long ntile = (long)a.nx * tpr;
+    const long ntile = (long)(a.r1 - a.r0) * tpr;
     for (long t = blockIdx.x; t < ntile; t += gridDim.x) {
-        const int i = (int)(t / tpr);
-        const int j = (int)(t - (long)i * tpr) * 256 + threadIdx.x;
+        const int i = a.r0 + (int)(t / tpr);
+        const int j = (int)(t - (long)(i - a.r0) * tpr) * 256 + threadIdx.x;
         const bool act = j < a.ny;
         const size_t k = (size_t)i * a.ny + j;
         bool comp = false, grid = false;
@@ -238,7 +238,8 @@ __device__ __forceinline__ void box_lines(const double* const (&v)[kBoxLines], d
 // run takes lines t, t + T, t + 2T, t + 3T (T = lines / 4, rounded up), so
 // consecutive threads store consecutive rows (coalesced).
 __global__ void k_box_rows(BoxArgs a) {
-    const int lines = 2 * a.nx;
+    const int rows = a.r1 - a.r0;
+    const int lines = 2 * rows;
     const int T = (lines + kBoxLines - 1) / kBoxLines;
     const long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
     const int nseg = (a.gj + a.seg - 1) / a.seg;
@@ -251,7 +252,7 @@ __global__ void k_box_rows(BoxArgs a) {
     for (int l = 0; l < kBoxLines; ++l) {
         const int lam = t + l * T;
         const bool ok = lam < lines;
-        const int img = (ok ? lam : 0) >= a.nx, i = (ok ? lam : 0) - img * a.nx;
+        const int img = (ok ? lam : 0) >= rows, i = a.r0 + (ok ? lam : 0) - img * rows;
         v[l] = (img ? a.f2 : a.f1) + (size_t)i * a.ny;
         o[l] = ok ? (img ? a.rt2 : a.rt1) + i : nullptr;
     }
@@ -265,10 +266,10 @@ __global__ void k_box_cols(BoxArgs a) {
     const int lines = 2 * a.gj;
     const int T = (lines + kBoxLines - 1) / kBoxLines;
     const long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    const int nseg = (a.gi + a.seg2 - 1) / a.seg2;
+    const int nseg = (a.q1 - a.q0 + a.seg2 - 1) / a.seg2;
     if (idx >= (long)T * nseg) return;
     const int sg = (int)(idx / T), t = (int)(idx - (long)sg * T);
-    const int q0 = sg * a.seg2, q1 = min(q0 + a.seg2, a.gi);
+    const int q0 = a.q0 + sg * a.seg2, q1 = min(q0 + a.seg2, a.q1);
     const double* v[kBoxLines];
     double* o[kBoxLines];
 #pragma unroll
@@ -431,14 +432,14 @@ __global__ void __launch_bounds__(kTileR * kTileC) k_interp_grid(InterpArgs a) {
     __shared__ int s_jz[kTileC];       // izero along y, -1 out of range
     __shared__ unsigned char s_gj[kTileC];  // grid column
     const int ntc = (a.ny + kTileC - 1) / kTileC;
-    const int ntr = (a.nx + kTileR - 1) / kTileR;
+    const int ntr = (a.i1 - a.i0 + kTileR - 1) / kTileR;
     const float inv = 1.0f / (float)a.skip;
     const int imax = (a.gx - 1) * a.skip, jmax = (a.gy - 1) * a.skip;
     const int ti = threadIdx.x / kTileC, tj = threadIdx.x - (threadIdx.x / kTileC) * kTileC;
     for (int tile = blockIdx.x; tile < ntr * ntc; tile += gridDim.x) {
-        const int i0 = (tile / ntc) * kTileR, j0 = (tile - (tile / ntc) * ntc) * kTileC;
+        const int i0 = a.i0 + (tile / ntc) * kTileR, j0 = (tile - (tile / ntc) * ntc) * kTileC;
         // cdata rows / columns the tile's in-range pixels use
-        const int dlo = max(i0 - a.xoff, 0), dhi = min(min(i0 + kTileR, a.nx) - 1 - a.xoff, imax);
+        const int dlo = max(i0 - a.xoff, 0), dhi = min(min(i0 + kTileR, a.i1) - 1 - a.xoff, imax);
         const int elo = max(j0 - a.yoff, 0), ehi = min(min(j0 + kTileC, a.ny) - 1 - a.yoff, jmax);
         const bool any = dlo <= dhi && elo <= ehi;
         const int r0 = any ? min(dlo / a.skip, a.gx - 2) : 0, r1 = any ? min(dhi / a.skip, a.gx - 2) + 3 : -1;
@@ -469,7 +470,7 @@ __global__ void __launch_bounds__(kTileR * kTileC) k_interp_grid(InterpArgs a) {
             const int di = i0 + r - a.xoff;
             float2 v = make_float2(0.f, 0.f);
             unsigned char bad = 3;
-            if (i0 + r < a.nx && di >= 0 && di <= imax) {
+            if (i0 + r < a.i1 && di >= 0 && di <= imax) {
                 const int iz = min(di / a.skip, a.gx - 2);
                 bad = 0;
 #pragma unroll
@@ -487,7 +488,7 @@ __global__ void __launch_bounds__(kTileR * kTileC) k_interp_grid(InterpArgs a) {
         }
         __syncthreads();
         const int i = i0 + ti, j = j0 + tj;
-        if (i >= a.nx || j >= a.ny) continue;
+        if (i >= a.i1 || j >= a.ny) continue;
         const int di = i - a.xoff;
         if (s_gj[tj] && (di % a.skip) == 0) continue;  // grid points keep their computed value
         const int jz = s_jz[tj];

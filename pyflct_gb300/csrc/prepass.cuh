@@ -18,6 +18,7 @@ struct ClassifyArgs {
     double *vx, *vy, *vm;
     float2* grid;             // skip-grid (vx, vy) for the interpolation, or null
     unsigned* status;
+    int r0, r1;               // rows to classify (the work list gets their windows)
 };
 
 constexpr int kBoxLines = 4;  // independent lines (FP64 add chains) per box-sum thread
@@ -33,6 +34,8 @@ struct BoxArgs {
     int seg, seg2;            // outputs per thread of the row / column pass
     double *rt1, *rt2;        // row sums [gj][nx]
     double *b1, *b2;          // box sums [gi][gj]
+    int r0, r1;               // frame rows of the row pass
+    int q0, q1;               // grid rows of the column pass
 };
 
 // The velocity pipeline's skip-grid interpolation (FP32 arithmetic).
@@ -41,6 +44,7 @@ struct InterpArgs {
     int gx, gy;               // grid counts along the slow / fast axis
     const float2* grid;       // (vx, vy) per grid point [gx][gy]
     double *vx, *vy, *vm;
+    int i0, i1;               // output rows to interpolate
 };
 
 __global__ void k_absmax(const double* f1, const double* f2, long n, unsigned long long* out);

@@ -67,8 +67,24 @@ def outputs(b, k):
 
 
 def single(f1, f2, kw, form):
-    from pyflct_gb300.flct import flct
-    return flct(f1, f2, 1.0, 1.0, form=form, **kw)
+    """One pair through the one-shot device entry point (the batch runs the
+    same whole-frame passes, so the outputs must agree bit for bit; the
+    host-buffer entry point pipelines large frames in row bands, whose FP64
+    box sums round differently in the last bits)."""
+    import ctypes as C
+    import torch
+    from pyflct_gb300 import _lib
+    from pyflct_gb300.flct import make_params
+    ctx = _lib.context(0)
+    p = make_params(1.0, 1.0, form=form, **kw)
+    dev = torch.device("cuda", 0)
+    d1, d2 = torch.from_numpy(np.ascontiguousarray(f1)).to(dev), torch.from_numpy(np.ascontiguousarray(f2)).to(dev)
+    out = [torch.empty(f1.shape, dtype=torch.float64, device=dev) for _ in range(3)]
+    ctx.check(ctx.lib.flct_gpu_velocity_device(ctx.h, C.byref(p), C.c_void_p(d1.data_ptr()),
+                                               C.c_void_p(d2.data_ptr()), f1.shape[0], f1.shape[1],
+                                               *[C.c_void_p(o.data_ptr()) for o in out], None))
+    ctx.timing()
+    return tuple(o.cpu().numpy() for o in out)
 
 
 @pytest.mark.parametrize("form", ["fp32", "auto"])

@@ -213,3 +213,52 @@ def test_sigma0_global_shift(shape, extra):
     dv = max(abs(got[0][0, 0] - ref[0][0, 0]), abs(got[1][0, 0] - ref[1][0, 0]))
     assert dv <= TOL, (dv, got, ref)
     print(shape, extra, "dv", dv, "v", got[0][0, 0], got[1][0, 0])
+
+
+@pytest.mark.parametrize("shape,sigma,extra", [
+    ((1024, 1024), 8, {"skip": 4, "interpolate": True}),
+    ((600, 520), 5, {"skip": 3, "poffset": 1, "qoffset": 2, "interpolate": True, "thresh": 0.2,
+                     "thresh_abs": True}),
+    ((512, 700), 12, {}), ((300, 260), 4, {"hires": True}), ((520, 512), 8, {"skip": 5, "kr": 0.5}),
+])
+def test_host_entry_matches_device(shape, sigma, extra):
+    """flct_gpu_velocity (host buffers, page-locked or pageable) must give
+    the device entry point's output (velocity_device on the same frames),
+    mask exactly, and the oracle's within tolerance."""
+    import ctypes as C
+    import torch
+    from pyflct_gb300 import _lib, synth
+    from pyflct_gb300.flct import make_params
+    rng = np.random.default_rng(sum(shape) + sigma)
+    f1 = synth.kfield(shape, rng)
+    f2 = synth.fourier_shift(f1, *rng.uniform(-1.2, 1.2, 2))
+    kw = dict(sigma=sigma, **extra)
+    pageable = gpu_flct(f1, f2, kw)
+    ctx = _lib.context(0)
+    thresh = kw.get("thresh")
+    if thresh is not None and kw.get("thresh_abs"):
+        thresh = f"{thresh!r}a"
+    skip = None
+    if kw.get("skip"):
+        skip = f"{kw['skip']}p{kw.get('poffset', 0)}q{kw.get('qoffset', 0)}" + ("i" if kw.get("interpolate") else "")
+    p = make_params(1.0, 1.0, sigma, thresh=thresh, kr=kw.get("kr"), skip=skip, hires=kw.get("hires", False))
+    pin = [torch.empty(shape, dtype=torch.float64, pin_memory=True) for _ in range(5)]
+    pin[0].copy_(torch.from_numpy(f1))
+    pin[1].copy_(torch.from_numpy(f2))
+    dp = [C.cast(C.c_void_p(x.data_ptr()), C.POINTER(C.c_double)) for x in pin]
+    for _ in range(2):
+        ctx.check(ctx.lib.flct_gpu_velocity(ctx.h, C.byref(p), dp[0], dp[1], shape[0], shape[1], *dp[2:]))
+    host = [x.numpy().copy() for x in pin[2:]]
+    assert ctx.timing().windows == int((host[2] == 1).sum())
+    dev = torch.device("cuda", 0)
+    d1, d2 = torch.from_numpy(f1).to(dev), torch.from_numpy(f2).to(dev)
+    out = [torch.empty(shape, dtype=torch.float64, device=dev) for _ in range(3)]
+    ctx.check(ctx.lib.flct_gpu_velocity_device(ctx.h, C.byref(p), C.c_void_p(d1.data_ptr()),
+                                               C.c_void_p(d2.data_ptr()), shape[0], shape[1],
+                                               *[C.c_void_p(o.data_ptr()) for o in out], None))
+    ctx.timing()
+    devout = [o.cpu().numpy() for o in out]
+    for got in (host, pageable):
+        assert np.array_equal(got[2], devout[2])
+        assert np.abs(got[0] - devout[0]).max() <= 1e-5 and np.abs(got[1] - devout[1]).max() <= 1e-5
+    print(shape, sigma, extra, compare(f1, f2, host, po.velocity(f1, f2, **kw), kw))
