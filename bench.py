@@ -123,6 +123,18 @@ def dist_init():
     return ws, rank, local
 
 
+def reduce_max(value: float, device=None) -> float:
+    """Max of a per-rank number over all ranks (the job's time is its
+    slowest rank's); the identity without a process group."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def oracle():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle as po
@@ -274,10 +286,7 @@ def run_ours(a):
             clk = clocks
         wall = time.perf_counter() - wall0
         total_ms = sum(e0.elapsed_time(e1) for e0, e1 in evs)
-        if ws > 1:
-            tt = torch.tensor([total_ms], device=dev)
-            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-            total_ms = float(tt.item())
+        total_ms = reduce_max(total_ms, dev)
         res[form] = dict(value=windows * a.steps * ws / (total_ms / 1e3), ms_per_step=total_ms / a.steps,
                          window_ms=statistics.mean(win_ms), windows=windows, launches=launches, box=box,
                          wall_s=wall, used=used)
@@ -311,7 +320,7 @@ def run_ours(a):
         flush.zero_()
         torch.cuda.synchronize()
     flush_s = time.perf_counter() - t1
-    e2e_val = windows * a.steps * ws / max(1e-9, e2e_s - flush_s)
+    e2e_val = windows * a.steps * ws / max(1e-9, reduce_max(e2e_s - flush_s, dev))
 
     batch = None if a.no_batch else run_batch(a, dev, flush)
 
