@@ -308,6 +308,8 @@ flct_status launch_windows(flct_ctx* ctx, int form, const WinEntry* we, int n, c
     ta.b1 = (const float*)ctx->b_tc.p;
     ta.b2 = (const float*)ctx->b_tc.p + 32 * 32;
     ta.status = status;
+    // failure-path test hook: stage waits that run out after this many ns
+    if (const char* w = getenv("FLCT_TEST_TC_STALL_NS")) ta.stall_ns = strtoull(w, nullptr, 10);
     for (int k = 0; k < 2 * kMaxBox + 1; ++k) ta.gauss[k] = wa.gauss[k];
     for (int k = 0; k < kMaxBox; ++k) ta.filt2[k] = wa.filt2[k];
     const int which = (form == FLCT_FORM_TC_BF16) ? 1 : 0;

@@ -58,6 +58,10 @@ struct TcArgs {
     const float* b1;      // [c][j] 32 x 32: S1 matrix, row = output column c
     const float* b2;      // [n][k] 64 x 64: S2 matrix, n = (re/im, q), k = (re/im, i), kx = tc_kx(q)
     unsigned* status;
+    // failure-path test hook: when nonzero, every stage waits this many ns
+    // on a barrier that nothing completes (instead of the MMA barrier), so
+    // that the wait runs out; the exit path still waits for the real MMAs
+    unsigned long long stall_ns;
     float gauss[2 * kMaxBox + 1];
     float filt2[kMaxBox];
 };
@@ -175,6 +179,7 @@ __global__ void __launch_bounds__(128) k_window_tc32(TcArgs a) {
     float4* s_mean = reinterpret_cast<float4*>(sm + TcSmem::off_misc + 512);  // 8
     uint64_t* s_mbar = reinterpret_cast<uint64_t*>(sm + TcSmem::off_misc + 640);
     uint32_t* s_tmem = reinterpret_cast<uint32_t*>(sm + TcSmem::off_misc + 648);
+    uint64_t* s_never = reinterpret_cast<uint64_t*>(sm + TcSmem::off_misc + 696);  // test hook only
     int* s_gi = reinterpret_cast<int*>(sm + TcSmem::off_misc + 656);                    // 8
     const float2** s_src = reinterpret_cast<const float2**>(sm + TcSmem::off_misc + 704);  // 8 x 2
     int2* s_dim = reinterpret_cast<int2*>(sm + TcSmem::off_misc + 832);                 // 8
@@ -207,7 +212,10 @@ __global__ void __launch_bounds__(128) k_window_tc32(TcArgs a) {
     for (int k = t; k < 2 * N + 1; k += 128) s_g[k] = a.gauss[k];
     for (int k = t; k < N; k += 128) s_f[k] = a.use_filter ? a.filt2[k] : 1.0f;
     if (warp == 0) tc::tmem_alloc(s_tmem, 256);
-    if (t == 0) tc::mbar_init(s_mbar, 1);
+    if (t == 0) {
+        tc::mbar_init(s_mbar, 1);
+        tc::mbar_init(s_never, 1);
+    }
     tc::fence_async_smem();
     tc::fence_before();
     __syncthreads();
@@ -235,7 +243,8 @@ __global__ void __launch_bounds__(128) k_window_tc32(TcArgs a) {
     };
     // all threads: wait for the stage's MMAs; any timeout stops the kernel
     auto wait_stage = [&]() -> bool {
-        const bool done = tc::mbar_wait(s_mbar, phase, kLimit);
+        const bool done =
+            a.stall_ns ? tc::mbar_wait(s_never, 0u, a.stall_ns) : tc::mbar_wait(s_mbar, phase, kLimit);
         phase ^= 1u;
         tc::fence_after();
         return __syncthreads_and(done ? 1 : 0) != 0;

@@ -100,3 +100,23 @@ def test_auto_form_and_unsupported_box():
     with pytest.raises(FlctError) as e:
         run(a, a, "tc_fp16", sigma=4.0)
     assert e.value.code == _lib.ERR_UNSUPPORTED
+
+
+def test_stage_wait_timeout_reports_and_context_survives(monkeypatch):
+    """Failure detection without a GPU fault: the test hook makes the
+    tensor-core kernel's first stage wait on a barrier that nothing completes,
+    with a 1 ms limit; the wait runs out, the kernel lets its own MMAs finish
+    (bounded exit wait), frees its TMEM and returns, the call reports
+    FLCT_ERR_TIMEOUT, and the context computes correctly afterwards."""
+    from pyflct_gb300 import _lib, synth
+    from pyflct_gb300.flct import FlctError
+    rng = np.random.default_rng(21)
+    f1 = synth.kfield((96, 96), rng)
+    f2 = synth.fourier_shift(f1, 0.5, -0.25)
+    monkeypatch.setenv("FLCT_TEST_TC_STALL_NS", "1000000")
+    with pytest.raises(FlctError) as e:
+        run(f1, f2, "tc_fp16", sigma=8.0)
+    assert e.value.code == _lib.ERR_TIMEOUT
+    monkeypatch.delenv("FLCT_TEST_TC_STALL_NS")
+    got = run(f1, f2, "tc_fp16", sigma=8.0)
+    compare(f1, f2, got, po.velocity(f1, f2, sigma=8), dict(sigma=8), tol=TOL["tc_fp16"])
