@@ -93,8 +93,41 @@ constexpr int dif_pos(int k) {
 
 // ------------------------------------------------------ complex helpers --
 
+// Complex add / subtract / scale-and-add on the packed FP32 pipe: one
+// add.f32x2 (sub, fma) instruction for the (re, im) pair instead of two
+// scalar ones.  The FFTs are issue-bound, and these are most of their work.
+#if defined(__CUDA_ARCH__)
+#define FLCT_PACKED_OP(OP)                                                                   \
+    float2 r;                                                                                \
+    asm("{\n.reg .b64 ra, rb, rd;\nmov.b64 ra, {%2, %3};\nmov.b64 rb, {%4, %5};\n" OP   \
+        " rd, ra, rb;\nmov.b64 {%0, %1}, rd;\n}"                                             \
+        : "=f"(r.x), "=f"(r.y)                                                               \
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));                                           \
+    return r;
+FLCT_HD float2 cadd(float2 a, float2 b) { FLCT_PACKED_OP("add.rn.f32x2") }
+FLCT_HD float2 csub(float2 a, float2 b) { FLCT_PACKED_OP("sub.rn.f32x2") }
+// element-wise product (a.x * b.x, a.y * b.y)
+FLCT_HD float2 emul(float2 a, float2 b) { FLCT_PACKED_OP("mul.rn.f32x2") }
+// a * k + b for a real k
+FLCT_HD float2 cfma(float2 a, float k, float2 b) {
+    float2 r;
+    asm("{\n.reg .b64 ra, rk, rb, rd;\nmov.b64 ra, {%2, %3};\nmov.b64 rk, {%4, %4};\nmov.b64 rb, {%5, %6};\n"
+        "fma.rn.f32x2 rd, ra, rk, rb;\nmov.b64 {%0, %1}, rd;\n}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a.x), "f"(a.y), "f"(k), "f"(b.x), "f"(b.y));
+    return r;
+}
+#undef FLCT_PACKED_OP
+#else
 FLCT_HD float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 FLCT_HD float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+FLCT_HD float2 cfma(float2 a, float k, float2 b) { return make_float2(fmaf(a.x, k, b.x), fmaf(a.y, k, b.y)); }
+FLCT_HD float2 emul(float2 a, float2 b) { return make_float2(a.x * b.x, a.y * b.y); }
+#endif
+// Scalar forms, for operands that are swapped or negated halves of a pair
+// (a packed instruction would first need them moved into a register pair).
+FLCT_HD float2 cadd_s(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+FLCT_HD float2 csub_s(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 // multiply by DIR*i
 template <int DIR>
 FLCT_HD float2 mul_i(float2 a) {
@@ -131,6 +164,16 @@ FLCT_HD float2 twmul(float2 a) {
     }
 }
 
+// a + d * exp(DIR * 2*pi*i * NUM/DEN): the sum is packed unless the twiddle
+// is a quarter turn (then the product is a swap / negation, free in scalar
+// form).
+template <int DIR, long NUM, long DEN>
+FLCT_HD float2 tw_add(float2 a, float2 d) {
+    constexpr long r = ((NUM % DEN) + DEN) % DEN;
+    if constexpr ((4 * r) % DEN == 0) return cadd_s(a, twmul<DIR, NUM, DEN>(d));
+    else return cadd(a, twmul<DIR, NUM, DEN>(d));
+}
+
 // ----------------------------------------------------------- butterflies --
 
 template <int R, int DIR>
@@ -144,13 +187,13 @@ FLCT_HD void small_dft(float2* t) {
         float2 s2 = cadd(t[1], t[3]), s3 = mul_i<DIR>(csub(t[1], t[3]));
         t[0] = cadd(s0, s2);
         t[2] = csub(s0, s2);
-        t[1] = cadd(s1, s3);
-        t[3] = csub(s1, s3);
+        t[1] = cadd_s(s1, s3);
+        t[3] = csub_s(s1, s3);
     } else if constexpr (R == 3) {
         constexpr float h = 0.866025403784438646763723170752936183f;
         float2 p = cadd(t[1], t[2]), m = csub(t[1], t[2]);
         float2 a = t[0];
-        float2 u = make_float2(a.x - 0.5f * p.x, a.y - 0.5f * p.y);
+        float2 u = cfma(p, -0.5f, a);
         float2 v = mul_i<DIR>(make_float2(h * m.x, h * m.y));
         t[0] = cadd(a, p);
         t[1] = cadd(u, v);
@@ -161,11 +204,11 @@ FLCT_HD void small_dft(float2* t) {
         float2 x0 = t[0];
         float2 a1 = cadd(t[1], t[4]), a2 = cadd(t[2], t[3]);
         float2 b1 = csub(t[1], t[4]), b2 = csub(t[2], t[3]);
-        float2 t1 = make_float2(x0.x + c1 * a1.x + c2 * a2.x, x0.y + c1 * a1.y + c2 * a2.y);
-        float2 t2 = make_float2(x0.x + c2 * a1.x + c1 * a2.x, x0.y + c2 * a1.y + c1 * a2.y);
+        float2 t1 = cfma(a2, c2, cfma(a1, c1, x0));
+        float2 t2 = cfma(a2, c1, cfma(a1, c2, x0));
         float2 u1 = mul_i<DIR>(make_float2(s1 * b1.x + s2 * b2.x, s1 * b1.y + s2 * b2.y));
         float2 u2 = mul_i<DIR>(make_float2(s2 * b1.x - s1 * b2.x, s2 * b1.y - s1 * b2.y));
-        t[0] = make_float2(x0.x + a1.x + a2.x, x0.y + a1.y + a2.y);
+        t[0] = cadd(cadd(x0, a1), a2);
         t[1] = cadd(t1, u1);
         t[4] = csub(t1, u1);
         t[2] = cadd(t2, u2);

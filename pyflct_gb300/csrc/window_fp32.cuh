@@ -10,11 +10,15 @@
 // it (window_common.cuh): k_means before, k_fit (3x3 Taylor fit, velocity,
 // mask) after; this kernel does no FP64 arithmetic.
 //
-// Layout: a "team" of n threads owns one window; a CTA runs TEAMS teams in
-// lockstep.  The two real sub-images travel as one complex array
-// z = g1 + i g2 (one forward FFT for both); A and B are separated with the
-// mirror Z(-k).  The 2-D transforms are register FFTs along one axis, a
-// shared-memory transpose, and register FFTs along the other axis.  Each
+// Layout: a "team" of n threads owns one window; a CTA runs TEAMS teams
+// (teams that tile whole warps synchronise per warp).  The two real
+// sub-images travel as one complex array z = g1 + i g2 (one forward FFT for
+// both); A and B are separated with the mirror Z(-k).  The forward 2-D
+// transform is register FFTs along one axis, a shared-memory transpose, and
+// register FFTs along the other axis.  The correlation image is real, so the
+// inverse runs as one complex n x n/2 transform (even and odd output columns
+// as real and imaginary parts), half the work of a complex n x n one.  The
+// butterflies' complex adds use the packed FP32 pipe (fft_reg.cuh).  Each
 // sub-image is scaled by an exact power of two so FP32 never over- or
 // under-flows; scaling changes neither the argmax nor the fit.
 #pragma once
@@ -47,12 +51,16 @@ struct WinShape {
     static constexpr int TEAMS = (N <= 8) ? (128 / N) : (N <= 20) ? 8 : (N <= 40) ? 4 : 2;
     static constexpr int THREADS = N * TEAMS;
     static constexpr int BUF = N * (N + 1);  // float2 per team
-    static constexpr size_t head = 32 * TEAMS + ((3 * N + 1) * 4 + 15) / 16 * 16;
-    static constexpr size_t smem = head + (size_t)TEAMS * BUF * 8 + (size_t)TEAMS * N * N * 4;
+    static constexpr size_t tw_off = 32 * TEAMS + ((3 * N + 1) * 4 + 15) / 16 * 16;
+    static constexpr size_t head = tw_off + (size_t)N * 8;
+    static constexpr size_t smem = head + (size_t)TEAMS * BUF * 8;  // |c| reuses the buffer
+    // CTAs per SM the register allocation is held to (0: no constraint).
+    // Box 32: 5 CTAs at 96 registers beat 4 at 119 (measured).
+    static constexpr int MINB = (N == 32) ? 5 : 0;
 };
 
 template <int N>
-__global__ void __launch_bounds__(WinShape<N>::THREADS)
+__global__ void __launch_bounds__(WinShape<N>::THREADS, WinShape<N>::MINB)
 k_window_fp32(WinArgs a) {
     using S = WinShape<N>;
     constexpr int TEAMS = S::TEAMS;
@@ -61,15 +69,28 @@ k_window_fp32(WinArgs a) {
     unsigned* s_max = reinterpret_cast<unsigned*>(sm + 24 * TEAMS);
     float* s_g = reinterpret_cast<float*>(sm + 32 * TEAMS);
     float* s_f = s_g + (2 * N + 1);
+    float2* s_tw = reinterpret_cast<float2*>(sm + S::tw_off);  // e^{2 pi i k / N}
     float2* s_buf = reinterpret_cast<float2*>(sm + S::head);
-    float* s_abs = reinterpret_cast<float*>(s_buf + TEAMS * S::BUF);
 
     const int team = threadIdx.x / N;
     const int ln = threadIdx.x - team * N;
+    // Teams that tile whole warps synchronise per warp, so warps run
+    // independently; other team widths share warps and use the CTA barrier.
+    auto team_sync = [] {
+        if constexpr (32 % N == 0) __syncwarp();
+        else __syncthreads();
+    };
     for (int k = threadIdx.x; k < 2 * N + 1; k += blockDim.x) s_g[k] = a.gauss[k];
     for (int k = threadIdx.x; k < N; k += blockDim.x) s_f[k] = a.use_filter ? a.filt2[k] : 1.0f;
+    if (threadIdx.x == 0) {
+        sfor<0, N>([&](auto kc) {
+            constexpr int k = decltype(kc)::value;
+            constexpr CS w = ct_cossin(k, N);
+            s_tw[k] = make_float2((float)w.c, (float)w.s);
+        });
+    }
     float2* buf = s_buf + team * S::BUF;
-    float* ab = s_abs + team * N * N;
+    float* ab = reinterpret_cast<float*>(buf);  // |c|, after the last transform
     const int nwork = *a.nwork;
     if (ln == 0) {
         s_max[2 * team] = 0u;
@@ -112,6 +133,7 @@ k_window_fp32(WinArgs a) {
         float2 x[N];
         {
             const float4 mm = a.means ? __ldg(a.means + gi) : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float2 m1 = make_float2(mm.x, mm.y), m2 = make_float2(mm.z, mm.w);
             const float wc = s_g[ln + jmin - j + N];
             const float2* p1 = f1s + (size_t)imin * ny + jmin + ln;
             const float2* p2 = f2s + (size_t)imin * ny + jmin + ln;
@@ -119,23 +141,22 @@ k_window_fp32(WinArgs a) {
             float mx1 = 0.f, mx2 = 0.f;
 #pragma unroll
             for (int ii = 0; ii < N; ++ii) {
-                const float2 u = __ldg(p1 + (size_t)ii * ny);
-                const float2 v = __ldg(p2 + (size_t)ii * ny);
+                // (hi - mean hi) + (lo - mean lo), the hi and lo halves packed
+                const float2 u = csub(__ldg(p1 + (size_t)ii * ny), m1);
+                const float2 v = csub(__ldg(p2 + (size_t)ii * ny), m2);
                 const float wgt = wc * gr[ii];
-                const float d1 = (u.x - mm.x) + (u.y - mm.y);
-                const float d2 = (v.x - mm.z) + (v.y - mm.w);
-                x[ii] = make_float2(wgt * d1, wgt * d2);
+                x[ii] = make_float2(wgt * (u.x + u.y), wgt * (v.x + v.y));
                 mx1 = fmaxf(mx1, fabsf(x[ii].x));
                 mx2 = fmaxf(mx2, fabsf(x[ii].y));
             }
             atomicMax(&s_max[2 * team], __float_as_uint(mx1));
             atomicMax(&s_max[2 * team + 1], __float_as_uint(mx2));
         }
-        __syncthreads();
+        team_sync();
         {
-            const float c1 = pow2_scale(s_max[2 * team]), c2 = pow2_scale(s_max[2 * team + 1]);
+            const float2 cs = make_float2(pow2_scale(s_max[2 * team]), pow2_scale(s_max[2 * team + 1]));
 #pragma unroll
-            for (int ii = 0; ii < N; ++ii) x[ii] = make_float2(x[ii].x * c1, x[ii].y * c2);
+            for (int ii = 0; ii < N; ++ii) x[ii] = emul(x[ii], cs);
         }
 
         // forward 2-D FFT: columns in registers, transpose, rows in registers
@@ -144,7 +165,7 @@ k_window_fp32(WinArgs a) {
             constexpr int k = decltype(kc)::value;
             buf[k * (N + 1) + ln] = x[dif_pos<N>(k)];
         });
-        __syncthreads();
+        team_sync();
         // every lane has read this window's scale factors and the previous
         // window's peak key: clear both for the next use
         if (ln == 0) {
@@ -156,19 +177,18 @@ k_window_fp32(WinArgs a) {
             constexpr int jj = decltype(jc)::value;
             x[jj] = buf[ln * (N + 1) + jj];
         });
-        __syncthreads();
+        team_sync();
         dif<N, 0, -1>(x);  // thread ln now holds Z[kx = ln][ky]
         sfor<0, N>([&](auto kc) {
             constexpr int k = decltype(kc)::value;
             buf[ln * (N + 1) + k] = x[dif_pos<N>(k)];
         });
-        __syncthreads();
+        team_sync();
 
         // separate A, B from Z and its mirror, C = conj(A) B filt^2
         float2 y[N];
         {
             const int mr = (N - ln) % N;
-            const float fr = s_f[ln];
             sfor<0, N>([&](auto kc) {
                 constexpr int k = decltype(kc)::value;
                 constexpr int mk = (N - k) % N;
@@ -176,43 +196,86 @@ k_window_fp32(WinArgs a) {
                 const float2 zm = buf[mr * (N + 1) + mk];
                 const float ax = z.x + zm.x, ay = z.y - zm.y;  // 2 s1 A
                 const float bx = z.y + zm.y, by = zm.x - z.x;  // 2 s2 B
-                const float f = fr * s_f[k];
-                y[k] = make_float2(f * (ax * bx + ay * by), f * (ax * by - ay * bx));
+                y[k] = make_float2(ax * bx + ay * by, ax * by - ay * bx);
+            });
+            if (a.use_filter) {
+                const float fr = s_f[ln];
+                sfor<0, N>([&](auto kc) {
+                    constexpr int k = decltype(kc)::value;
+                    const float f = fr * s_f[k];
+                    y[k] = make_float2(f * y[k].x, f * y[k].y);
+                });
+            }
+        }
+
+        // Inverse transform of a spectrum whose image is real, at half the
+        // work of a complex N x N transform.  Along ky, the even and odd
+        // output columns come from a_k = C[k] + C[k+H] and
+        // b_k = (C[k] - C[k+H]) w^k (w = e^{2 pi i / N}); both halves have real
+        // images, so one complex N x H transform of a + i b yields
+        // c[i][2m] + i c[i][2m+1].  Rows: H-point transforms in registers.
+        constexpr int H = N / 2;
+        float2 u[H];
+        sfor<0, H>([&](auto kc) {
+            constexpr int k = decltype(kc)::value;
+            const float2 ak = cadd(y[k], y[k + H]);
+            const float2 dk = csub(y[k], y[k + H]);
+            // + i w^k dk = dk e^{2 pi i (4k + N) / 4N}
+            u[k] = tw_add<+1, 4L * k + N, 4L * N>(ak, dk);
+        });
+        dif<H, 0, +1>(u);  // u[dif_pos<H>(m)] = row kx = ln, column m
+        // Columns (kx -> i), split by the parity h of i over two lanes: with
+        // P0 = Y and P1 = Y w^kx stored side by side, lane (m, h) transforms
+        // P_h[kx'] + P_h[kx' + H] (kx' < H), which is the first radix-2 stage
+        // of the length-N column transform for outputs i = 2 i' + h.
+        team_sync();
+        {
+            const float2 tw = s_tw[ln];
+            sfor<0, H>([&](auto mc) {
+                constexpr int m = decltype(mc)::value;
+                const float2 v = u[dif_pos<H>(m)];
+                buf[ln * (N + 1) + m] = v;
+                buf[ln * (N + 1) + H + m] = make_float2(v.x * tw.x - v.y * tw.y, v.x * tw.y + v.y * tw.x);
             });
         }
-        // inverse: rows (ky -> j) in registers, transpose, columns (kx -> i)
-        dif<N, 0, +1>(y);
-        __syncthreads();
-        sfor<0, N>([&](auto jc) {
-            constexpr int jj = decltype(jc)::value;
-            buf[ln * (N + 1) + jj] = y[dif_pos<N>(jj)];
-        });
-        __syncthreads();
-        sfor<0, N>([&](auto kc) {
+        team_sync();
+        const int cm = ln % H, ch = ln / H;
+        sfor<0, H>([&](auto kc) {
             constexpr int k = decltype(kc)::value;
-            y[k] = buf[k * (N + 1) + ln];
+            u[k] = cadd(buf[k * (N + 1) + ch * H + cm], buf[(k + H) * (N + 1) + ch * H + cm]);
         });
-        dif<N, 0, +1>(y);  // y[dif_pos(i)].x = c[i][ln]
+        dif<H, 0, +1>(u);  // u[dif_pos<H>(i')] = c[2i'+h][2m] + i c[2i'+h][2m+1]
+        team_sync();  // |c| overwrites the transform buffer
 
-        // |c| in the half-shifted frame and the first strict maximum
+        // |c| in the half-shifted frame and the first strict maximum.  H is
+        // even, so the shifted row I = 2 I'' + h keeps the parity of i; a
+        // lane visits its values in increasing row-major order.
         {
-            const int J = (ln + N / 2) % N;
-            unsigned long long best = 0ull;
-            sfor<0, N>([&](auto Ic) {
-                constexpr int I = decltype(Ic)::value;
-                constexpr int ii = (I + N / 2) % N;
-                const float v = fabsf(y[dif_pos<N>(ii)].x);
-                ab[I * N + J] = v;
-                if (!(v != v)) {
-                    const unsigned long long key =
-                        ((unsigned long long)__float_as_uint(v) << 32) |
-                        (unsigned long long)(0xffffffffu - (unsigned)(I * N + J));
-                    best = key > best ? key : best;
+            const int J = (2 * cm + H) % N;
+            float bv = -1.0f;  // below every |c|; NaN never compares greater
+            int bi = 0;        // row-major index of bv less ch * N + J
+            sfor<0, H>([&](auto Ic) {
+                constexpr int I2 = decltype(Ic)::value;
+                constexpr int ip = (I2 + H / 2) % H;
+                const float2 c = u[dif_pos<H>(ip)];
+                const float v0 = fabsf(c.x), v1 = fabsf(c.y);
+                *reinterpret_cast<float2*>(ab + (2 * I2 + ch) * N + J) = make_float2(v0, v1);
+                if (v0 > bv) {
+                    bv = v0;
+                    bi = 2 * I2 * N;
+                }
+                if (v1 > bv) {
+                    bv = v1;
+                    bi = 2 * I2 * N + 1;
                 }
             });
+            // the team's maximum of (|c|, -index): the first strict maximum
+            const unsigned idx = (unsigned)(bi + ch * N + J);
+            const unsigned long long best =
+                bv >= 0.0f ? ((unsigned long long)__float_as_uint(bv) << 32) | (0xffffffffu - idx) : 0ull;
             atomicMax(&s_key[team], best);
         }
-        __syncthreads();
+        team_sync();
 
         // integer peak (all lanes decode the same key), then the team stores
         // the peak record for k_fit
