@@ -119,7 +119,20 @@ struct flct_ctx {
     int batch_pending = 0;        // pairs of the batch whose timing awaits collection
     int batch_launches = 0;
     int batch_box = 0, batch_form = 0;
-    unsigned char* hctr = nullptr;  // page-locked copy of a call's work count and status
+    unsigned char* hctr = nullptr;  // page-locked copies of a call's work counts and status words
+    // host-buffer calls in row bands, so that the copies overlap the
+    // computation: copy-in and copy-out streams, per-band events
+    static constexpr int kMaxBands = 8;
+    int host_bands_max = 6;        // FLCT_HOST_BANDS (0 or 1: one band)
+    int host_bands = 0;            // bands of the pending host call (0: not banded)
+    cudaStream_t cstream[2] = {};  // copy-in, copy-out
+    // per-band compute streams, band 0 at the highest priority: a band's
+    // windows fill the SMs the band before leaves idle at its tail, and a
+    // band's small kernels go ahead of the next band's windows
+    cudaStream_t bandstream[kMaxBands] = {};
+    // band b copied in: [b]; finished rows ready for copy-out: [kMaxBands + b];
+    // fitted: [2 kMaxBands + b]; whole-frame prepass done: [3 kMaxBands]
+    cudaEvent_t hev[3 * kMaxBands + 1] = {};
 };
 
 namespace {
@@ -595,6 +608,14 @@ flct_status enqueue_box_rows(flct_ctx* ctx, const Job& j, const JobBufs& b, int 
     return FLCT_OK;
 }
 
+// Run length (grid rows) of the column box sums, from the whole frame: a
+// range of grid rows starting at a multiple of it sums exactly as the whole.
+int box_cols_seg(const Job& j) {
+    const long T2 = (2l * j.gj + kBoxLines - 1) / kBoxLines;
+    const int nseg2 = (int)std::min<long>(j.gi, std::max(1l, (kBoxThreads + T2 - 1) / T2));
+    return (j.gi + nseg2 - 1) / nseg2;
+}
+
 // FP64 box sums of grid rows [q0, q1) (their row sums must be complete).
 flct_status enqueue_box_cols(flct_ctx* ctx, const Job& j, const JobBufs& b, int q0, int q1, cudaStream_t st,
                              int* launches) {
@@ -603,8 +624,7 @@ flct_status enqueue_box_cols(flct_ctx* ctx, const Job& j, const JobBufs& b, int 
     ba.q0 = q0;
     ba.q1 = q1;
     const long T2 = (2l * j.gj + kBoxLines - 1) / kBoxLines;
-    const int nseg2 = (int)std::min<long>(j.gi, std::max(1l, (kBoxThreads + T2 - 1) / T2));
-    ba.seg2 = (j.gi + nseg2 - 1) / nseg2;  // run length from the whole frame
+    ba.seg2 = box_cols_seg(j);
     const long t = T2 * ((q1 - q0 + ba.seg2 - 1) / ba.seg2);
     k_box_cols<<<(int)((t + 127) / 128), 128, 0, st>>>(ba);
     ++*launches;
@@ -671,7 +691,8 @@ void make_wargs(const Job& j, const JobBufs& b, WinArgs* wa) {
 }
 
 // 3x3 fit, velocity, mask and skip-grid copy per work item (flct.c:901-942).
-flct_status enqueue_fit(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaStream_t st, int* launches) {
+flct_status enqueue_fit(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaStream_t st, int* launches,
+                        long max_items = -1) {
     FitArgs fa{};
     fa.work = b.work;
     fa.nwork = (const int*)b.ctr;
@@ -688,7 +709,7 @@ flct_status enqueue_fit(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaStrea
     fa.vy = j.vy;
     fa.vm = j.vm;
     fa.grid = j.interp ? b.grid : nullptr;
-    const size_t npx = (size_t)j.nx * j.ny;
+    const size_t npx = max_items >= 0 ? (size_t)max_items : (size_t)j.nx * j.ny;
     if (j.p->hires) {
         fa.peaks_h = b.peaks_h;
         long blocks = std::min<long>((long)(npx + 3) / 4, (long)ctx->nsm * 16);
@@ -1241,6 +1262,161 @@ flct_status rebuild_batch(flct_ctx* ctx, int npairs, const flct_pair* pairs, cud
     return FLCT_OK;
 }
 
+// ------------------------------------------------ banded host calls --
+
+// Row bands of a host-buffer call.  Band b classifies pixel rows
+// [R[b], R[b+1]) (its windows are the grid rows [Q[b], Q[b+1])) and
+// completes output rows [O[b], O[b+1]).  The interpolation of an output row
+// reads two grid rows below it, so O[b+1] trails Q[b+1] by two.
+struct Bands {
+    int nb = 0;
+    int R[flct_ctx::kMaxBands + 1], Q[flct_ctx::kMaxBands + 1], O[flct_ctx::kMaxBands + 1];
+};
+
+bool plan_bands(const flct_ctx* ctx, const Job& j, Bands* bd) {
+    if (j.d.global || j.d.rel_thresh || j.gi < 1) return false;
+    for (int nb = std::min(ctx->host_bands_max, j.gi / 4); nb >= 2; --nb) {
+        bool ok = true;
+        for (int b = 0; b <= nb; ++b) bd->Q[b] = (int)((long)j.gi * b / nb);
+        for (int b = 0; b <= nb; ++b) bd->R[b] = (b == 0) ? 0 : (b == nb) ? j.nx : j.xo + bd->Q[b] * j.gs;
+        bd->O[0] = 0;
+        bd->O[nb] = j.nx;
+        for (int b = 1; b < nb; ++b)
+            bd->O[b] = j.interp ? std::min(std::max(j.xo + (bd->Q[b] - 2) * j.gs, bd->O[b - 1]), j.nx) : bd->R[b];
+        for (int b = 0; b < nb && ok; ++b)
+            if (bd->Q[b + 1] <= bd->Q[b]) ok = false;
+        if (ok) {
+            bd->nb = nb;
+            return true;
+        }
+    }
+    return false;
+}
+
+// flct_gpu_velocity in bands: each band's rows are classified as soon as
+// they are copied in, and band b's finished output rows are copied out
+// while band b + 1's windows compute.  Each kernel does the same per-window
+// and per-pixel work as in the one-band call, so the results are identical.
+flct_status velocity_banded(flct_ctx* ctx, const Job& j, const Bands& bd, int form, int grid_div,
+                            const double* f1, const double* f2, double* vx, double* vy, double* vm) {
+    const int nb = bd.nb;
+    const size_t ny = (size_t)j.ny;
+    const JobSizes z = job_sizes(j);
+    ENSURE(ctx->b_s1, z.s);
+    ENSURE(ctx->b_s2, z.s);
+    ENSURE(ctx->b_work, z.work);
+    ENSURE(ctx->b_ctr, 64 * flct_ctx::kMaxBands);
+    ENSURE(ctx->b_r1, z.r);
+    ENSURE(ctx->b_r2, z.r);
+    ENSURE(ctx->b_b1, z.b);
+    ENSURE(ctx->b_b2, z.b);
+    ENSURE(ctx->b_means, z.means);
+    ENSURE(ctx->b_peaks, z.peaks);
+    if (z.peaks_h) ENSURE(ctx->b_peaks_h, z.peaks_h);
+    if (j.interp) ENSURE(ctx->b_grid, z.grid);
+    JobBufs base;
+    base.s1 = (float2*)ctx->b_s1.p;
+    base.s2 = (float2*)ctx->b_s2.p;
+    base.work = (int*)ctx->b_work.p;
+    base.means = (float4*)ctx->b_means.p;
+    base.peaks = (PeakRec*)ctx->b_peaks.p;
+    base.peaks_h = (PeakRecH*)ctx->b_peaks_h.p;
+    base.r1 = (double*)ctx->b_r1.p;
+    base.r2 = (double*)ctx->b_r2.p;
+    base.b1 = (double*)ctx->b_b1.p;
+    base.b2 = (double*)ctx->b_b2.p;
+    base.grid = (float2*)ctx->b_grid.p;
+    // band b's work items, means and peak records start at pixel R[b] * ny
+    // (a band has at most that many windows); its counters at ctr + 64 b
+    JobBufs bb[flct_ctx::kMaxBands];
+    for (int b = 0; b < nb; ++b) {
+        bb[b] = base;
+        const size_t off = (size_t)bd.R[b] * ny;
+        bb[b].work = base.work + off;
+        bb[b].means = base.means + off;
+        bb[b].peaks = base.peaks + off;
+        bb[b].peaks_h = z.peaks_h ? base.peaks_h + off : nullptr;
+        bb[b].ctr = (unsigned char*)ctx->b_ctr.p + 64 * b;
+    }
+    cudaStream_t st = ctx->stream, cin = ctx->cstream[0], cout = ctx->cstream[1];
+    cudaStream_t* bs = ctx->bandstream;
+    constexpr int kC = flct_ctx::kMaxBands, kF = 2 * flct_ctx::kMaxBands, kP = 3 * flct_ctx::kMaxBands;
+    double *d_f1 = (double*)j.f1, *d_f2 = (double*)j.f2;
+    CK(cudaEventRecord(ctx->ev[4], st));
+    CK(cudaStreamWaitEvent(cin, ctx->ev[4], 0));
+    CK(cudaStreamWaitEvent(cout, ctx->ev[4], 0));
+    CK(cudaStreamWaitEvent(bs[0], ctx->ev[4], 0));
+    for (int b = 0; b < nb; ++b) {
+        const size_t o = (size_t)bd.R[b] * ny, len = (size_t)(bd.R[b + 1] - bd.R[b]) * ny * sizeof(double);
+        CK(cudaMemcpyAsync(d_f1 + o, f1 + o, len, cudaMemcpyHostToDevice, cin));
+        CK(cudaMemcpyAsync(d_f2 + o, f2 + o, len, cudaMemcpyHostToDevice, cin));
+        CK(cudaEventRecord(ctx->hev[b], cin));
+    }
+    int launches = 0;
+    WinArgs wa;
+    make_wargs(j, base, &wa);
+    // the classification of each band follows its copy-in; the FP64 box
+    // sums, whose time hardly shrinks with the rows they cover (a few warps
+    // per SM sub-partition wait on the FP64 pipe), run once on the whole frame
+    CK(cudaMemsetAsync(ctx->b_ctr.p, 0, 64 * nb, bs[0]));
+    flct_status s = FLCT_OK;
+    for (int b = 0; b < nb && s == FLCT_OK; ++b) {
+        CK(cudaStreamWaitEvent(bs[0], ctx->hev[b], 0));
+        s = enqueue_classify(ctx, j, bb[b], bd.R[b], bd.R[b + 1], nullptr, bs[0], &launches);
+    }
+    if (s == FLCT_OK) s = enqueue_box_rows(ctx, j, base, 0, j.nx, bs[0], &launches);
+    if (s == FLCT_OK) s = enqueue_box_cols(ctx, j, base, 0, j.gi, bs[0], &launches);
+    if (s == FLCT_OK) CK(cudaEventRecord(ctx->hev[kP], bs[0]));
+    for (int b = 0; b < nb && s == FLCT_OK; ++b) {
+        cudaStream_t sb = bs[b];
+        if (b > 0) CK(cudaStreamWaitEvent(sb, ctx->hev[kP], 0));
+        const long items = (long)(bd.R[b + 1] - bd.R[b]) * j.ny;
+        s = enqueue_means(ctx, j, bb[b], items, sb, &launches);
+        if (s != FLCT_OK) break;
+        WinArgs wb = wa;
+        wb.means = bb[b].means;
+        wb.work = bb[b].work;
+        wb.nwork = (const int*)bb[b].ctr;
+        wb.peaks = bb[b].peaks;
+        wb.peaks_h = j.p->hires ? bb[b].peaks_h : nullptr;
+        s = launch_windows(ctx, form, j.we, j.n, wb, (unsigned*)(bb[b].ctr + 4), sb, grid_div);
+        ++launches;
+        if (s == FLCT_OK) s = enqueue_fit(ctx, j, bb[b], sb, &launches, items);
+        if (s != FLCT_OK) break;
+        CK(cudaEventRecord(ctx->hev[kF + b], sb));
+        // the band's first output rows interpolate from the band before's grid
+        if (b > 0) CK(cudaStreamWaitEvent(sb, ctx->hev[kF + b - 1], 0));
+        if (j.interp) s = enqueue_interp(ctx, j, base, sb, &launches, bd.O[b], bd.O[b + 1]);
+        if (s != FLCT_OK) break;
+        CK(cudaEventRecord(ctx->hev[kC + b], sb));
+        CK(cudaStreamWaitEvent(cout, ctx->hev[kC + b], 0));
+        const size_t o = (size_t)bd.O[b] * ny, len = (size_t)(bd.O[b + 1] - bd.O[b]) * ny * sizeof(double);
+        if (len) {
+            CK(cudaMemcpyAsync(vx + o, j.vx + o, len, cudaMemcpyDeviceToHost, cout));
+            CK(cudaMemcpyAsync(vy + o, j.vy + o, len, cudaMemcpyDeviceToHost, cout));
+            CK(cudaMemcpyAsync(vm + o, j.vm + o, len, cudaMemcpyDeviceToHost, cout));
+        }
+        CK(cudaStreamWaitEvent(st, ctx->hev[kC + b], 0));
+    }
+    if (s != FLCT_OK) {
+        cudaStreamSynchronize(cin);
+        for (int b = 0; b < nb; ++b) cudaStreamSynchronize(bs[b]);
+        cudaStreamSynchronize(cout);
+        return s;
+    }
+    // every band's work count and status to page-locked memory
+    CK(cudaMemcpyAsync(ctx->hctr, ctx->b_ctr.p, 64 * nb, cudaMemcpyDeviceToHost, st));
+    CK(cudaEventRecord(ctx->ev[3], st));
+    CK(cudaEventRecord(ctx->ev[6], cout));
+    ctx->timing = flct_timing{};
+    ctx->timing.launches = launches;
+    ctx->timing.box = j.n;
+    ctx->timing.form = form;
+    ctx->host_bands = nb;
+    ctx->pending = true;
+    return FLCT_OK;
+}
+
 }  // namespace
 
 // ===================================================================== ABI
@@ -1298,7 +1474,35 @@ flct_status flct_gpu_create(int device, flct_ctx** out) {
             flct_gpu_destroy(ctx);
             return FLCT_ERR_CUDA;
         }
-    if (cudaHostAlloc((void**)&ctx->hctr, 64, cudaHostAllocDefault) != cudaSuccess) {
+    for (auto& st : ctx->cstream)
+        if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+            st = nullptr;
+            flct_gpu_destroy(ctx);
+            return FLCT_ERR_CUDA;
+        }
+    {
+        int least = 0, greatest = 0;  // numerically: greatest <= least
+        if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) {
+            flct_gpu_destroy(ctx);
+            return FLCT_ERR_CUDA;
+        }
+        for (int b = 0; b < flct_ctx::kMaxBands; ++b)
+            if (cudaStreamCreateWithPriority(&ctx->bandstream[b], cudaStreamNonBlocking,
+                                             std::min(least, greatest + b)) != cudaSuccess) {
+                ctx->bandstream[b] = nullptr;
+                flct_gpu_destroy(ctx);
+                return FLCT_ERR_CUDA;
+            }
+    }
+    for (auto& e : ctx->hev)
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+            e = nullptr;
+            flct_gpu_destroy(ctx);
+            return FLCT_ERR_CUDA;
+        }
+    if (const char* nb = getenv("FLCT_HOST_BANDS"))
+        ctx->host_bands_max = std::max(0, std::min(flct_ctx::kMaxBands, atoi(nb)));
+    if (cudaHostAlloc((void**)&ctx->hctr, 64 * flct_ctx::kMaxBands, cudaHostAllocDefault) != cudaSuccess) {
         ctx->hctr = nullptr;
         flct_gpu_destroy(ctx);
         return FLCT_ERR_ALLOC;
@@ -1314,6 +1518,10 @@ void flct_gpu_destroy(flct_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (auto& st : ctx->cstream)
+        if (st) cudaStreamSynchronize(st);
+    for (auto& st : ctx->bandstream)
+        if (st) cudaStreamSynchronize(st);
     for (auto& st : ctx->bstream)
         if (st) cudaStreamSynchronize(st);
     if (ctx->bdone) cudaEventSynchronize(ctx->bdone);
@@ -1326,6 +1534,12 @@ void flct_gpu_destroy(flct_ctx* ctx) {
         if (e) cudaEventDestroy(e);
     for (auto& e : ctx->bev)
         if (e) cudaEventDestroy(e);
+    for (auto& e : ctx->hev)
+        if (e) cudaEventDestroy(e);
+    for (auto& st : ctx->cstream)
+        if (st) cudaStreamDestroy(st);
+    for (auto& st : ctx->bandstream)
+        if (st) cudaStreamDestroy(st);
     if (ctx->hctr) cudaFreeHost(ctx->hctr);
     if (ctx->bdone) cudaEventDestroy(ctx->bdone);
     for (auto& st : ctx->bstream)
@@ -1462,19 +1676,30 @@ static flct_status collect_timing(flct_ctx* ctx) {
             status |= st;
         }
     } else {
-        int w = 0;
-        memcpy(&w, ctx->hctr, sizeof(int));
-        memcpy(&status, ctx->hctr + 4, sizeof(unsigned));
-        nwork = w;
+        // one band, or each band of a banded host call
+        const int nb = std::max(1, ctx->host_bands);
+        for (int b = 0; b < nb; ++b) {
+            int w = 0;
+            unsigned sb = 0;
+            memcpy(&w, ctx->hctr + 64 * b, sizeof(int));
+            memcpy(&sb, ctx->hctr + 64 * b + 4, sizeof(unsigned));
+            nwork += w;
+            status |= sb;
+        }
     }
     ctx->timing.windows = nwork;
-    if (!batch) {  // a batch's graph has no per-stage events
+    if (ctx->host_bands > 0) {  // stages interleave across bands: only the total
+        ctx->host_bands = 0;
+        ctx->timing.ms_total = ev_ms(ctx->ev[4], ctx->ev[3]);
+    } else if (!batch) {  // a batch's graph has no per-stage events
         ctx->timing.ms_prepass = ev_ms(ctx->ev[0], ctx->ev[1]);
         ctx->timing.ms_window = ev_ms(ctx->ev[1], ctx->ev[2]);
         ctx->timing.ms_fit = ev_ms(ctx->ev[2], ctx->ev[7]);
         ctx->timing.ms_interp = ev_ms(ctx->ev[7], ctx->ev[3]);
+        ctx->timing.ms_total = ev_ms(ctx->ev[0], ctx->ev[3]);
+    } else {
+        ctx->timing.ms_total = ev_ms(ctx->ev[0], ctx->ev[3]);
     }
-    ctx->timing.ms_total = ev_ms(ctx->ev[0], ctx->ev[3]);
     if (status & kStatusRange)
         return fail(ctx, FLCT_ERR_UNSUPPORTED, "an input magnitude exceeds the FP32 range of the GPU kernels");
     if (status & kStatusTimeout)
@@ -1496,6 +1721,30 @@ flct_status flct_gpu_velocity(flct_ctx* ctx, const flct_params* p, const double*
     ENSURE(ctx->b_vy, npx * sizeof(double));
     ENSURE(ctx->b_vm, npx * sizeof(double));
     cudaStream_t st = ctx->stream;
+    // row bands whose copies overlap the computation, once the window form
+    // is settled (a first FLCT_FORM_AUTO call tunes in one band)
+    {
+        Job j;
+        flct_status s = plan_job(ctx, p, (const double*)ctx->b_f1.p, (const double*)ctx->b_f2.p, nx, ny,
+                                 (double*)ctx->b_vx.p, (double*)ctx->b_vy.p, (double*)ctx->b_vm.p, &j);
+        if (s != FLCT_OK) return s;
+        Bands bd;
+        if (!j.d.global && (p->form != FLCT_FORM_AUTO || ctx->tune.count(j.n)) && plan_bands(ctx, j, &bd)) {
+            int form = FLCT_FORM_FP32, grid_div = 1;
+            s = pick_form(ctx, p->form, j.n, &form);
+            if (s != FLCT_OK) return s;
+            resolved_config(ctx, p->form, j.n, &form, &grid_div);
+            s = prime_form(ctx, form, j.n);
+            if (s != FLCT_OK) return s;
+            ctx->batch_pending = 0;
+            s = velocity_banded(ctx, j, bd, form, grid_div, f1, f2, vx, vy, vm);
+            if (s != FLCT_OK) return s;
+            CK(cudaEventSynchronize(ctx->ev[6]));
+            s = collect_timing(ctx);
+            ctx->timing.ms_total = ev_ms(ctx->ev[4], ctx->ev[6]);
+            return s;
+        }
+    }
     CK(cudaEventRecord(ctx->ev[4], st));
     CK(cudaMemcpyAsync(ctx->b_f1.p, f1, npx * sizeof(double), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(ctx->b_f2.p, f2, npx * sizeof(double), cudaMemcpyHostToDevice, st));

@@ -74,10 +74,15 @@ k_window_fp32(WinArgs a) {
 
     const int team = threadIdx.x / N;
     const int ln = threadIdx.x - team * N;
-    // Teams that tile whole warps synchronise per warp, so warps run
-    // independently; other team widths share warps and use the CTA barrier.
+    // Teams that tile whole warps (n = 4, 8, 16, 32) synchronise per warp,
+    // reduce with warp reductions and exchange the mirror spectrum by
+    // shuffles; other team widths share warps and go through shared memory
+    // and the CTA barrier.
+    constexpr bool kWarp = (32 % N == 0);
+    const unsigned tmask =
+        (N == 32) ? 0xffffffffu : (((1u << (N & 31)) - 1u) << ((threadIdx.x & 31) & ~(unsigned)(N - 1)));
     auto team_sync = [] {
-        if constexpr (32 % N == 0) __syncwarp();
+        if constexpr (kWarp) __syncwarp();
         else __syncthreads();
     };
     for (int k = threadIdx.x; k < 2 * N + 1; k += blockDim.x) s_g[k] = a.gauss[k];
@@ -137,7 +142,7 @@ k_window_fp32(WinArgs a) {
             const float wc = s_g[ln + jmin - j + N];
             const float2* p1 = f1s + (size_t)imin * ny + jmin + ln;
             const float2* p2 = f2s + (size_t)imin * ny + jmin + ln;
-            const float* gr = s_g + (imin - i + N);
+            const float* gr = a.gauss + (imin - i + N);  // row weights: uniform, from the parameter bank
             float mx1 = 0.f, mx2 = 0.f;
 #pragma unroll
             for (int ii = 0; ii < N; ++ii) {
@@ -149,12 +154,17 @@ k_window_fp32(WinArgs a) {
                 mx1 = fmaxf(mx1, fabsf(x[ii].x));
                 mx2 = fmaxf(mx2, fabsf(x[ii].y));
             }
-            atomicMax(&s_max[2 * team], __float_as_uint(mx1));
-            atomicMax(&s_max[2 * team + 1], __float_as_uint(mx2));
-        }
-        team_sync();
-        {
-            const float2 cs = make_float2(pow2_scale(s_max[2 * team]), pow2_scale(s_max[2 * team + 1]));
+            float2 cs;
+            if constexpr (kWarp) {
+                cs = make_float2(pow2_scale(__reduce_max_sync(tmask, __float_as_uint(mx1))),
+                                 pow2_scale(__reduce_max_sync(tmask, __float_as_uint(mx2))));
+                team_sync();  // the previous window's |c| reads are done
+            } else {
+                atomicMax(&s_max[2 * team], __float_as_uint(mx1));
+                atomicMax(&s_max[2 * team + 1], __float_as_uint(mx2));
+                team_sync();
+                cs = make_float2(pow2_scale(s_max[2 * team]), pow2_scale(s_max[2 * team + 1]));
+            }
 #pragma unroll
             for (int ii = 0; ii < N; ++ii) x[ii] = emul(x[ii], cs);
         }
@@ -166,24 +176,28 @@ k_window_fp32(WinArgs a) {
             buf[k * (N + 1) + ln] = x[dif_pos<N>(k)];
         });
         team_sync();
-        // every lane has read this window's scale factors and the previous
-        // window's peak key: clear both for the next use
-        if (ln == 0) {
-            s_max[2 * team] = 0u;
-            s_max[2 * team + 1] = 0u;
-            s_key[team] = 0ull;
+        if constexpr (!kWarp) {
+            // every lane has read this window's scale factors and the
+            // previous window's peak key: clear both for the next use
+            if (ln == 0) {
+                s_max[2 * team] = 0u;
+                s_max[2 * team + 1] = 0u;
+                s_key[team] = 0ull;
+            }
         }
         sfor<0, N>([&](auto jc) {
             constexpr int jj = decltype(jc)::value;
             x[jj] = buf[ln * (N + 1) + jj];
         });
-        team_sync();
+        if constexpr (!kWarp) team_sync();
         dif<N, 0, -1>(x);  // thread ln now holds Z[kx = ln][ky]
-        sfor<0, N>([&](auto kc) {
-            constexpr int k = decltype(kc)::value;
-            buf[ln * (N + 1) + k] = x[dif_pos<N>(k)];
-        });
-        team_sync();
+        if constexpr (!kWarp) {
+            sfor<0, N>([&](auto kc) {
+                constexpr int k = decltype(kc)::value;
+                buf[ln * (N + 1) + k] = x[dif_pos<N>(k)];
+            });
+            team_sync();
+        }
 
         // separate A, B from Z and its mirror, C = conj(A) B filt^2
         float2 y[N];
@@ -193,7 +207,13 @@ k_window_fp32(WinArgs a) {
                 constexpr int k = decltype(kc)::value;
                 constexpr int mk = (N - k) % N;
                 const float2 z = x[dif_pos<N>(k)];
-                const float2 zm = buf[mr * (N + 1) + mk];
+                float2 zm;
+                if constexpr (kWarp) {
+                    zm.x = __shfl_sync(tmask, x[dif_pos<N>(mk)].x, mr, N);
+                    zm.y = __shfl_sync(tmask, x[dif_pos<N>(mk)].y, mr, N);
+                } else {
+                    zm = buf[mr * (N + 1) + mk];
+                }
                 const float ax = z.x + zm.x, ay = z.y - zm.y;  // 2 s1 A
                 const float bx = z.y + zm.y, by = zm.x - z.x;  // 2 s2 B
                 y[k] = make_float2(ax * bx + ay * by, ax * by - ay * bx);
@@ -247,6 +267,7 @@ k_window_fp32(WinArgs a) {
         dif<H, 0, +1>(u);  // u[dif_pos<H>(i')] = c[2i'+h][2m] + i c[2i'+h][2m+1]
         team_sync();  // |c| overwrites the transform buffer
 
+        unsigned long long key;  // max over the team of (|c|, -index)
         // |c| in the half-shifted frame and the first strict maximum.  H is
         // even, so the shifted row I = 2 I'' + h keeps the parity of i; a
         // lane visits its values in increasing row-major order.
@@ -271,11 +292,18 @@ k_window_fp32(WinArgs a) {
             });
             // the team's maximum of (|c|, -index): the first strict maximum
             const unsigned idx = (unsigned)(bi + ch * N + J);
-            const unsigned long long best =
-                bv >= 0.0f ? ((unsigned long long)__float_as_uint(bv) << 32) | (0xffffffffu - idx) : 0ull;
-            atomicMax(&s_key[team], best);
+            const unsigned khi = bv >= 0.0f ? __float_as_uint(bv) : 0u;
+            const unsigned klo = bv >= 0.0f ? 0xffffffffu - idx : 0u;
+            if constexpr (kWarp) {
+                const unsigned mhi = __reduce_max_sync(tmask, khi);
+                key = ((unsigned long long)mhi << 32) | __reduce_max_sync(tmask, khi == mhi ? klo : 0u);
+                team_sync();
+            } else {
+                atomicMax(&s_key[team], ((unsigned long long)khi << 32) | klo);
+                team_sync();
+                key = s_key[team];
+            }
         }
-        team_sync();
 
         // integer peak (all lanes decode the same key), then the team stores
         // the peak record for k_fit
@@ -289,7 +317,6 @@ k_window_fp32(WinArgs a) {
                 J = 0;
                 have = true;
             } else {
-                const unsigned long long key = s_key[team];
                 const unsigned L = 0xffffffffu - (unsigned)(key & 0xffffffffull);
                 have = __uint_as_float((unsigned)(key >> 32)) != 0.0f;
                 I = have ? (int)(L / N) : N / 2;

@@ -262,3 +262,51 @@ def test_host_entry_matches_device(shape, sigma, extra):
         assert np.array_equal(got[2], devout[2])
         assert np.abs(got[0] - devout[0]).max() <= 1e-5 and np.abs(got[1] - devout[1]).max() <= 1e-5
     print(shape, sigma, extra, compare(f1, f2, host, po.velocity(f1, f2, **kw), kw))
+
+
+@pytest.mark.parametrize("shape,sigma,extra", [
+    ((1024, 1024), 8, {"skip": 4, "interpolate": True}),
+    ((600, 520), 5, {"skip": 3, "poffset": 1, "qoffset": 2, "interpolate": True, "thresh": 0.2,
+                     "thresh_abs": True}),
+    ((512, 700), 12, {}), ((300, 260), 4, {"hires": True}), ((520, 512), 8, {"skip": 5, "kr": 0.5}),
+    ((200, 96), 4, {"skip": 2, "interpolate": True}), ((130, 140), 6, {"skip": 7, "interpolate": True}),
+])
+def test_host_bands_match_one_band(shape, sigma, extra, monkeypatch):
+    """The host-buffer call in row bands (copies overlapping the kernels)
+    gives exactly the one-band call's output for every band count, the
+    window count included."""
+    import ctypes as C
+    import torch
+    from pyflct_gb300 import _lib, synth
+    from pyflct_gb300.flct import make_params
+    rng = np.random.default_rng(sum(shape) + 7 * sigma)
+    f1 = synth.kfield(shape, rng) + 2.0
+    f2 = synth.fourier_shift(f1, *rng.uniform(-1.2, 1.2, 2))
+    thresh = extra.get("thresh")
+    if thresh is not None and extra.get("thresh_abs"):
+        thresh = f"{thresh!r}a"
+    skip = None
+    if extra.get("skip"):
+        skip = (f"{extra['skip']}p{extra.get('poffset', 0)}q{extra.get('qoffset', 0)}"
+                + ("i" if extra.get("interpolate") else ""))
+    p = make_params(1.0, 1.0, sigma, thresh=thresh, kr=extra.get("kr"), skip=skip,
+                    hires=extra.get("hires", False))
+    pin = [torch.empty(shape, dtype=torch.float64, pin_memory=True) for _ in range(5)]
+    pin[0].copy_(torch.from_numpy(f1))
+    pin[1].copy_(torch.from_numpy(f2))
+    dp = [C.cast(C.c_void_p(x.data_ptr()), C.POINTER(C.c_double)) for x in pin]
+    results = {}
+    for nb in (0, 2, 3, 4, 8):
+        monkeypatch.setenv("FLCT_HOST_BANDS", str(nb))
+        ctx = _lib.Context(0)
+        for x in pin[2:]:
+            x.fill_(-7.0)
+        ctx.check(ctx.lib.flct_gpu_velocity(ctx.h, C.byref(p), dp[0], dp[1], shape[0], shape[1], *dp[2:]))
+        results[nb] = ([x.numpy().copy() for x in pin[2:]], ctx.timing().windows)
+        ctx.close()
+    ref, nref = results[0]
+    assert nref == int((ref[2] == 1).sum())
+    for nb, (got, nwin) in results.items():
+        assert nwin == nref, (nb, nwin, nref)
+        for a, b in zip(got, ref):
+            assert np.array_equal(a, b), (nb, np.abs(a - b).max())
