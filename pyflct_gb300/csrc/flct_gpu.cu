@@ -96,6 +96,7 @@ struct flct_ctx {
     int bps_tc[2] = {0, 0};
     Buf b_tc;              // tensor-core DFT matrices (b1 32x32, b2 64x64 floats)
     bool tc_ready = false;
+    bool box_attr = false;  // k_box_rows' shared-memory size is set
     bool pending = false;  // a velocity call's events await collection
     // autotuner: the fastest window configuration per box size
     struct Tune {
@@ -502,13 +503,15 @@ struct JobBufs {
     float4* means = nullptr;
     PeakRec* peaks = nullptr;
     PeakRecH* peaks_h = nullptr;  // -h only
-    double* r1 = nullptr;  // row sums [gj][nx]
-    double* r2 = nullptr;
-    double* b1 = nullptr;  // box sums [gi][gj]
-    double* b2 = nullptr;
+    BoxSum* r1 = nullptr;  // exact row sums [nx][gj]
+    BoxSum* r2 = nullptr;
+    BoxSum* b1 = nullptr;  // exact box sums [gi][gj]
+    BoxSum* b2 = nullptr;
     // 64 bytes: [0] work count (int), [4] status bits, [8..23] |f1|,|f2|
-    // maxima, [24..31] relative threshold
+    // maxima, [24..31] relative threshold, [32..39] the frames' exponents
+    // for the exact box sums
     unsigned char* ctr = nullptr;
+    unsigned* emax = nullptr;  // the job's exponents (ctr + 32 unless shared between bands)
     float2* grid = nullptr;  // skip-grid (vx, vy) [gi][gj] for the interpolation
 };
 
@@ -525,8 +528,8 @@ JobSizes job_sizes(const Job& j) {
     z.means = npx * sizeof(float4);
     z.peaks = npx * sizeof(PeakRec);
     if (j.p->hires) z.peaks_h = npx * sizeof(PeakRecH);
-    z.r = (size_t)j.gj * j.nx * sizeof(double);
-    z.b = (size_t)j.gi * j.gj * sizeof(double);
+    z.r = (size_t)j.gj * j.nx * sizeof(BoxSum);
+    z.b = (size_t)j.gi * j.gj * sizeof(BoxSum);
     if (j.interp) z.grid = (size_t)j.gi * j.gj * sizeof(float2);
     return z;
 }
@@ -557,6 +560,7 @@ flct_status enqueue_classify(flct_ctx* ctx, const Job& j, const JobBufs& b, int 
     ca.vm = j.vm;
     ca.grid = j.interp ? b.grid : nullptr;
     ca.status = (unsigned*)(b.ctr + 4);
+    ca.emax = b.emax ? b.emax : (unsigned*)(b.ctr + 32);
     ca.r0 = r0;
     ca.r1 = r1;
     const long tiles = (long)(r1 - r0) * ((j.ny + 255) / 256);
@@ -583,49 +587,41 @@ BoxArgs box_args(const Job& j, const JobBufs& b) {
     ba.rt2 = b.r2;
     ba.b1 = b.b1;
     ba.b2 = b.b2;
+    ba.emax = b.emax ? b.emax : (const unsigned*)(b.ctr + 32);
     return ba;
 }
 
-// Runs per line chosen for ~16K threads per pass: the FP64 pipe, not the
-// thread count, bounds these passes, and longer runs add less start-up.
-constexpr long kBoxThreads = 16384;
-
-// FP64 row sums of frame rows [r0, r1) at the grid's box columns.
+// Exact row sums of frame rows [r0, r1) at the grid's box columns.
 flct_status enqueue_box_rows(flct_ctx* ctx, const Job& j, const JobBufs& b, int r0, int r1, cudaStream_t st,
                              int* launches) {
     if (r1 <= r0) return FLCT_OK;
     BoxArgs ba = box_args(j, b);
     ba.r0 = r0;
     ba.r1 = r1;
-    // run length from the whole frame's line count
-    const long Tf = (2l * j.nx + kBoxLines - 1) / kBoxLines, T = (2l * (r1 - r0) + kBoxLines - 1) / kBoxLines;
-    const int nseg = (int)std::min<long>(j.gj, std::max(1l, (kBoxThreads + Tf - 1) / Tf));
-    ba.seg = (j.gj + nseg - 1) / nseg;
-    const long t = T * ((j.gj + ba.seg - 1) / ba.seg);
-    k_box_rows<<<(int)((t + 127) / 128), 128, 0, st>>>(ba);
+    // a warp pass covers P grid columns whose input span fits kRowSpan
+    ba.pass_r = std::max(1, std::min(j.gj, (kRowSpan - j.n) / j.gs + 1));
+    const long tasks = 2l * (r1 - r0) * ((j.gj + ba.pass_r - 1) / ba.pass_r);
+    const size_t smem = (size_t)kBoxWarps * (5 * (kRowSpan + 64) + 5 * 32) * sizeof(unsigned);
+    if (!ctx->box_attr) {
+        CK(cudaFuncSetAttribute(k_box_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        ctx->box_attr = true;
+    }
+    const long blocks = std::min<long>((tasks + kBoxWarps - 1) / kBoxWarps, (long)ctx->nsm * 4);
+    k_box_rows<<<(int)std::max(1l, blocks), kBoxWarps * 32, smem, st>>>(ba);
     ++*launches;
     CK(cudaGetLastError());
     return FLCT_OK;
 }
 
-// Run length (grid rows) of the column box sums, from the whole frame: a
-// range of grid rows starting at a multiple of it sums exactly as the whole.
-int box_cols_seg(const Job& j) {
-    const long T2 = (2l * j.gj + kBoxLines - 1) / kBoxLines;
-    const int nseg2 = (int)std::min<long>(j.gi, std::max(1l, (kBoxThreads + T2 - 1) / T2));
-    return (j.gi + nseg2 - 1) / nseg2;
-}
-
-// FP64 box sums of grid rows [q0, q1) (their row sums must be complete).
+// Exact box sums of grid rows [q0, q1) (their row sums must be complete).
 flct_status enqueue_box_cols(flct_ctx* ctx, const Job& j, const JobBufs& b, int q0, int q1, cudaStream_t st,
                              int* launches) {
     if (q1 <= q0) return FLCT_OK;
     BoxArgs ba = box_args(j, b);
     ba.q0 = q0;
     ba.q1 = q1;
-    const long T2 = (2l * j.gj + kBoxLines - 1) / kBoxLines;
-    ba.seg2 = box_cols_seg(j);
-    const long t = T2 * ((q1 - q0 + ba.seg2 - 1) / ba.seg2);
+    ba.run_q = (int)std::min<long>(64, std::max(1l, (2l * (q1 - q0) * j.gj + 65535) / 65536));
+    const long t = 2l * j.gj * ((q1 - q0 + ba.run_q - 1) / ba.run_q);
     k_box_cols<<<(int)((t + 127) / 128), 128, 0, st>>>(ba);
     ++*launches;
     CK(cudaGetLastError());
@@ -646,6 +642,7 @@ flct_status enqueue_means(flct_ctx* ctx, const Job& j, const JobBufs& b, long ma
     ma.gj = j.gj;
     ma.bs1 = b.b1;
     ma.bs2 = b.b2;
+    ma.emax = b.emax ? b.emax : (const unsigned*)(b.ctr + 32);
     ma.inv_n2 = 1. / ((double)j.n * j.n);
     ma.means = b.means;
     long blocks = std::min<long>((max_items + 255) / 256, (long)ctx->nsm * 8);
@@ -661,7 +658,7 @@ flct_status enqueue_prepass(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaS
     const size_t npx = (size_t)j.nx * j.ny;
     unsigned long long* d_absmax = (unsigned long long*)(b.ctr + 8);
     double* d_thr = (double*)(b.ctr + 24);
-    CK(cudaMemsetAsync(b.ctr, 0, 32, st));
+    CK(cudaMemsetAsync(b.ctr, 0, 64, st));
     if (j.d.rel_thresh) {
         k_absmax<<<ctx->nsm * 4, 256, 0, st>>>(j.f1, j.f2, (long)npx, d_absmax);
         k_thresh_final<<<1, 1, 0, st>>>(j.f1, j.f2, d_absmax, j.p->thresh, d_thr);
@@ -1065,10 +1062,10 @@ flct_status plan_batch(flct_ctx* ctx, int npairs, const flct_pair* pairs, BatchP
         JobBufs& b = bp->bufs[k];
         b.s1 = (float2*)(A + o.s1);
         b.s2 = (float2*)(A + o.s2);
-        b.r1 = (double*)(A + o.r1);
-        b.r2 = (double*)(A + o.r2);
-        b.b1 = (double*)(A + o.b1);
-        b.b2 = (double*)(A + o.b2);
+        b.r1 = (BoxSum*)(A + o.r1);
+        b.r2 = (BoxSum*)(A + o.r2);
+        b.b1 = (BoxSum*)(A + o.b1);
+        b.b2 = (BoxSum*)(A + o.b2);
         b.grid = (float2*)(A + o.grid);
         b.work = (int*)ctx->bb_work.p + o.base;
         b.means = (float4*)ctx->bb_means.p + o.base;
@@ -1321,11 +1318,12 @@ flct_status velocity_banded(flct_ctx* ctx, const Job& j, const Bands& bd, int fo
     base.means = (float4*)ctx->b_means.p;
     base.peaks = (PeakRec*)ctx->b_peaks.p;
     base.peaks_h = (PeakRecH*)ctx->b_peaks_h.p;
-    base.r1 = (double*)ctx->b_r1.p;
-    base.r2 = (double*)ctx->b_r2.p;
-    base.b1 = (double*)ctx->b_b1.p;
-    base.b2 = (double*)ctx->b_b2.p;
+    base.r1 = (BoxSum*)ctx->b_r1.p;
+    base.r2 = (BoxSum*)ctx->b_r2.p;
+    base.b1 = (BoxSum*)ctx->b_b1.p;
+    base.b2 = (BoxSum*)ctx->b_b2.p;
     base.grid = (float2*)ctx->b_grid.p;
+    base.emax = (unsigned*)((unsigned char*)ctx->b_ctr.p + 32);  // band 0's slot, shared by all bands
     // band b's work items, means and peak records start at pixel R[b] * ny
     // (a band has at most that many windows); its counters at ctr + 64 b
     JobBufs bb[flct_ctx::kMaxBands];
@@ -1603,10 +1601,10 @@ flct_status flct_gpu_velocity_device(flct_ctx* ctx, const flct_params* p, const 
     b.means = (float4*)ctx->b_means.p;
     b.peaks = (PeakRec*)ctx->b_peaks.p;
     b.peaks_h = (PeakRecH*)ctx->b_peaks_h.p;
-    b.r1 = (double*)ctx->b_r1.p;
-    b.r2 = (double*)ctx->b_r2.p;
-    b.b1 = (double*)ctx->b_b1.p;
-    b.b2 = (double*)ctx->b_b2.p;
+    b.r1 = (BoxSum*)ctx->b_r1.p;
+    b.r2 = (BoxSum*)ctx->b_r2.p;
+    b.b1 = (BoxSum*)ctx->b_b1.p;
+    b.b2 = (BoxSum*)ctx->b_b2.p;
     b.ctr = (unsigned char*)ctx->b_ctr.p;
     b.grid = (float2*)ctx->b_grid.p;
     unsigned* d_status = (unsigned*)(b.ctr + 4);
@@ -1817,6 +1815,7 @@ flct_status flct_gpu_cross_cor_batch(flct_ctx* ctx, const double* g1, const doub
     ca.nwork = (int*)(ctr + 32);
     ca.vx = ca.vy = ca.vm = nullptr;
     ca.status = (unsigned*)(ctr + 4);
+    ca.emax = (unsigned*)(ctr + 40);  // no box sums here
     ca.r0 = 0;
     ca.r1 = nwin * n;
     CK(cudaEventRecord(ctx->ev[0], st));

@@ -5,9 +5,9 @@
 //                               float hi+lo split of both frames, and the
 //                               final values of pixels without a window
 //                               (flct.c:721-755, 918-930, 1125-1133)
-//   k_box_rows / k_box_cols     FP64 box sums for the local means
-//                               (flct.c:815-827) as sliding sums, at the
-//                               boxes the skip grid needs
+//   k_box_rows / k_box_cols     exact box sums for the local means
+//                               (flct.c:815-827, fixsum.cuh) as sliding
+//                               sums, at the boxes the skip grid needs
 //   k_interp_grid               skip-grid cubic-convolution interpolation
 //                               (flct.c:958-1120 with interpcc2d,
 //                               flct.c:2226-2463) and the xmiss reset
@@ -83,6 +83,7 @@ __global__ void __launch_bounds__(256) k_classify(ClassifyArgs a) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int tpr = (a.ny + 255) >> 8;  // tiles per row
     const long ntile = (long)(a.r1 - a.r0) * tpr;
+    unsigned em1 = 0u, em2 = 0u;  // largest finite biased exponents seen
     for (long t = blockIdx.x; t < ntile; t += gridDim.x) {
         const int i = a.r0 + (int)(t / tpr);
         const int j = (int)(t - (long)(i - a.r0) * tpr) * 256 + threadIdx.x;
@@ -91,6 +92,10 @@ __global__ void __launch_bounds__(256) k_classify(ClassifyArgs a) {
         bool comp = false, grid = false;
         if (act) {
             const double fa = a.f1[k], fb = a.f2[k];
+            const unsigned ea = (unsigned)((__double_as_longlong(fa) >> 52) & 0x7ff),
+                           eb = (unsigned)((__double_as_longlong(fb) >> 52) & 0x7ff);
+            if (ea != 0x7ffu) em1 = max(em1, ea);
+            if (eb != 0x7ffu) em2 = max(em2, eb);
             const float2 sa = split_double_fast(fa), sb = split_double_fast(fb);
             a.s1[k] = sa;
             a.s2[k] = sb;
@@ -146,141 +151,158 @@ __global__ void __launch_bounds__(256) k_classify(ClassifyArgs a) {
         }
         __syncthreads();  // s_cnt / s_base are rewritten by the next tile
     }
+    // the exponents the exact box sums scale by (fixsum.cuh)
+    em1 = __reduce_max_sync(0xffffffffu, em1);
+    em2 = __reduce_max_sync(0xffffffffu, em2);
+    if (lane == 0) {
+        atomicMax(a.emax, em1);
+        atomicMax(a.emax + 1, em2);
+    }
 }
 
 // ------------------------------------------------------- box sums ----
 
-// One thread's runs of box sums along kBoxLines lines v[l][0..len) (frame
-// rows, or columns of row sums) that share their box starts: outputs
-// k = k0..k1-1 are out(l, k) = sum_{d<n} v[l][start(k) + d], start()
-// non-decreasing.  The first box is summed directly (n adds), every later
-// one by sliding column steps (an add and a subtract each), with the loads
-// of four steps issued before their adds.  A non-finite value anywhere in
-// the run switches the run to direct sums, so a NaN or an infinity taints
-// only the boxes holding it (the reference sums each box directly,
-// flct.c:815-827).  n is a multiple of 4; a null o[l] marks a padding line
-// (read from a valid line, stored nowhere).
-template <class Start>
-__device__ __forceinline__ void box_lines(const double* const (&v)[kBoxLines], double* const (&o)[kBoxLines],
-                                          long ks, int n, int k0, int k1, Start start) {
-    constexpr int L = kBoxLines;
-    double P[L];
-    bool fin = true;
-    const int s0 = start(k0);
+// Row sums RT[i][m] = sum_{jj<n} f[i][s_m + jj] at the grid's box columns
+// s_m = box_start(yo + m gs), exact (fixsum.cuh).  A warp takes one line
+// (frame, row) and a pass of grid columns whose input span fits kRowSpan.
+// Lane L converts the span's elements [L C, L C + C) (C odd, so the lanes'
+// shared-memory words fall in distinct banks) into running sums, an
+// exclusive warp scan of the lane totals gives each chunk's offset, and
+// lane L then takes grid columns M + L, M + L + 32, ...: a box sum is the
+// difference of two prefix sums, stored coalesced.
+__global__ void __launch_bounds__(kBoxWarps * 32) k_box_rows(BoxArgs a) {
+    extern __shared__ unsigned s_rw[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    constexpr int SW = kRowSpan + 64;  // staged words per array (chunks of up to C <= kRowSpan / 32 + 2)
+    unsigned* sw = s_rw + (size_t)warp * (5 * SW + 5 * 32);  // w0..w3, count; then lane offsets
+    unsigned* so = sw + 5 * SW;
+    const int rows = a.r1 - a.r0, lines = 2 * rows;
+    const int P = a.pass_r;
+    const int passes = (a.gj + P - 1) / P;
+    for (long task = (long)blockIdx.x * kBoxWarps + warp; task < (long)lines * passes;
+         task += (long)gridDim.x * kBoxWarps) {
+        const int lam = (int)(task / passes), pass = (int)(task - (long)lam * passes);
+        const int img = lam >= rows, i = a.r0 + lam - img * rows;
+        const double* __restrict__ v = (img ? a.f2 : a.f1) + (size_t)i * a.ny;
+        BoxSum* __restrict__ o = (img ? a.rt2 : a.rt1) + (size_t)i * a.gj;
+        const int ee = max((int)a.emax[img], 1);
+        const int M = pass * P, Mend = min(M + P, a.gj);
+        const int base = box_start(a.yo + M * a.gs, a.ny, a.nsize);
+        const int span = box_start(a.yo + (Mend - 1) * a.gs, a.ny, a.nsize) + a.n - base;  // <= kRowSpan
+        const int C = max(3, ((span + 31) >> 5) | 1);  // odd, >= 3: the division below is exact
+        const int e0 = min(lane * C, span), e1 = min(e0 + C, span);
+        unsigned acc[4] = {0u, 0u, 0u, 0u}, cnt = 0u;
+        for (int e = e0; e < e1; e += 4) {
+            double x[4];
 #pragma unroll
-    for (int l = 0; l < L; ++l) P[l] = 0.;
-    for (int d = 0; d < n; d += 4) {
-        double x[4][L];
+            for (int u = 0; u < 4; ++u) x[u] = (e + u < e1) ? v[base + e + u] : 0.0;
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
+            for (int u = 0; u < 4; ++u) {
+                if (e + u < e1) {
+                    fx_accum(x[u], ee, acc, cnt);
 #pragma unroll
-            for (int l = 0; l < L; ++l) x[u][l] = v[l][s0 + d + u];
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-#pragma unroll
-            for (int l = 0; l < L; ++l) {
-                fin &= finite_bits(x[u][l]);
-                P[l] = __dadd_rn(P[l], x[u][l]);
-            }
-    }
-    int k = k0;
-    int kn = s0;  // start(k) of the next output to store
-    while (k < k1 && kn == s0) {
-#pragma unroll
-        for (int l = 0; l < L; ++l)
-            if (o[l]) o[l][k * ks] = P[l];
-        if (++k < k1) kn = start(k);
-    }
-    const int cend = start(k1 - 1);
-    for (int c = s0; c < cend; c += 4) {
-        double xi[4][L], xo[4][L];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const bool ok = c + u < cend;
-#pragma unroll
-            for (int l = 0; l < L; ++l) {
-                xi[u][l] = ok ? v[l][c + u + n] : 0.;
-                xo[u][l] = ok ? v[l][c + u] : 0.;
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            if (c + u < cend) {
-#pragma unroll
-                for (int l = 0; l < L; ++l) {
-                    fin &= finite_bits(xi[u][l]) & finite_bits(xo[u][l]);
-                    P[l] = __dsub_rn(__dadd_rn(P[l], xi[u][l]), xo[u][l]);
-                }
-                while (k < k1 && kn == c + u + 1) {
-#pragma unroll
-                    for (int l = 0; l < L; ++l)
-                        if (o[l]) o[l][k * ks] = P[l];
-                    if (++k < k1) kn = start(k);
+                    for (int k = 0; k < 4; ++k) sw[k * SW + e + u] = acc[k];
+                    sw[4 * SW + e + u] = cnt;
                 }
             }
         }
-    }
-    if (!fin) {
-        for (int kk = k0; kk < k1; ++kk) {
-            const int s = start(kk);
-            for (int l = 0; l < L; ++l) {
-                if (!o[l]) continue;
-                double t = 0.;
-                for (int d = 0; d < n; ++d) t = __dadd_rn(t, v[l][s + d]);
-                o[l][kk * ks] = t;
+        // exclusive scan of the lane totals
+        unsigned t[5] = {acc[0], acc[1], acc[2], acc[3], cnt};
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            unsigned y[4], yc;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) y[k] = __shfl_up_sync(0xffffffffu, t[k], d);
+            yc = __shfl_up_sync(0xffffffffu, t[4], d);
+            if (lane >= d) {
+                unsigned z[4] = {t[0], t[1], t[2], t[3]};
+                add4(z, y);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) t[k] = z[k];
+                t[4] += yc;
             }
         }
-    }
-}
-
-// Row sums RT[m][i] = sum_{jj<n} f[i][s_m + jj] at the grid's box columns
-// s_m = box_start(yo + m gs).  Lines are (frame, row) pairs; thread t of a
-// run takes lines t, t + T, t + 2T, t + 3T (T = lines / 4, rounded up), so
-// consecutive threads store consecutive rows (coalesced).
-__global__ void k_box_rows(BoxArgs a) {
-    const int rows = a.r1 - a.r0;
-    const int lines = 2 * rows;
-    const int T = (lines + kBoxLines - 1) / kBoxLines;
-    const long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    const int nseg = (a.gj + a.seg - 1) / a.seg;
-    if (idx >= (long)T * nseg) return;
-    const int sg = (int)(idx / T), t = (int)(idx - (long)sg * T);
-    const int m0 = sg * a.seg, m1 = min(m0 + a.seg, a.gj);
-    const double* v[kBoxLines];
-    double* o[kBoxLines];
 #pragma unroll
-    for (int l = 0; l < kBoxLines; ++l) {
-        const int lam = t + l * T;
-        const bool ok = lam < lines;
-        const int img = (ok ? lam : 0) >= rows, i = a.r0 + (ok ? lam : 0) - img * rows;
-        v[l] = (img ? a.f2 : a.f1) + (size_t)i * a.ny;
-        o[l] = ok ? (img ? a.rt2 : a.rt1) + i : nullptr;
+        for (int k = 0; k < 5; ++k) {
+            const unsigned ex = __shfl_up_sync(0xffffffffu, t[k], 1);
+            so[k * 32 + lane] = lane ? ex : 0u;
+        }
+        __syncwarp();
+        const unsigned magic = 0xffffffffu / (unsigned)C + 1u;  // ceil(2^32 / C): e / C = umulhi(e, magic)
+        auto prefix = [&](int e, unsigned (&p)[4], unsigned& pc) {
+            const int L = (int)__umulhi((unsigned)e, magic);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) p[k] = sw[k * SW + e];
+            pc = sw[4 * SW + e] + so[4 * 32 + L];
+            const unsigned off[4] = {so[L], so[32 + L], so[64 + L], so[96 + L]};
+            add4(p, off);
+        };
+        for (int m = M + lane; m < Mend; m += 32) {
+            const int sb = box_start(a.yo + m * a.gs, a.ny, a.nsize) - base;
+            unsigned hiw[4], hc;
+            prefix(sb + a.n - 1, hiw, hc);
+            if (sb > 0) {
+                unsigned low[4], lc;
+                prefix(sb - 1, low, lc);
+                sub4(hiw, low);
+                hc -= lc;
+            }
+            o[m] = BoxSum{(unsigned long long)hiw[0] | ((unsigned long long)hiw[1] << 32),
+                          (unsigned long long)hiw[2] | ((unsigned long long)hiw[3] << 32), cnt_wide(hc), 0ull};
+        }
+        __syncwarp();  // the next pass overwrites the stage
     }
-    box_lines(v, o, a.nx, a.n, m0, m1, [&](int m) { return box_start(a.yo + m * a.gs, a.ny, a.nsize); });
 }
 
-// Box sums B[q][m] = sum_{ii<n} RT[m][t_q + ii] at the grid's box rows
-// t_q = box_start(xo + q gs).  Lines are (frame, grid column) pairs, spread
-// over threads as in k_box_rows.
-__global__ void k_box_cols(BoxArgs a) {
+// Box sums B[q][m] = sum_{ii<n} RT[t_q + ii][m] at the grid's box rows
+// t_q = box_start(xo + q gs), exact.  A thread takes one line (frame, grid
+// column) and a run of run_q grid rows of [q0, q1); consecutive threads
+// take consecutive columns, so loads and stores are coalesced.
+__global__ void __launch_bounds__(128) k_box_cols(BoxArgs a) {
     const int lines = 2 * a.gj;
-    const int T = (lines + kBoxLines - 1) / kBoxLines;
+    const int R = a.run_q, runs = (a.q1 - a.q0 + R - 1) / R;
     const long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    const int nseg = (a.q1 - a.q0 + a.seg2 - 1) / a.seg2;
-    if (idx >= (long)T * nseg) return;
-    const int sg = (int)(idx / T), t = (int)(idx - (long)sg * T);
-    const int q0 = a.q0 + sg * a.seg2, q1 = min(q0 + a.seg2, a.q1);
-    const double* v[kBoxLines];
-    double* o[kBoxLines];
+    if (idx >= (long)lines * runs) return;
+    const int run = (int)(idx / lines), lam = (int)(idx - (long)run * lines);
+    const int img = lam >= a.gj, m = lam - img * a.gj;
+    const BoxSum* __restrict__ v = (img ? a.rt2 : a.rt1) + m;  // row r at v[r * gj]
+    BoxSum* __restrict__ o = (img ? a.b2 : a.b1) + m;
+    const size_t gj = (size_t)a.gj;
+    const int q0 = a.q0 + run * R, q1 = min(q0 + R, a.q1);
+    int t = box_start(a.xo + q0 * a.gs, a.nx, a.nsize);
+    unsigned long long lo[4] = {0ull, 0ull, 0ull, 0ull}, hi[4] = {0ull, 0ull, 0ull, 0ull}, cnt = 0ull;
+    int d = 0;
+    for (; d + 8 <= a.n; d += 8) {
+        BoxSum r[8];
 #pragma unroll
-    for (int l = 0; l < kBoxLines; ++l) {
-        const int lam = t + l * T;
-        const bool ok = lam < lines;
-        const int img = (ok ? lam : 0) >= a.gj, m = (ok ? lam : 0) - img * a.gj;
-        v[l] = (img ? a.rt2 : a.rt1) + (size_t)m * a.nx;
-        o[l] = ok ? (img ? a.b2 : a.b1) + m : nullptr;
+        for (int u = 0; u < 8; ++u) r[u] = v[(t + d + u) * gj];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            add128(lo[u & 3], hi[u & 3], r[u].lo, r[u].hi);
+            cnt += r[u].cnt;
+        }
     }
-    box_lines(v, o, a.gj, a.n, q0, q1, [&](int q) { return box_start(a.xo + q * a.gs, a.nx, a.nsize); });
+    for (; d < a.n; ++d) {
+        const BoxSum r = v[(t + d) * gj];
+        add128(lo[0], hi[0], r.lo, r.hi);
+        cnt += r.cnt;
+    }
+    add128(lo[0], hi[0], lo[1], hi[1]);
+    add128(lo[2], hi[2], lo[3], hi[3]);
+    add128(lo[0], hi[0], lo[2], hi[2]);
+    for (int q = q0;;) {
+        o[q * gj] = BoxSum{lo[0], hi[0], cnt, 0ull};
+        if (++q >= q1) break;
+        const int tn = box_start(a.xo + q * a.gs, a.nx, a.nsize);
+#pragma unroll 4
+        for (int r = t; r < tn; ++r) {
+            const BoxSum in = v[(r + a.n) * gj], out = v[r * gj];
+            add128(lo[0], hi[0], in.lo, in.hi);
+            sub128(lo[0], hi[0], out.lo, out.hi);
+            cnt += in.cnt - out.cnt;
+        }
+        t = tn;
+    }
 }
 
 // --------------------------------------------------- interpolation ----

@@ -1,6 +1,7 @@
 // prepass.cuh -- argument structs and launch helpers for prepass.cu.
 #pragma once
 #include "common.cuh"
+#include "fixsum.cuh"
 
 namespace flct {
 
@@ -18,22 +19,28 @@ struct ClassifyArgs {
     double *vx, *vy, *vm;
     float2* grid;             // skip-grid (vx, vy) for the interpolation, or null
     unsigned* status;
+    unsigned* emax;           // [2]: largest biased exponent of the finite values per frame (atomicMax)
     int r0, r1;               // rows to classify (the work list gets their windows)
 };
 
-constexpr int kBoxLines = 4;  // independent lines (FP64 add chains) per box-sum thread
+// Row pass of the box sums: warps per block, and the longest input span a
+// warp converts into shared memory per pass.
+constexpr int kBoxWarps = 4;
+constexpr int kRowSpan = 544;
 
-// Local-mean box sums for the boxes the grid needs.  Grid point (q, m) is
-// pixel (xo + q gs, yo + m gs) (gs = 1, xo = yo = 0 without -s); its box
-// starts at (box_start(xo + q gs), box_start(yo + m gs)).
+// Local-mean box sums for the boxes the grid needs, exact (fixsum.cuh).
+// Grid point (q, m) is pixel (xo + q gs, yo + m gs) (gs = 1, xo = yo = 0
+// without -s); its box starts at (box_start(xo + q gs), box_start(yo + m gs)).
 struct BoxArgs {
     const double* f1;
     const double* f2;
     int nx, ny, n, nsize;
     int gs, xo, yo, gi, gj;   // grid step, offsets and counts (slow, fast axis)
-    int seg, seg2;            // outputs per thread of the row / column pass
-    double *rt1, *rt2;        // row sums [gj][nx]
-    double *b1, *b2;          // box sums [gi][gj]
+    const unsigned* emax;     // [2] per frame, from k_classify
+    int pass_r;               // row pass: grid columns per warp pass
+    int run_q;                // column pass: grid rows per thread
+    BoxSum *rt1, *rt2;        // row sums [nx][gj]
+    BoxSum *b1, *b2;          // box sums [gi][gj]
     int r0, r1;               // frame rows of the row pass
     int q0, q1;               // grid rows of the column pass
 };

@@ -12,6 +12,7 @@
 //            the final xmiss reset (flct.c:918-942, 1125-1133).
 #pragma once
 #include "common.cuh"
+#include "fixsum.cuh"
 
 namespace flct {
 
@@ -49,8 +50,9 @@ struct MeansArgs {
     const int* nwork;
     int ny;
     int gs, xo, yo, gj;   // grid step and offsets; box sums are [grid row][grid column]
-    const double* bs1;
-    const double* bs2;
+    const BoxSum* bs1;    // exact box sums [gi][gj] (fixsum.cuh)
+    const BoxSum* bs2;
+    const unsigned* emax; // [2]: the box sums' exponents
     double inv_n2;
     float4* means;
 };

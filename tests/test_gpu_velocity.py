@@ -125,6 +125,40 @@ def test_random_fields(shape, sigma, extra):
     print(shape, sigma, rep)
 
 
+@pytest.mark.parametrize("offset", [1.0e4, -3.0e7, 2.0e-9])
+def test_large_offsets(offset):
+    """Frames on a large (or tiny) constant offset: the local means must be
+    exact to well below the variations, or the mean-subtracted FP32 windows
+    carry a residual bump.  The exact fixed-point box sums keep them so."""
+    from pyflct_gb300 import synth
+    rng = np.random.default_rng(int(abs(offset)) % 1000 + 5)
+    f1 = synth.kfield((96, 104), rng)
+    f2 = synth.fourier_shift(f1, 0.6, -0.4)
+    scale = abs(offset) if abs(offset) < 1 else 1.0
+    a, b = f1 * scale + offset, f2 * scale + offset
+    for kw in (dict(sigma=5), dict(sigma=4, skip=3, interpolate=True)):
+        rep = compare(a, b, gpu_flct(a, b, kw), po.velocity(a, b, **kw), kw)
+        print(offset, kw, rep)
+
+
+def test_nonfinite_inputs():
+    """NaN and infinities in the frames: the boxes holding them get the
+    means a sequential double sum gives (NaN, or the infinity present), as
+    in the oracle; every other box is unaffected."""
+    from pyflct_gb300 import synth
+    rng = np.random.default_rng(11)
+    f1 = synth.kfield((90, 100), rng)
+    f2 = synth.fourier_shift(f1, 0.3, 0.5)
+    f1[10, 12] = np.nan
+    f2[60, 70] = np.inf
+    f1[70, 20] = -np.inf
+    f2[30, 80] = np.inf
+    f2[32, 84] = -np.inf
+    kw = dict(sigma=3)
+    rep = compare(f1, f2, gpu_flct(f1, f2, kw), po.velocity(f1, f2, **kw), kw)
+    print(rep)
+
+
 def test_config3_full_size_1024():
     """The headline workload (1024^2, sigma 8, -s 4i) against the oracle."""
     from pyflct_gb300 import synth
