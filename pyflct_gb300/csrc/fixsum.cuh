@@ -2,17 +2,21 @@
 //
 // The local means of the reference are FP64 box sums (source/flct.c:815-827).
 // GB300's FP64 pipe is narrow, and sliding FP64 sums round differently for
-// every run partition.  Here every finite double of a frame becomes a
-// two's-complement 128-bit integer in units of 2^(emax - 1137), emax = the
-// frame's largest biased exponent over its finite values (max(e, 1) for
+// every run partition.  Here the doubles of a span of one row become
+// two's-complement 128-bit integers in units of 2^(e - 1137), e = the span's
+// largest biased exponent over its finite values (max(e, 1) for
 // subnormals): a 53-bit significand lands at or below bit 114, so the sum
 // of up to 4096 of them (a 64 x 64 box) stays below 2^127.  Bits below the
 // unit are dropped, which touches only values 2^62 times smaller than the
-// frame's largest.  Integer sums are exact, so a box sum is the same for
-// any order, run length or band split, and is rounded once when it becomes
-// a double.  Non-finite inputs are counted instead (NaN, +inf and -inf in
-// 16-bit fields) and give the value a sequential double sum would have:
-// NaN with any NaN or with both infinities, else the infinity present.
+// span's largest.  Row sums carry their span's exponent; a run of box sums
+// down a grid column takes the largest exponent of the row sums it reads
+// and shifts the others down to it (again dropping only bits 2^62 below the
+// largest).  Spans and runs are fixed by the frame geometry alone, and
+// integer sums are exact, so every box sum is the same for any order, run
+// length or band split, and is rounded once when it becomes a double.
+// Non-finite inputs are counted instead (NaN, +inf and -inf in 16-bit
+// fields) and give the value a sequential double sum would have: NaN with
+// any NaN or with both infinities, else the infinity present.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -21,7 +25,7 @@ namespace flct {
 struct BoxSum {
     unsigned long long lo, hi;  // fixed-point sum
     unsigned long long cnt;     // NaN | +inf << 16 | -inf << 32 counts
-    unsigned long long pad;
+    unsigned long long e;       // the unit's exponent (the sum is in units of 2^(e - 1137))
 };
 
 __device__ __forceinline__ void add128(unsigned long long& lo, unsigned long long& hi, unsigned long long bl,
@@ -31,6 +35,17 @@ __device__ __forceinline__ void add128(unsigned long long& lo, unsigned long lon
 __device__ __forceinline__ void sub128(unsigned long long& lo, unsigned long long& hi, unsigned long long bl,
                                        unsigned long long bh) {
     asm("sub.cc.u64 %0, %0, %2;\n\tsubc.u64 %1, %1, %3;" : "+l"(lo), "+l"(hi) : "l"(bl), "l"(bh));
+}
+
+// Arithmetic right shift of a two's-complement 128-bit value, 0 <= d < 128.
+__device__ __forceinline__ void sar128(unsigned long long& lo, unsigned long long& hi, int d) {
+    if (d >= 64) {
+        lo = (unsigned long long)((long long)hi >> (d - 64));
+        hi = (unsigned long long)((long long)hi >> 63);
+    } else if (d > 0) {
+        lo = (lo >> d) | (hi << (64 - d));
+        hi = (unsigned long long)((long long)hi >> d);
+    }
 }
 
 // acc (four 32-bit words, two's complement) += x in units of 2^(ee - 1137);

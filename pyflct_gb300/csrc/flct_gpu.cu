@@ -37,9 +37,10 @@ struct WinEntry {
     int n;
     cudaError_t (*launch)(const WinArgs&, int, cudaStream_t);
     int (*bps)();
+    int teams;  // windows per CTA iteration
 };
 
-#define FLCT_WIN(N) {N, &launch_window_fp32<N>, &window_fp32_blocks_per_sm<N>}
+#define FLCT_WIN(N) {N, &launch_window_fp32<N>, &window_fp32_blocks_per_sm<N>, WinShape<N>::TEAMS}
 const WinEntry kWin[] = {FLCT_WIN(4),  FLCT_WIN(8),  FLCT_WIN(12), FLCT_WIN(16),
                          FLCT_WIN(20), FLCT_WIN(24), FLCT_WIN(28), FLCT_WIN(32),
                          FLCT_WIN(36), FLCT_WIN(40), FLCT_WIN(44), FLCT_WIN(48),
@@ -85,12 +86,12 @@ struct flct_ctx {
         size_t n = 0;
     };
     Buf b_s1, b_s2, b_work, b_ctr, b_r1, b_r2, b_b1, b_b2, b_gvx, b_gvy, b_ix, b_iy;
-    Buf b_f1, b_f2, b_vx, b_vy, b_vm, b_aux1, b_aux2, b_means, b_peaks, b_grid, b_peaks_h;
+    Buf b_f1, b_f2, b_vx, b_vy, b_vm, b_aux1, b_aux2, b_means, b_peaks, b_grid, b_peaks_h, b_re1, b_re2;
     std::vector<Buf*> all() {
         return {&b_s1,   &b_s2,   &b_work,   &b_ctr,    &b_r1,     &b_r2,     &b_b1,     &b_b2,
                 &b_gvx,  &b_gvy,  &b_ix,     &b_iy,     &b_f1,     &b_f2,     &b_vx,     &b_vy,
                 &b_vm,   &b_aux1, &b_aux2,   &b_means,  &b_peaks,  &b_grid,   &b_tc,     &bb_arena,
-                &bb_work, &bb_means, &bb_peaks, &bb_ctr, &bb_meta, &b_peaks_h, &bb_peaks_h};
+                &bb_work, &bb_means, &bb_peaks, &bb_ctr, &bb_meta, &b_peaks_h, &bb_peaks_h, &b_re1, &b_re2};
     }
     int bps[sizeof(kWin) / sizeof(kWin[0])] = {0};
     int bps_tc[2] = {0, 0};
@@ -124,16 +125,23 @@ struct flct_ctx {
     // host-buffer calls in row bands, so that the copies overlap the
     // computation: copy-in and copy-out streams, per-band events
     static constexpr int kMaxBands = 8;
-    int host_bands_max = 6;        // FLCT_HOST_BANDS (0 or 1: one band)
+    int host_bands_max = 4;        // FLCT_HOST_BANDS (0 or 1: one band)
     int host_bands = 0;            // bands of the pending host call (0: not banded)
     cudaStream_t cstream[2] = {};  // copy-in, copy-out
-    // per-band compute streams, band 0 at the highest priority: a band's
-    // windows fill the SMs the band before leaves idle at its tail, and a
-    // band's small kernels go ahead of the next band's windows
+    // the bands' prepass (highest priority), then per-band compute streams
+    // in falling priority: a band's windows fill the SMs the band before
+    // leaves idle at its tail, and a band's small kernels go ahead of the
+    // next band's windows
+    cudaStream_t prestream = nullptr;
     cudaStream_t bandstream[kMaxBands] = {};
     // band b copied in: [b]; finished rows ready for copy-out: [kMaxBands + b];
-    // fitted: [2 kMaxBands + b]; whole-frame prepass done: [3 kMaxBands]
-    cudaEvent_t hev[3 * kMaxBands + 1] = {};
+    // fitted: [2 kMaxBands + b]; prepass (means inputs) ready: [3 kMaxBands + b];
+    // start (fork): [4 kMaxBands]; copy-out done (join): [4 kMaxBands + 1]
+    cudaEvent_t hev[4 * kMaxBands + 2] = {};
+    // the last banded call with page-locked buffers, captured as a graph
+    cudaGraphExec_t hexec = nullptr;
+    std::vector<unsigned char> hkey;
+    int hlaunches = 0;
 };
 
 namespace {
@@ -294,11 +302,16 @@ flct_status pick_form(flct_ctx* ctx, int requested, int n, int* form) {
 }
 
 // Launch the window kernel of the chosen form on the prepared work list.
+// max_items >= 0: one CTA per group of windows up to that many items
+// instead of a persistent grid, so that CTAs retire often and kernels of
+// higher-priority streams get SMs in between (banded host calls).
 flct_status launch_windows(flct_ctx* ctx, int form, const WinEntry* we, int n, const WinArgs& wa, unsigned* status,
-                           cudaStream_t st, int grid_div = 1) {
+                           cudaStream_t st, int grid_div = 1, long max_items = -1) {
     if (grid_div < 1) grid_div = 1;
     if (form == FLCT_FORM_FP32) {
-        CK(we->launch(wa, std::max(ctx->nsm, win_grid(ctx, n) / grid_div), st));
+        int grid = std::max(ctx->nsm, win_grid(ctx, n) / grid_div);
+        if (max_items >= 0) grid = (int)std::max<long>(1, (max_items + we->teams - 1) / we->teams);
+        CK(we->launch(wa, grid, st));
         return FLCT_OK;
     }
     flct_status s = ensure_tc_tables(ctx);
@@ -330,7 +343,8 @@ flct_status launch_windows(flct_ctx* ctx, int form, const WinEntry* we, int n, c
     if (ctx->bps_tc[which] == 0)
         ctx->bps_tc[which] = std::max(1, which ? window_tc32_blocks_per_sm<__nv_bfloat16>()
                                                : window_tc32_blocks_per_sm<__half>());
-    const int grid = std::max(ctx->nsm, ctx->nsm * ctx->bps_tc[which] / grid_div);
+    int grid = std::max(ctx->nsm, ctx->nsm * ctx->bps_tc[which] / grid_div);
+    if (max_items >= 0) grid = (int)std::max<long>(1, (max_items + 7) / 8);  // 8 windows per CTA iteration
     if (which) CK(launch_window_tc32<__nv_bfloat16>(ta, grid, st));
     else CK(launch_window_tc32<__half>(ta, grid, st));
     return FLCT_OK;
@@ -507,17 +521,17 @@ struct JobBufs {
     BoxSum* r2 = nullptr;
     BoxSum* b1 = nullptr;  // exact box sums [gi][gj]
     BoxSum* b2 = nullptr;
+    int* re1 = nullptr;    // the row sums' exponents [nx][gj]
+    int* re2 = nullptr;
     // 64 bytes: [0] work count (int), [4] status bits, [8..23] |f1|,|f2|
-    // maxima, [24..31] relative threshold, [32..39] the frames' exponents
-    // for the exact box sums
+    // maxima, [24..31] relative threshold
     unsigned char* ctr = nullptr;
-    unsigned* emax = nullptr;  // the job's exponents (ctr + 32 unless shared between bands)
     float2* grid = nullptr;  // skip-grid (vx, vy) [gi][gj] for the interpolation
 };
 
 // Bytes of each workspace region of a job.
 struct JobSizes {
-    size_t s = 0, work = 0, means = 0, peaks = 0, peaks_h = 0, r = 0, b = 0, grid = 0;
+    size_t s = 0, work = 0, means = 0, peaks = 0, peaks_h = 0, r = 0, re = 0, b = 0, grid = 0;
 };
 
 JobSizes job_sizes(const Job& j) {
@@ -529,6 +543,7 @@ JobSizes job_sizes(const Job& j) {
     z.peaks = npx * sizeof(PeakRec);
     if (j.p->hires) z.peaks_h = npx * sizeof(PeakRecH);
     z.r = (size_t)j.gj * j.nx * sizeof(BoxSum);
+    z.re = (size_t)j.gj * j.nx * sizeof(int);
     z.b = (size_t)j.gi * j.gj * sizeof(BoxSum);
     if (j.interp) z.grid = (size_t)j.gi * j.gj * sizeof(float2);
     return z;
@@ -560,7 +575,6 @@ flct_status enqueue_classify(flct_ctx* ctx, const Job& j, const JobBufs& b, int 
     ca.vm = j.vm;
     ca.grid = j.interp ? b.grid : nullptr;
     ca.status = (unsigned*)(b.ctr + 4);
-    ca.emax = b.emax ? b.emax : (unsigned*)(b.ctr + 32);
     ca.r0 = r0;
     ca.r1 = r1;
     const long tiles = (long)(r1 - r0) * ((j.ny + 255) / 256);
@@ -587,7 +601,8 @@ BoxArgs box_args(const Job& j, const JobBufs& b) {
     ba.rt2 = b.r2;
     ba.b1 = b.b1;
     ba.b2 = b.b2;
-    ba.emax = b.emax ? b.emax : (const unsigned*)(b.ctr + 32);
+    ba.re1 = b.re1;
+    ba.re2 = b.re2;
     return ba;
 }
 
@@ -613,15 +628,15 @@ flct_status enqueue_box_rows(flct_ctx* ctx, const Job& j, const JobBufs& b, int 
     return FLCT_OK;
 }
 
-// Exact box sums of grid rows [q0, q1) (their row sums must be complete).
+// Exact box sums of grid rows [q0, q1) (their row sums must be complete; q0
+// a multiple of kColRun, so the runs are those of the whole frame).
 flct_status enqueue_box_cols(flct_ctx* ctx, const Job& j, const JobBufs& b, int q0, int q1, cudaStream_t st,
                              int* launches) {
     if (q1 <= q0) return FLCT_OK;
     BoxArgs ba = box_args(j, b);
     ba.q0 = q0;
     ba.q1 = q1;
-    ba.run_q = (int)std::min<long>(64, std::max(1l, (2l * (q1 - q0) * j.gj + 65535) / 65536));
-    const long t = 2l * j.gj * ((q1 - q0 + ba.run_q - 1) / ba.run_q);
+    const long t = 2l * j.gj * ((q1 - q0 + kColRun - 1) / kColRun);
     k_box_cols<<<(int)((t + 127) / 128), 128, 0, st>>>(ba);
     ++*launches;
     CK(cudaGetLastError());
@@ -642,7 +657,6 @@ flct_status enqueue_means(flct_ctx* ctx, const Job& j, const JobBufs& b, long ma
     ma.gj = j.gj;
     ma.bs1 = b.b1;
     ma.bs2 = b.b2;
-    ma.emax = b.emax ? b.emax : (const unsigned*)(b.ctr + 32);
     ma.inv_n2 = 1. / ((double)j.n * j.n);
     ma.means = b.means;
     long blocks = std::min<long>((max_items + 255) / 256, (long)ctx->nsm * 8);
@@ -1016,7 +1030,7 @@ flct_status plan_batch(flct_ctx* ctx, int npairs, const flct_pair* pairs, BatchP
     }
     // workspace: per-pair arena slices, item-indexed arrays shared by all pairs
     struct Off {
-        size_t s1, s2, r1, r2, b1, b2, grid;
+        size_t s1, s2, r1, r2, re1, re2, b1, b2, grid;
         long long base;
     };
     std::vector<Off> off(npairs);
@@ -1034,6 +1048,8 @@ flct_status plan_batch(flct_ctx* ctx, int npairs, const flct_pair* pairs, BatchP
         o.s2 = take(z.s);
         o.r1 = take(z.r);
         o.r2 = take(z.r);
+        o.re1 = take(z.re);
+        o.re2 = take(z.re);
         o.b1 = take(z.b);
         o.b2 = take(z.b);
         o.grid = take(z.grid);
@@ -1064,6 +1080,8 @@ flct_status plan_batch(flct_ctx* ctx, int npairs, const flct_pair* pairs, BatchP
         b.s2 = (float2*)(A + o.s2);
         b.r1 = (BoxSum*)(A + o.r1);
         b.r2 = (BoxSum*)(A + o.r2);
+        b.re1 = (int*)(A + o.re1);
+        b.re2 = (int*)(A + o.re2);
         b.b1 = (BoxSum*)(A + o.b1);
         b.b2 = (BoxSum*)(A + o.b2);
         b.grid = (float2*)(A + o.grid);
@@ -1263,8 +1281,10 @@ flct_status rebuild_batch(flct_ctx* ctx, int npairs, const flct_pair* pairs, cud
 
 // Row bands of a host-buffer call.  Band b classifies pixel rows
 // [R[b], R[b+1]) (its windows are the grid rows [Q[b], Q[b+1])) and
-// completes output rows [O[b], O[b+1]).  The interpolation of an output row
-// reads two grid rows below it, so O[b+1] trails Q[b+1] by two.
+// completes output rows [O[b], O[b+1]).  Its box sums and windows read
+// input rows up to a box below the band, so a band must be taller than a
+// box; the interpolation of an output row reads two grid rows below it, so
+// O[b+1] trails Q[b+1] by two.
 struct Bands {
     int nb = 0;
     int R[flct_ctx::kMaxBands + 1], Q[flct_ctx::kMaxBands + 1], O[flct_ctx::kMaxBands + 1];
@@ -1272,16 +1292,23 @@ struct Bands {
 
 bool plan_bands(const flct_ctx* ctx, const Job& j, Bands* bd) {
     if (j.d.global || j.d.rel_thresh || j.gi < 1) return false;
-    for (int nb = std::min(ctx->host_bands_max, j.gi / 4); nb >= 2; --nb) {
+    for (int nb = std::min(ctx->host_bands_max, j.gi / (2 * kColRun)); nb >= 2; --nb) {
         bool ok = true;
-        for (int b = 0; b <= nb; ++b) bd->Q[b] = (int)((long)j.gi * b / nb);
+        // band starts at multiples of the column pass's run
+        for (int b = 0; b <= nb; ++b)
+            bd->Q[b] = (b == nb) ? j.gi : (int)((long)j.gi * b / nb) / kColRun * kColRun;
         for (int b = 0; b <= nb; ++b) bd->R[b] = (b == 0) ? 0 : (b == nb) ? j.nx : j.xo + bd->Q[b] * j.gs;
         bd->O[0] = 0;
         bd->O[nb] = j.nx;
         for (int b = 1; b < nb; ++b)
             bd->O[b] = j.interp ? std::min(std::max(j.xo + (bd->Q[b] - 2) * j.gs, bd->O[b - 1]), j.nx) : bd->R[b];
-        for (int b = 0; b < nb && ok; ++b)
+        for (int b = 0; b < nb && ok; ++b) {
             if (bd->Q[b + 1] <= bd->Q[b]) ok = false;
+            // input rows the band's box sums and windows read lie in bands <= b + 1
+            const int last = j.xo + (bd->Q[b + 1] - 1) * j.gs;
+            const int need = box_start(last, j.nx, j.d.nsize) + j.n;
+            if (b + 2 <= nb && need > bd->R[b + 2]) ok = false;
+        }
         if (ok) {
             bd->nb = nb;
             return true;
@@ -1290,14 +1317,8 @@ bool plan_bands(const flct_ctx* ctx, const Job& j, Bands* bd) {
     return false;
 }
 
-// flct_gpu_velocity in bands: each band's rows are classified as soon as
-// they are copied in, and band b's finished output rows are copied out
-// while band b + 1's windows compute.  Each kernel does the same per-window
-// and per-pixel work as in the one-band call, so the results are identical.
-flct_status velocity_banded(flct_ctx* ctx, const Job& j, const Bands& bd, int form, int grid_div,
-                            const double* f1, const double* f2, double* vx, double* vy, double* vm) {
-    const int nb = bd.nb;
-    const size_t ny = (size_t)j.ny;
+// Workspace of a banded call.
+flct_status banded_buffers(flct_ctx* ctx, const Job& j) {
     const JobSizes z = job_sizes(j);
     ENSURE(ctx->b_s1, z.s);
     ENSURE(ctx->b_s2, z.s);
@@ -1305,12 +1326,30 @@ flct_status velocity_banded(flct_ctx* ctx, const Job& j, const Bands& bd, int fo
     ENSURE(ctx->b_ctr, 64 * flct_ctx::kMaxBands);
     ENSURE(ctx->b_r1, z.r);
     ENSURE(ctx->b_r2, z.r);
+    ENSURE(ctx->b_re1, z.re);
+    ENSURE(ctx->b_re2, z.re);
     ENSURE(ctx->b_b1, z.b);
     ENSURE(ctx->b_b2, z.b);
     ENSURE(ctx->b_means, z.means);
     ENSURE(ctx->b_peaks, z.peaks);
     if (z.peaks_h) ENSURE(ctx->b_peaks_h, z.peaks_h);
     if (j.interp) ENSURE(ctx->b_grid, z.grid);
+    return FLCT_OK;
+}
+
+// Enqueues flct_gpu_velocity in bands (buffers from banded_buffers): each
+// band's rows are classified and summed as soon as they (and a box of rows
+// below them) are copied in, its windows compute while later bands are
+// still copied in, and its finished output rows are copied out while later
+// bands compute.  Each kernel does the same per-window and per-pixel work as
+// in the one-band call, and the box sums are exact, so the results are
+// identical.  Every stream joins ctx->stream at the end, so the enqueue can
+// also run inside a stream capture.
+flct_status enqueue_banded(flct_ctx* ctx, const Job& j, const Bands& bd, int form, int grid_div, const double* f1,
+                           const double* f2, double* vx, double* vy, double* vm, int* nlaunch) {
+    const int nb = bd.nb;
+    const size_t ny = (size_t)j.ny;
+    const JobSizes z = job_sizes(j);
     JobBufs base;
     base.s1 = (float2*)ctx->b_s1.p;
     base.s2 = (float2*)ctx->b_s2.p;
@@ -1323,7 +1362,8 @@ flct_status velocity_banded(flct_ctx* ctx, const Job& j, const Bands& bd, int fo
     base.b1 = (BoxSum*)ctx->b_b1.p;
     base.b2 = (BoxSum*)ctx->b_b2.p;
     base.grid = (float2*)ctx->b_grid.p;
-    base.emax = (unsigned*)((unsigned char*)ctx->b_ctr.p + 32);  // band 0's slot, shared by all bands
+    base.re1 = (int*)ctx->b_re1.p;
+    base.re2 = (int*)ctx->b_re2.p;
     // band b's work items, means and peak records start at pixel R[b] * ny
     // (a band has at most that many windows); its counters at ctr + 64 b
     JobBufs bb[flct_ctx::kMaxBands];
@@ -1336,14 +1376,14 @@ flct_status velocity_banded(flct_ctx* ctx, const Job& j, const Bands& bd, int fo
         bb[b].peaks_h = z.peaks_h ? base.peaks_h + off : nullptr;
         bb[b].ctr = (unsigned char*)ctx->b_ctr.p + 64 * b;
     }
-    cudaStream_t st = ctx->stream, cin = ctx->cstream[0], cout = ctx->cstream[1];
+    cudaStream_t st = ctx->stream, cin = ctx->cstream[0], cout = ctx->cstream[1], pre = ctx->prestream;
     cudaStream_t* bs = ctx->bandstream;
-    constexpr int kC = flct_ctx::kMaxBands, kF = 2 * flct_ctx::kMaxBands, kP = 3 * flct_ctx::kMaxBands;
+    constexpr int kB = flct_ctx::kMaxBands, kC = kB, kF = 2 * kB, kP = 3 * kB, kFork = 4 * kB, kJoin = 4 * kB + 1;
     double *d_f1 = (double*)j.f1, *d_f2 = (double*)j.f2;
-    CK(cudaEventRecord(ctx->ev[4], st));
-    CK(cudaStreamWaitEvent(cin, ctx->ev[4], 0));
-    CK(cudaStreamWaitEvent(cout, ctx->ev[4], 0));
-    CK(cudaStreamWaitEvent(bs[0], ctx->ev[4], 0));
+    CK(cudaEventRecord(ctx->hev[kFork], st));
+    CK(cudaStreamWaitEvent(cin, ctx->hev[kFork], 0));
+    CK(cudaStreamWaitEvent(cout, ctx->hev[kFork], 0));
+    CK(cudaStreamWaitEvent(pre, ctx->hev[kFork], 0));
     for (int b = 0; b < nb; ++b) {
         const size_t o = (size_t)bd.R[b] * ny, len = (size_t)(bd.R[b + 1] - bd.R[b]) * ny * sizeof(double);
         CK(cudaMemcpyAsync(d_f1 + o, f1 + o, len, cudaMemcpyHostToDevice, cin));
@@ -1353,22 +1393,26 @@ flct_status velocity_banded(flct_ctx* ctx, const Job& j, const Bands& bd, int fo
     int launches = 0;
     WinArgs wa;
     make_wargs(j, base, &wa);
-    // the classification of each band follows its copy-in; the FP64 box
-    // sums, whose time hardly shrinks with the rows they cover (a few warps
-    // per SM sub-partition wait on the FP64 pipe), run once on the whole frame
-    CK(cudaMemsetAsync(ctx->b_ctr.p, 0, 64 * nb, bs[0]));
+    // prepass, one band ahead: band b's box sums (and windows) read input
+    // rows of band b + 1, so they follow its classification and row sums
+    CK(cudaMemsetAsync(ctx->b_ctr.p, 0, 64 * nb, pre));
     flct_status s = FLCT_OK;
-    for (int b = 0; b < nb && s == FLCT_OK; ++b) {
-        CK(cudaStreamWaitEvent(bs[0], ctx->hev[b], 0));
-        s = enqueue_classify(ctx, j, bb[b], bd.R[b], bd.R[b + 1], nullptr, bs[0], &launches);
+    for (int b = 0; b <= nb && s == FLCT_OK; ++b) {
+        if (b < nb) {
+            CK(cudaStreamWaitEvent(pre, ctx->hev[b], 0));
+            s = enqueue_classify(ctx, j, bb[b], bd.R[b], bd.R[b + 1], nullptr, pre, &launches);
+            if (s == FLCT_OK) s = enqueue_box_rows(ctx, j, base, bd.R[b], bd.R[b + 1], pre, &launches);
+        }
+        if (s == FLCT_OK && b > 0) {
+            s = enqueue_box_cols(ctx, j, base, bd.Q[b - 1], bd.Q[b], pre, &launches);
+            CK(cudaEventRecord(ctx->hev[kP + b - 1], pre));
+        }
     }
-    if (s == FLCT_OK) s = enqueue_box_rows(ctx, j, base, 0, j.nx, bs[0], &launches);
-    if (s == FLCT_OK) s = enqueue_box_cols(ctx, j, base, 0, j.gi, bs[0], &launches);
-    if (s == FLCT_OK) CK(cudaEventRecord(ctx->hev[kP], bs[0]));
     for (int b = 0; b < nb && s == FLCT_OK; ++b) {
         cudaStream_t sb = bs[b];
-        if (b > 0) CK(cudaStreamWaitEvent(sb, ctx->hev[kP], 0));
-        const long items = (long)(bd.R[b + 1] - bd.R[b]) * j.ny;
+        CK(cudaStreamWaitEvent(sb, ctx->hev[kP + b], 0));
+        // the band's windows: at most its grid points
+        const long items = (long)(bd.Q[b + 1] - bd.Q[b]) * j.gj;
         s = enqueue_means(ctx, j, bb[b], items, sb, &launches);
         if (s != FLCT_OK) break;
         WinArgs wb = wa;
@@ -1377,7 +1421,7 @@ flct_status velocity_banded(flct_ctx* ctx, const Job& j, const Bands& bd, int fo
         wb.nwork = (const int*)bb[b].ctr;
         wb.peaks = bb[b].peaks;
         wb.peaks_h = j.p->hires ? bb[b].peaks_h : nullptr;
-        s = launch_windows(ctx, form, j.we, j.n, wb, (unsigned*)(bb[b].ctr + 4), sb, grid_div);
+        s = launch_windows(ctx, form, j.we, j.n, wb, (unsigned*)(bb[b].ctr + 4), sb, grid_div, items);
         ++launches;
         if (s == FLCT_OK) s = enqueue_fit(ctx, j, bb[b], sb, &launches, items);
         if (s != FLCT_OK) break;
@@ -1396,21 +1440,102 @@ flct_status velocity_banded(flct_ctx* ctx, const Job& j, const Bands& bd, int fo
         }
         CK(cudaStreamWaitEvent(st, ctx->hev[kC + b], 0));
     }
-    if (s != FLCT_OK) {
-        cudaStreamSynchronize(cin);
-        for (int b = 0; b < nb; ++b) cudaStreamSynchronize(bs[b]);
-        cudaStreamSynchronize(cout);
-        return s;
-    }
-    // every band's work count and status to page-locked memory
+    if (s != FLCT_OK) return s;
+    // every band's work count and status to page-locked memory; the
+    // copy-out and the copy-in stream join the call's stream
     CK(cudaMemcpyAsync(ctx->hctr, ctx->b_ctr.p, 64 * nb, cudaMemcpyDeviceToHost, st));
+    CK(cudaEventRecord(ctx->hev[kJoin], cout));
+    CK(cudaStreamWaitEvent(st, ctx->hev[kJoin], 0));
+    CK(cudaEventRecord(ctx->hev[kJoin], cin));
+    CK(cudaStreamWaitEvent(st, ctx->hev[kJoin], 0));
+    CK(cudaEventRecord(ctx->hev[kJoin], pre));
+    CK(cudaStreamWaitEvent(st, ctx->hev[kJoin], 0));
+    *nlaunch = launches;
+    return FLCT_OK;
+}
+
+bool page_locked(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
+// flct_gpu_velocity in bands (see Bands).  With page-locked host buffers the
+// whole enqueue is captured once as a CUDA graph and replayed while the
+// call's parameters, sizes and pointers stay the same: one launch instead
+// of ~100 stream operations per call.
+flct_status velocity_banded(flct_ctx* ctx, const Job& j, const Bands& bd, int form, int grid_div,
+                            const double* f1, const double* f2, double* vx, double* vy, double* vm) {
+    flct_status s = banded_buffers(ctx, j);
+    if (s != FLCT_OK) return s;
+    cudaStream_t st = ctx->stream;
+    int launches = 0;
+    const bool graph = page_locked(f1) && page_locked(f2) && page_locked(vx) && page_locked(vy) && page_locked(vm);
+    if (graph) {
+        std::vector<unsigned char> key;
+        auto put = [&key](const void* v, size_t n) {
+            const unsigned char* c = (const unsigned char*)v;
+            key.insert(key.end(), c, c + n);
+        };
+        const flct_params& p = *j.p;
+        const int ints[] = {j.nx, j.ny, bd.nb, form, grid_div, p.thresh_abs, p.skip, p.poffset, p.qoffset,
+                            p.interpolate, p.filter, p.hires};
+        const double dbl[] = {p.deltat, p.deltas, p.sigma, p.thresh, p.kr};
+        const void* ptrs[] = {f1, f2, vx, vy, vm, ctx->b_f1.p, ctx->b_f2.p, ctx->b_vx.p, ctx->b_vy.p, ctx->b_vm.p,
+                              ctx->b_s1.p, ctx->b_s2.p, ctx->b_work.p, ctx->b_ctr.p, ctx->b_r1.p, ctx->b_r2.p,
+                              ctx->b_b1.p, ctx->b_b2.p, ctx->b_means.p, ctx->b_peaks.p, ctx->b_peaks_h.p,
+                              ctx->b_grid.p, ctx->b_tc.p, ctx->hctr, ctx->b_re1.p, ctx->b_re2.p};
+        put(ints, sizeof(ints));
+        put(dbl, sizeof(dbl));
+        put(ptrs, sizeof(ptrs));
+        if (!ctx->hexec || key != ctx->hkey) {
+            if (ctx->hexec) {
+                cudaGraphExecDestroy(ctx->hexec);
+                ctx->hexec = nullptr;
+            }
+            ctx->hkey.clear();
+            CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+            s = enqueue_banded(ctx, j, bd, form, grid_div, f1, f2, vx, vy, vm, &launches);
+            cudaGraph_t g = nullptr;
+            const cudaError_t ec = cudaStreamEndCapture(st, &g);
+            if (s != FLCT_OK || ec != cudaSuccess) {
+                if (g) cudaGraphDestroy(g);
+                cudaGetLastError();
+                if (s != FLCT_OK) return s;
+                return fail(ctx, FLCT_ERR_CUDA, "capturing the banded call failed: %s", cudaGetErrorString(ec));
+            }
+            // keep the band streams' priorities inside the graph
+            const cudaError_t ei =
+                cudaGraphInstantiateWithFlags(&ctx->hexec, g, cudaGraphInstantiateFlagUseNodePriority);
+            cudaGraphDestroy(g);
+            if (ei != cudaSuccess) {
+                ctx->hexec = nullptr;
+                return fail(ctx, FLCT_ERR_CUDA, "instantiating the banded graph failed: %s", cudaGetErrorString(ei));
+            }
+            ctx->hkey = key;
+            ctx->hlaunches = launches;
+        }
+        launches = ctx->hlaunches;
+        CK(cudaEventRecord(ctx->ev[4], st));
+        CK(cudaGraphLaunch(ctx->hexec, st));
+    } else {
+        CK(cudaEventRecord(ctx->ev[4], st));
+        s = enqueue_banded(ctx, j, bd, form, grid_div, f1, f2, vx, vy, vm, &launches);
+        if (s != FLCT_OK) {
+            cudaStreamSynchronize(st);
+            return s;
+        }
+    }
     CK(cudaEventRecord(ctx->ev[3], st));
-    CK(cudaEventRecord(ctx->ev[6], cout));
+    CK(cudaEventRecord(ctx->ev[6], st));
     ctx->timing = flct_timing{};
     ctx->timing.launches = launches;
     ctx->timing.box = j.n;
     ctx->timing.form = form;
-    ctx->host_bands = nb;
+    ctx->host_bands = bd.nb;
     ctx->pending = true;
     return FLCT_OK;
 }
@@ -1484,9 +1609,14 @@ flct_status flct_gpu_create(int device, flct_ctx** out) {
             flct_gpu_destroy(ctx);
             return FLCT_ERR_CUDA;
         }
+        if (cudaStreamCreateWithPriority(&ctx->prestream, cudaStreamNonBlocking, greatest) != cudaSuccess) {
+            ctx->prestream = nullptr;
+            flct_gpu_destroy(ctx);
+            return FLCT_ERR_CUDA;
+        }
         for (int b = 0; b < flct_ctx::kMaxBands; ++b)
             if (cudaStreamCreateWithPriority(&ctx->bandstream[b], cudaStreamNonBlocking,
-                                             std::min(least, greatest + b)) != cudaSuccess) {
+                                             std::min(least, greatest + 1 + b)) != cudaSuccess) {
                 ctx->bandstream[b] = nullptr;
                 flct_gpu_destroy(ctx);
                 return FLCT_ERR_CUDA;
@@ -1520,10 +1650,12 @@ void flct_gpu_destroy(flct_ctx* ctx) {
         if (st) cudaStreamSynchronize(st);
     for (auto& st : ctx->bandstream)
         if (st) cudaStreamSynchronize(st);
+    if (ctx->prestream) cudaStreamSynchronize(ctx->prestream);
     for (auto& st : ctx->bstream)
         if (st) cudaStreamSynchronize(st);
     if (ctx->bdone) cudaEventSynchronize(ctx->bdone);
     if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+    if (ctx->hexec) cudaGraphExecDestroy(ctx->hexec);
     for (auto* b : ctx->all())
         if (b->p) cudaFree(b->p);
     for (auto& e : ctx->ev)
@@ -1538,6 +1670,7 @@ void flct_gpu_destroy(flct_ctx* ctx) {
         if (st) cudaStreamDestroy(st);
     for (auto& st : ctx->bandstream)
         if (st) cudaStreamDestroy(st);
+    if (ctx->prestream) cudaStreamDestroy(ctx->prestream);
     if (ctx->hctr) cudaFreeHost(ctx->hctr);
     if (ctx->bdone) cudaEventDestroy(ctx->bdone);
     for (auto& st : ctx->bstream)
@@ -1586,6 +1719,8 @@ flct_status flct_gpu_velocity_device(flct_ctx* ctx, const flct_params* p, const 
     ENSURE(ctx->b_ctr, 64);
     ENSURE(ctx->b_r1, z.r);
     ENSURE(ctx->b_r2, z.r);
+    ENSURE(ctx->b_re1, z.re);
+    ENSURE(ctx->b_re2, z.re);
     ENSURE(ctx->b_b1, z.b);
     ENSURE(ctx->b_b2, z.b);
     ENSURE(ctx->b_means, z.means);
@@ -1603,6 +1738,8 @@ flct_status flct_gpu_velocity_device(flct_ctx* ctx, const flct_params* p, const 
     b.peaks_h = (PeakRecH*)ctx->b_peaks_h.p;
     b.r1 = (BoxSum*)ctx->b_r1.p;
     b.r2 = (BoxSum*)ctx->b_r2.p;
+    b.re1 = (int*)ctx->b_re1.p;
+    b.re2 = (int*)ctx->b_re2.p;
     b.b1 = (BoxSum*)ctx->b_b1.p;
     b.b2 = (BoxSum*)ctx->b_b2.p;
     b.ctr = (unsigned char*)ctx->b_ctr.p;
@@ -1815,7 +1952,6 @@ flct_status flct_gpu_cross_cor_batch(flct_ctx* ctx, const double* g1, const doub
     ca.nwork = (int*)(ctr + 32);
     ca.vx = ca.vy = ca.vm = nullptr;
     ca.status = (unsigned*)(ctr + 4);
-    ca.emax = (unsigned*)(ctr + 40);  // no box sums here
     ca.r0 = 0;
     ca.r1 = nwin * n;
     CK(cudaEventRecord(ctx->ev[0], st));

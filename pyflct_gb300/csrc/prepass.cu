@@ -83,7 +83,6 @@ __global__ void __launch_bounds__(256) k_classify(ClassifyArgs a) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int tpr = (a.ny + 255) >> 8;  // tiles per row
     const long ntile = (long)(a.r1 - a.r0) * tpr;
-    unsigned em1 = 0u, em2 = 0u;  // largest finite biased exponents seen
     for (long t = blockIdx.x; t < ntile; t += gridDim.x) {
         const int i = a.r0 + (int)(t / tpr);
         const int j = (int)(t - (long)(i - a.r0) * tpr) * 256 + threadIdx.x;
@@ -92,10 +91,6 @@ __global__ void __launch_bounds__(256) k_classify(ClassifyArgs a) {
         bool comp = false, grid = false;
         if (act) {
             const double fa = a.f1[k], fb = a.f2[k];
-            const unsigned ea = (unsigned)((__double_as_longlong(fa) >> 52) & 0x7ff),
-                           eb = (unsigned)((__double_as_longlong(fb) >> 52) & 0x7ff);
-            if (ea != 0x7ffu) em1 = max(em1, ea);
-            if (eb != 0x7ffu) em2 = max(em2, eb);
             const float2 sa = split_double_fast(fa), sb = split_double_fast(fb);
             a.s1[k] = sa;
             a.s2[k] = sb;
@@ -151,21 +146,15 @@ __global__ void __launch_bounds__(256) k_classify(ClassifyArgs a) {
         }
         __syncthreads();  // s_cnt / s_base are rewritten by the next tile
     }
-    // the exponents the exact box sums scale by (fixsum.cuh)
-    em1 = __reduce_max_sync(0xffffffffu, em1);
-    em2 = __reduce_max_sync(0xffffffffu, em2);
-    if (lane == 0) {
-        atomicMax(a.emax, em1);
-        atomicMax(a.emax + 1, em2);
-    }
 }
 
 // ------------------------------------------------------- box sums ----
 
 // Row sums RT[i][m] = sum_{jj<n} f[i][s_m + jj] at the grid's box columns
 // s_m = box_start(yo + m gs), exact (fixsum.cuh).  A warp takes one line
-// (frame, row) and a pass of grid columns whose input span fits kRowSpan.
-// Lane L converts the span's elements [L C, L C + C) (C odd, so the lanes'
+// (frame, row) and a pass of grid columns whose input span fits kRowSpan;
+// the span's largest finite exponent sets its unit (fixsum.cuh).  Lane L
+// converts the span's elements [L C, L C + C) (C odd, so the lanes'
 // shared-memory words fall in distinct banks) into running sums, an
 // exclusive warp scan of the lane totals gives each chunk's offset, and
 // lane L then takes grid columns M + L, M + L + 32, ...: a box sum is the
@@ -185,12 +174,18 @@ __global__ void __launch_bounds__(kBoxWarps * 32) k_box_rows(BoxArgs a) {
         const int img = lam >= rows, i = a.r0 + lam - img * rows;
         const double* __restrict__ v = (img ? a.f2 : a.f1) + (size_t)i * a.ny;
         BoxSum* __restrict__ o = (img ? a.rt2 : a.rt1) + (size_t)i * a.gj;
-        const int ee = max((int)a.emax[img], 1);
+        int* __restrict__ oe = (img ? a.re2 : a.re1) + (size_t)i * a.gj;
         const int M = pass * P, Mend = min(M + P, a.gj);
         const int base = box_start(a.yo + M * a.gs, a.ny, a.nsize);
         const int span = box_start(a.yo + (Mend - 1) * a.gs, a.ny, a.nsize) + a.n - base;  // <= kRowSpan
         const int C = max(3, ((span + 31) >> 5) | 1);  // odd, >= 3: the division below is exact
         const int e0 = min(lane * C, span), e1 = min(e0 + C, span);
+        unsigned em = 0u;
+        for (int e = e0; e < e1; ++e) {
+            const unsigned x = ((unsigned)__double2hiint(v[base + e]) >> 20) & 0x7ffu;
+            em = (x != 0x7ffu && x > em) ? x : em;
+        }
+        const int ee = max((int)__reduce_max_sync(0xffffffffu, em), 1);
         unsigned acc[4] = {0u, 0u, 0u, 0u}, cnt = 0u;
         for (int e = e0; e < e1; e += 4) {
             double x[4];
@@ -248,7 +243,9 @@ __global__ void __launch_bounds__(kBoxWarps * 32) k_box_rows(BoxArgs a) {
                 hc -= lc;
             }
             o[m] = BoxSum{(unsigned long long)hiw[0] | ((unsigned long long)hiw[1] << 32),
-                          (unsigned long long)hiw[2] | ((unsigned long long)hiw[3] << 32), cnt_wide(hc), 0ull};
+                          (unsigned long long)hiw[2] | ((unsigned long long)hiw[3] << 32), cnt_wide(hc),
+                          (unsigned long long)ee};
+            oe[m] = ee;
         }
         __syncwarp();  // the next pass overwrites the stage
     }
@@ -256,20 +253,26 @@ __global__ void __launch_bounds__(kBoxWarps * 32) k_box_rows(BoxArgs a) {
 
 // Box sums B[q][m] = sum_{ii<n} RT[t_q + ii][m] at the grid's box rows
 // t_q = box_start(xo + q gs), exact.  A thread takes one line (frame, grid
-// column) and a run of run_q grid rows of [q0, q1); consecutive threads
-// take consecutive columns, so loads and stores are coalesced.
+// column) and a run of kColRun grid rows starting at a multiple of kColRun;
+// the run's unit is the largest of the row sums' units it reads.
+// Consecutive threads take consecutive columns, so loads and stores are
+// coalesced.
 __global__ void __launch_bounds__(128) k_box_cols(BoxArgs a) {
     const int lines = 2 * a.gj;
-    const int R = a.run_q, runs = (a.q1 - a.q0 + R - 1) / R;
+    const int runs = (a.q1 - a.q0 + kColRun - 1) / kColRun;
     const long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
     if (idx >= (long)lines * runs) return;
     const int run = (int)(idx / lines), lam = (int)(idx - (long)run * lines);
     const int img = lam >= a.gj, m = lam - img * a.gj;
     const BoxSum* __restrict__ v = (img ? a.rt2 : a.rt1) + m;  // row r at v[r * gj]
+    const int* __restrict__ ve = (img ? a.re2 : a.re1) + m;
     BoxSum* __restrict__ o = (img ? a.b2 : a.b1) + m;
     const size_t gj = (size_t)a.gj;
-    const int q0 = a.q0 + run * R, q1 = min(q0 + R, a.q1);
+    const int q0 = a.q0 + run * kColRun, q1 = min(q0 + kColRun, a.q1);
     int t = box_start(a.xo + q0 * a.gs, a.nx, a.nsize);
+    const int tend = box_start(a.xo + (q1 - 1) * a.gs, a.nx, a.nsize) + a.n;
+    int eb = 1;
+    for (int r = t; r < tend; ++r) eb = max(eb, __ldg(ve + r * gj));
     unsigned long long lo[4] = {0ull, 0ull, 0ull, 0ull}, hi[4] = {0ull, 0ull, 0ull, 0ull}, cnt = 0ull;
     int d = 0;
     for (; d + 8 <= a.n; d += 8) {
@@ -278,12 +281,14 @@ __global__ void __launch_bounds__(128) k_box_cols(BoxArgs a) {
         for (int u = 0; u < 8; ++u) r[u] = v[(t + d + u) * gj];
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
+            sar128(r[u].lo, r[u].hi, eb - (int)r[u].e);
             add128(lo[u & 3], hi[u & 3], r[u].lo, r[u].hi);
             cnt += r[u].cnt;
         }
     }
     for (; d < a.n; ++d) {
-        const BoxSum r = v[(t + d) * gj];
+        BoxSum r = v[(t + d) * gj];
+        sar128(r.lo, r.hi, eb - (int)r.e);
         add128(lo[0], hi[0], r.lo, r.hi);
         cnt += r.cnt;
     }
@@ -291,12 +296,14 @@ __global__ void __launch_bounds__(128) k_box_cols(BoxArgs a) {
     add128(lo[2], hi[2], lo[3], hi[3]);
     add128(lo[0], hi[0], lo[2], hi[2]);
     for (int q = q0;;) {
-        o[q * gj] = BoxSum{lo[0], hi[0], cnt, 0ull};
+        o[q * gj] = BoxSum{lo[0], hi[0], cnt, (unsigned long long)eb};
         if (++q >= q1) break;
         const int tn = box_start(a.xo + q * a.gs, a.nx, a.nsize);
 #pragma unroll 4
         for (int r = t; r < tn; ++r) {
-            const BoxSum in = v[(r + a.n) * gj], out = v[r * gj];
+            BoxSum in = v[(r + a.n) * gj], out = v[r * gj];
+            sar128(in.lo, in.hi, eb - (int)in.e);
+            sar128(out.lo, out.hi, eb - (int)out.e);
             add128(lo[0], hi[0], in.lo, in.hi);
             sub128(lo[0], hi[0], out.lo, out.hi);
             cnt += in.cnt - out.cnt;

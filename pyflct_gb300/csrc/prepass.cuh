@@ -19,7 +19,6 @@ struct ClassifyArgs {
     double *vx, *vy, *vm;
     float2* grid;             // skip-grid (vx, vy) for the interpolation, or null
     unsigned* status;
-    unsigned* emax;           // [2]: largest biased exponent of the finite values per frame (atomicMax)
     int r0, r1;               // rows to classify (the work list gets their windows)
 };
 
@@ -27,6 +26,9 @@ struct ClassifyArgs {
 // warp converts into shared memory per pass.
 constexpr int kBoxWarps = 4;
 constexpr int kRowSpan = 544;
+// Column pass: grid rows per thread, runs start at multiples of it (the
+// units of a run's box sums depend on the rows it reads)
+constexpr int kColRun = 4;
 
 // Local-mean box sums for the boxes the grid needs, exact (fixsum.cuh).
 // Grid point (q, m) is pixel (xo + q gs, yo + m gs) (gs = 1, xo = yo = 0
@@ -36,10 +38,9 @@ struct BoxArgs {
     const double* f2;
     int nx, ny, n, nsize;
     int gs, xo, yo, gi, gj;   // grid step, offsets and counts (slow, fast axis)
-    const unsigned* emax;     // [2] per frame, from k_classify
     int pass_r;               // row pass: grid columns per warp pass
-    int run_q;                // column pass: grid rows per thread
     BoxSum *rt1, *rt2;        // row sums [nx][gj]
+    int *re1, *re2;           // their exponents, compact [nx][gj]
     BoxSum *b1, *b2;          // box sums [gi][gj]
     int r0, r1;               // frame rows of the row pass
     int q0, q1;               // grid rows of the column pass

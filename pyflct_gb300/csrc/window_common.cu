@@ -9,13 +9,13 @@ __device__ __forceinline__ double ds(double a, double b) { return __dsub_rn(a, b
 
 __global__ void k_means(MeansArgs a) {
     const int nw = *a.nwork;
-    const int e1 = max((int)a.emax[0], 1), e2 = max((int)a.emax[1], 1);
     for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < nw; w += gridDim.x * blockDim.x) {
         const int pix = a.work[w];
         const int i = pix / a.ny, j = pix - (pix / a.ny) * a.ny;
         const size_t b = (size_t)((i - a.xo) / a.gs) * a.gj + (j - a.yo) / a.gs;
-        const float2 m1 = split_double_fast(dm(fx_to_double(a.bs1[b], e1), a.inv_n2));
-        const float2 m2 = split_double_fast(dm(fx_to_double(a.bs2[b], e2), a.inv_n2));
+        const BoxSum s1 = a.bs1[b], s2 = a.bs2[b];
+        const float2 m1 = split_double_fast(dm(fx_to_double(s1, (int)s1.e), a.inv_n2));
+        const float2 m2 = split_double_fast(dm(fx_to_double(s2, (int)s2.e), a.inv_n2));
         a.means[w] = make_float4(m1.x, m1.y, m2.x, m2.y);
     }
 }

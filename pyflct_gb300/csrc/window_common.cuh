@@ -52,7 +52,6 @@ struct MeansArgs {
     int gs, xo, yo, gj;   // grid step and offsets; box sums are [grid row][grid column]
     const BoxSum* bs1;    // exact box sums [gi][gj] (fixsum.cuh)
     const BoxSum* bs2;
-    const unsigned* emax; // [2]: the box sums' exponents
     double inv_n2;
     float4* means;
 };
