@@ -18,9 +18,10 @@
 // register FFTs along the other axis.  The correlation image is real, so the
 // inverse runs as one complex n x n/2 transform (even and odd output columns
 // as real and imaginary parts), half the work of a complex n x n one.  The
-// butterflies' complex adds use the packed FP32 pipe (fft_reg.cuh).  Each
-// sub-image is scaled by an exact power of two so FP32 never over- or
-// under-flows; scaling changes neither the argmax nor the fit.
+// butterflies' complex adds use the packed FP32 pipe (fft_reg.cuh).  A
+// sub-image whose maximum is far from 1 is scaled by an exact power of two
+// so FP32 never over- or under-flows; scaling changes neither the argmax
+// nor the fit.
 #pragma once
 #include "common.cuh"
 #include "fft_reg.cuh"
@@ -154,19 +155,26 @@ k_window_fp32(WinArgs a) {
                 mx1 = fmaxf(mx1, fabsf(x[ii].x));
                 mx2 = fmaxf(mx2, fabsf(x[ii].y));
             }
-            float2 cs;
+            unsigned b1, b2;
             if constexpr (kWarp) {
-                cs = make_float2(pow2_scale(__reduce_max_sync(tmask, __float_as_uint(mx1))),
-                                 pow2_scale(__reduce_max_sync(tmask, __float_as_uint(mx2))));
+                b1 = __reduce_max_sync(tmask, __float_as_uint(mx1));
+                b2 = __reduce_max_sync(tmask, __float_as_uint(mx2));
                 team_sync();  // the previous window's |c| reads are done
             } else {
                 atomicMax(&s_max[2 * team], __float_as_uint(mx1));
                 atomicMax(&s_max[2 * team + 1], __float_as_uint(mx2));
                 team_sync();
-                cs = make_float2(pow2_scale(s_max[2 * team]), pow2_scale(s_max[2 * team + 1]));
+                b1 = s_max[2 * team];
+                b2 = s_max[2 * team + 1];
             }
+            // maxima within 2^+-40 of 1 need no scaling: every value of the
+            // transforms then stays inside FP32's normal range
+            auto near1 = [](unsigned b) { return b == 0u || (b >> 23) - 87u <= 80u; };
+            if (!(near1(b1) && near1(b2))) {
+                const float2 cs = make_float2(pow2_scale(b1), pow2_scale(b2));
 #pragma unroll
-            for (int ii = 0; ii < N; ++ii) x[ii] = emul(x[ii], cs);
+                for (int ii = 0; ii < N; ++ii) x[ii] = emul(x[ii], cs);
+            }
         }
 
         // forward 2-D FFT: columns in registers, transpose, rows in registers
