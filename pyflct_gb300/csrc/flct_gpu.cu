@@ -754,8 +754,8 @@ flct_status enqueue_interp(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaSt
     ia.vm = j.vm;
     ia.i0 = i0;
     ia.i1 = i1;
-    const long tiles = (long)((i1 - i0 + 7) / 8) * ((j.ny + 31) / 32);
-    k_interp_grid<<<(int)std::min<long>(tiles, (long)ctx->nsm * 8), 256, 0, st>>>(ia);
+    const long tiles = (long)((i1 - i0 + kTileR - 1) / kTileR) * ((j.ny + kTileC - 1) / kTileC);
+    k_interp_grid<<<(int)std::max(1l, std::min<long>(tiles, (long)ctx->nsm * 8)), kInterpThreads, 0, st>>>(ia);
     ++*launches;
     CK(cudaGetLastError());
     return FLCT_OK;

@@ -449,17 +449,20 @@ __device__ __noinline__ float2 cdata_f(const float2* __restrict__ g, int gx, int
 // y stencils tabulated alongside); then each pixel contracts four V values
 // with its y weights.  xmiss flags travel with the values (bit 0: vx,
 // bit 1: vy).
-constexpr int kTileR = 8, kTileC = 32;
+constexpr int kTileRT = kInterpThreads / kTileC;  // thread rows; a thread takes tile rows ti + kTileRT k
 constexpr int kPatchR = kTileR + 4, kPatchC = kTileC + 4;  // cdata rows / columns at skip 1
 
-__global__ void __launch_bounds__(kTileR * kTileC) k_interp_grid(InterpArgs a) {
+__global__ void __launch_bounds__(kInterpThreads) k_interp_grid(InterpArgs a) {
     __shared__ float2 s_p[kPatchR * kPatchC];
     __shared__ unsigned char s_pb[kPatchR * kPatchC];
     __shared__ float2 s_v[kTileR * kPatchC];
     __shared__ unsigned char s_vb[kTileR * kPatchC];
     __shared__ float s_ry[kTileC][4];
-    __shared__ int s_jz[kTileC];       // izero along y, -1 out of range
+    __shared__ float s_rx[kTileR][4];
+    __shared__ int s_jz[kTileC];            // izero along y, -1 out of range
+    __shared__ int s_iz[kTileR];            // izero along x, -1 out of range (or past i1)
     __shared__ unsigned char s_gj[kTileC];  // grid column
+    __shared__ unsigned char s_gi[kTileR];  // grid row
     const int ntc = (a.ny + kTileC - 1) / kTileC;
     const int ntr = (a.i1 - a.i0 + kTileR - 1) / kTileR;
     const float inv = 1.0f / (float)a.skip;
@@ -473,16 +476,20 @@ __global__ void __launch_bounds__(kTileR * kTileC) k_interp_grid(InterpArgs a) {
         const bool any = dlo <= dhi && elo <= ehi;
         const int r0 = any ? min(dlo / a.skip, a.gx - 2) : 0, r1 = any ? min(dhi / a.skip, a.gx - 2) + 3 : -1;
         const int c0 = any ? min(elo / a.skip, a.gy - 2) : 0, c1 = any ? min(ehi / a.skip, a.gy - 2) + 3 : -1;
-        const int pw = c1 - c0 + 1, pn = (r1 - r0 + 1) * pw;
+        const int pw = c1 - c0 + 1, ph = r1 - r0 + 1;
         __syncthreads();  // the previous tile's tables are consumed
-        for (int e = threadIdx.x; e < pn; e += blockDim.x) {
-            const int ra = r0 + e / pw, cb = c0 + (e - (e / pw) * pw);
-            const float2 v = (ra >= 1 && ra <= a.gx && cb >= 1 && cb <= a.gy)
-                                 ? __ldg(a.grid + (size_t)(ra - 1) * a.gy + (cb - 1))
-                                 : cdata_f(a.grid, a.gx, a.gy, ra, cb);
-            s_p[e] = v;
-            s_pb[e] = (v.x == kXmissF ? 1 : 0) | (v.y == kXmissF ? 2 : 0);
-        }
+        // patch: row pr = t / 32 (+ 8 k), column pc = t % 32 (+ 32 k)
+        for (int pr = ti; pr < ph; pr += kTileRT)
+            for (int pc = tj; pc < pw; pc += kTileC) {
+                const int ra = r0 + pr, cb = c0 + pc;
+                const float2 v = (ra >= 1 && ra <= a.gx && cb >= 1 && cb <= a.gy)
+                                     ? __ldg(a.grid + (size_t)(ra - 1) * a.gy + (cb - 1))
+                                     : cdata_f(a.grid, a.gx, a.gy, ra, cb);
+                const int e = pr * kPatchC + pc;
+                s_p[e] = v;
+                s_pb[e] = (v.x == kXmissF ? 1 : 0) | (v.y == kXmissF ? 2 : 0);
+            }
+        // per-column and per-row stencil tables
         if (threadIdx.x < kTileC) {
             const int dj = j0 + threadIdx.x - a.yoff;
             const bool okj = dj >= 0 && dj <= jmax;
@@ -492,54 +499,71 @@ __global__ void __launch_bounds__(kTileR * kTileC) k_interp_grid(InterpArgs a) {
 #pragma unroll
             for (int q = 0; q < 4; ++q)
                 s_ry[threadIdx.x][q] = okj ? keys_f(fabsf((float)(dj - (jz + q - 1) * a.skip) * inv)) : 0.f;
+        } else if (threadIdx.x < kTileC + kTileR) {  // kTileC + kTileR <= kInterpThreads
+            const int r = threadIdx.x - kTileC;
+            const int di = i0 + r - a.xoff;
+            const bool oki = i0 + r < a.i1 && di >= 0 && di <= imax;
+            const int iz = oki ? min(di / a.skip, a.gx - 2) : -1;
+            s_iz[r] = iz;
+            s_gi[r] = (di % a.skip) == 0;
+#pragma unroll
+            for (int p = 0; p < 4; ++p)
+                s_rx[r][p] = oki ? keys_f(fabsf((float)(di - (iz + p - 1) * a.skip) * inv)) : 0.f;
         }
         __syncthreads();
-        for (int e = threadIdx.x; e < kTileR * pw; e += blockDim.x) {
-            const int r = e / pw, b = e - (e / pw) * pw;
-            const int di = i0 + r - a.xoff;
-            float2 v = make_float2(0.f, 0.f);
-            unsigned char bad = 3;
-            if (i0 + r < a.i1 && di >= 0 && di <= imax) {
-                const int iz = min(di / a.skip, a.gx - 2);
-                bad = 0;
+        // V[r][b] = sum_p rx[r][p] patch[iz_r - r0 + p][b]
+        for (int r = ti; r < kTileR; r += kTileRT)
+            for (int b = tj; b < pw; b += kTileC) {
+                const int iz = s_iz[r];
+                float2 v = make_float2(0.f, 0.f);
+                unsigned char bad = 3;
+                if (iz >= 0) {
+                    bad = 0;
 #pragma unroll
-                for (int p = 0; p < 4; ++p) {
-                    const float rx = keys_f(fabsf((float)(di - (iz + p - 1) * a.skip) * inv));
-                    const int pe = (iz - r0 + p) * pw + b;
-                    const float2 c = s_p[pe];
-                    bad |= s_pb[pe];
-                    v.x = fmaf(rx, c.x, v.x);
-                    v.y = fmaf(rx, c.y, v.y);
+                    for (int p = 0; p < 4; ++p) {
+                        const float rx = s_rx[r][p];
+                        const int pe = (iz - r0 + p) * kPatchC + b;
+                        const float2 c = s_p[pe];
+                        bad |= s_pb[pe];
+                        v.x = fmaf(rx, c.x, v.x);
+                        v.y = fmaf(rx, c.y, v.y);
+                    }
+                }
+                s_v[r * kPatchC + b] = v;
+                s_vb[r * kPatchC + b] = bad;
+            }
+        __syncthreads();
+        const int j = j0 + tj;
+        if (j >= a.ny) continue;
+        const int jz = s_jz[tj];
+        const bool gj = s_gj[tj];
+        float ry[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) ry[q] = s_ry[tj][q];
+#pragma unroll
+        for (int k4 = 0; k4 < kTileR / kTileRT; ++k4) {
+            const int r = ti + kTileRT * k4, i = i0 + r;
+            if (i >= a.i1) break;
+            if (gj && s_gi[r] && i - a.xoff >= 0) continue;  // grid points keep their computed value
+            float sx = 0.f, sy = 0.f;
+            unsigned bad = 3;
+            if (jz >= 0 && s_iz[r] >= 0) {
+                bad = 0;
+                const int vb = r * kPatchC + (jz - c0);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const float2 v = s_v[vb + q];
+                    bad |= s_vb[vb + q];
+                    sx = fmaf(ry[q], v.x, sx);
+                    sy = fmaf(ry[q], v.y, sy);
                 }
             }
-            s_v[r * kPatchC + b] = v;
-            s_vb[r * kPatchC + b] = bad;
+            const size_t k = (size_t)i * a.ny + j;
+            // xmiss reset: a missing vx clears the mask, a missing vy only vy
+            a.vx[k] = (bad & 1) ? 0. : f2d(sx);
+            a.vy[k] = (bad & 2) ? 0. : f2d(sy);
+            a.vm[k] = (bad & 1) ? 0. : 0.5;
         }
-        __syncthreads();
-        const int i = i0 + ti, j = j0 + tj;
-        if (i >= a.i1 || j >= a.ny) continue;
-        const int di = i - a.xoff;
-        if (s_gj[tj] && (di % a.skip) == 0) continue;  // grid points keep their computed value
-        const int jz = s_jz[tj];
-        float sx = 0.f, sy = 0.f;
-        unsigned bad = 3;
-        if (jz >= 0 && di >= 0 && di <= imax) {  // (V is not built when no tile row is in range)
-            bad = 0;
-            const int vb = ti * kPatchC + (jz - c0);
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const float ry = s_ry[tj][q];
-                const float2 v = s_v[vb + q];
-                bad |= s_vb[vb + q];
-                sx = fmaf(ry, v.x, sx);
-                sy = fmaf(ry, v.y, sy);
-            }
-        }
-        const size_t k = (size_t)i * a.ny + j;
-        // xmiss reset: a missing vx clears the mask, a missing vy only vy
-        a.vx[k] = (bad & 1) ? 0. : f2d(sx);
-        a.vy[k] = (bad & 2) ? 0. : f2d(sy);
-        a.vm[k] = (bad & 1) ? 0. : 0.5;
     }
 }
 

@@ -46,6 +46,9 @@ struct BoxArgs {
     int q0, q1;               // grid rows of the column pass
 };
 
+// Interpolation tiles: kTileR x kTileC pixels per block of kInterpThreads.
+constexpr int kTileR = 32, kTileC = 32, kInterpThreads = 256;
+
 // The velocity pipeline's skip-grid interpolation (FP32 arithmetic).
 struct InterpArgs {
     int nx, ny, skip, xoff, yoff;
