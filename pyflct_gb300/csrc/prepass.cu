@@ -180,13 +180,9 @@ __global__ void __launch_bounds__(kBoxWarps * 32) k_box_rows(BoxArgs a) {
         const int span = box_start(a.yo + (Mend - 1) * a.gs, a.ny, a.nsize) + a.n - base;  // <= kRowSpan
         const int C = max(3, ((span + 31) >> 5) | 1);  // odd, >= 3: the division below is exact
         const int e0 = min(lane * C, span), e1 = min(e0 + C, span);
+        // the chunk's doubles into words 0 and 1 of the stage, and the span's
+        // largest finite exponent (its unit)
         unsigned em = 0u;
-        for (int e = e0; e < e1; ++e) {
-            const unsigned x = ((unsigned)__double2hiint(v[base + e]) >> 20) & 0x7ffu;
-            em = (x != 0x7ffu && x > em) ? x : em;
-        }
-        const int ee = max((int)__reduce_max_sync(0xffffffffu, em), 1);
-        unsigned acc[4] = {0u, 0u, 0u, 0u}, cnt = 0u;
         for (int e = e0; e < e1; e += 4) {
             double x[4];
 #pragma unroll
@@ -194,12 +190,21 @@ __global__ void __launch_bounds__(kBoxWarps * 32) k_box_rows(BoxArgs a) {
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 if (e + u < e1) {
-                    fx_accum(x[u], ee, acc, cnt);
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) sw[k * SW + e + u] = acc[k];
-                    sw[4 * SW + e + u] = cnt;
+                    const unsigned hw = (unsigned)__double2hiint(x[u]), xe = (hw >> 20) & 0x7ffu;
+                    em = (xe != 0x7ffu && xe > em) ? xe : em;
+                    sw[e + u] = (unsigned)__double2loint(x[u]);
+                    sw[SW + e + u] = hw;
                 }
             }
+        }
+        const int ee = max((int)__reduce_max_sync(0xffffffffu, em), 1);
+        // running sums of the chunk, in place
+        unsigned acc[4] = {0u, 0u, 0u, 0u}, cnt = 0u;
+        for (int e = e0; e < e1; ++e) {
+            fx_accum(__hiloint2double((int)sw[SW + e], (int)sw[e]), ee, acc, cnt);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) sw[k * SW + e] = acc[k];
+            sw[4 * SW + e] = cnt;
         }
         // exclusive scan of the lane totals
         unsigned t[5] = {acc[0], acc[1], acc[2], acc[3], cnt};
