@@ -142,6 +142,11 @@ struct flct_ctx {
     cudaGraphExec_t hexec = nullptr;
     std::vector<unsigned char> hkey;
     int hlaunches = 0;
+    // device-buffer calls: the last call's key, and the graph of a call
+    // made twice in a row (replayed while the key repeats)
+    cudaGraphExec_t dexec = nullptr;
+    std::vector<unsigned char> dkey, dlast;
+    int dlaunches = 0;
 };
 
 namespace {
@@ -710,8 +715,7 @@ flct_status enqueue_fit(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaStrea
     fa.peaks = b.peaks;
     fa.n = j.n;
     fa.ny = j.ny;
-    fa.deltinv = 1. / j.p->deltat;  // flct.c:343
-    fa.deltas = j.p->deltas;
+    fa.vscale = (1. / j.p->deltat) * j.p->deltas;  // flct.c:343, 901-905
     fa.skip = j.d.skip > 0 ? j.d.skip : 1;
     fa.xoff = j.d.xoff;
     fa.yoff = j.d.yoff;
@@ -911,8 +915,7 @@ flct_status velocity_global(flct_ctx* ctx, const Job& j, cudaStream_t st) {
     fa.n = nx;
     fa.n1 = ny;
     fa.ny = 1;
-    fa.deltinv = 1. / p->deltat;
-    fa.deltas = p->deltas;
+    fa.vscale = (1. / p->deltat) * p->deltas;  // flct.c:343, 901-905
     fa.skip = 1;
     fa.vx = j.vx;
     fa.vy = j.vy;
@@ -1274,6 +1277,39 @@ flct_status rebuild_batch(flct_ctx* ctx, int npairs, const flct_pair* pairs, cud
     ctx->batch_launches = launches;
     ctx->batch_box = bp.groups.size() == 1 ? bp.groups[0].n : 0;
     ctx->batch_form = bp.groups[0].form;
+    return FLCT_OK;
+}
+
+// The device call's kernels after the tuning point (from_start: also the
+// prepass): stage events for flct_gpu_last_timing (recorded as graph nodes
+// when capturing), windows, fit, interpolation and the counters' copy to
+// page-locked memory.
+flct_status enqueue_device_tail(flct_ctx* ctx, const Job& j, const JobBufs& b, int form, int grid_div,
+                                cudaStream_t st, bool graph, int* launches, bool from_start = false) {
+    const unsigned evf = graph ? cudaEventRecordExternal : cudaEventRecordDefault;
+    flct_status s = FLCT_OK;
+    if (from_start) {
+        CK(cudaEventRecordWithFlags(ctx->ev[0], st, evf));
+        s = enqueue_prepass(ctx, j, b, st, launches);
+        if (s != FLCT_OK) return s;
+    }
+    WinArgs wa;
+    make_wargs(j, b, &wa);
+    CK(cudaEventRecordWithFlags(ctx->ev[1], st, evf));
+    s = launch_windows(ctx, form, j.we, j.n, wa, (unsigned*)(b.ctr + 4), st, grid_div);
+    if (s != FLCT_OK) return s;
+    ++*launches;
+    CK(cudaEventRecordWithFlags(ctx->ev[2], st, evf));
+    s = enqueue_fit(ctx, j, b, st, launches);
+    if (s != FLCT_OK) return s;
+    CK(cudaEventRecordWithFlags(ctx->ev[7], st, evf));
+    if (j.interp) {
+        s = enqueue_interp(ctx, j, b, st, launches);
+        if (s != FLCT_OK) return s;
+    }
+    // work count and status to page-locked memory, complete with ev[3]
+    CK(cudaMemcpyAsync(ctx->hctr, b.ctr, 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaEventRecordWithFlags(ctx->ev[3], st, evf));
     return FLCT_OK;
 }
 
@@ -1656,6 +1692,7 @@ void flct_gpu_destroy(flct_ctx* ctx) {
     if (ctx->bdone) cudaEventSynchronize(ctx->bdone);
     if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
     if (ctx->hexec) cudaGraphExecDestroy(ctx->hexec);
+    if (ctx->dexec) cudaGraphExecDestroy(ctx->dexec);
     for (auto* b : ctx->all())
         if (b->p) cudaFree(b->p);
     for (auto& e : ctx->ev)
@@ -1746,16 +1783,16 @@ flct_status flct_gpu_velocity_device(flct_ctx* ctx, const flct_params* p, const 
     b.grid = (float2*)ctx->b_grid.p;
     unsigned* d_status = (unsigned*)(b.ctr + 4);
 
-    int launches = 0;
     ctx->batch_pending = 0;
-    CK(cudaEventRecord(ctx->ev[0], st));
-    s = enqueue_prepass(ctx, j, b, st, &launches);
-    if (s != FLCT_OK) return s;
-    WinArgs wa;
-    make_wargs(j, b, &wa);
+    int launches = 0, grid_div = 1;
     // first FLCT_FORM_AUTO call for this box size: time the candidates on
-    // this work list (not possible inside a stream capture)
+    // this work list, eagerly (not possible inside a stream capture)
     if (p->form == FLCT_FORM_AUTO && !ctx->tune.count(n) && !capturing(st)) {
+        CK(cudaEventRecord(ctx->ev[0], st));
+        s = enqueue_prepass(ctx, j, b, st, &launches);
+        if (s != FLCT_OK) return s;
+        WinArgs wa;
+        make_wargs(j, b, &wa);
         for (int f : {FLCT_FORM_FP32, FLCT_FORM_TC_FP16}) {
             if (f != FLCT_FORM_FP32 && n != 32) continue;
             s = prime_form(ctx, f, n);
@@ -1763,24 +1800,67 @@ flct_status flct_gpu_velocity_device(flct_ctx* ctx, const flct_params* p, const 
         }
         s = tune_windows(ctx, j.we, n, wa, d_status, (const int*)b.ctr, st);
         if (s != FLCT_OK) return s;
-    }
-    int grid_div = 1;
-    resolved_config(ctx, p->form, n, &form, &grid_div);
-    CK(cudaEventRecord(ctx->ev[1], st));
-    s = launch_windows(ctx, form, j.we, n, wa, d_status, st, grid_div);
-    if (s != FLCT_OK) return s;
-    ++launches;
-    CK(cudaEventRecord(ctx->ev[2], st));
-    s = enqueue_fit(ctx, j, b, st, &launches);
-    if (s != FLCT_OK) return s;
-    CK(cudaEventRecord(ctx->ev[7], st));
-    if (j.interp) {
-        s = enqueue_interp(ctx, j, b, st, &launches);
+        resolved_config(ctx, p->form, n, &form, &grid_div);
+        s = enqueue_device_tail(ctx, j, b, form, grid_div, st, false, &launches);
         if (s != FLCT_OK) return s;
+    } else {
+        resolved_config(ctx, p->form, n, &form, &grid_div);
+        s = prime_form(ctx, form, n);
+        if (s != FLCT_OK) return s;
+        // a call repeated with the same parameters and buffers is captured
+        // once as a CUDA graph and replayed (one launch instead of ~12)
+        std::vector<unsigned char> key;
+        if (!capturing(st)) {
+            auto put = [&key](const void* v, size_t nb) {
+                const unsigned char* c = (const unsigned char*)v;
+                key.insert(key.end(), c, c + nb);
+            };
+            const int ints[] = {nx, ny, form, grid_div, p->thresh_abs, p->skip, p->poffset, p->qoffset,
+                                p->interpolate, p->filter, p->hires};
+            const double dbl[] = {p->deltat, p->deltas, p->sigma, p->thresh, p->kr};
+            const void* ptrs[] = {d_f1, d_f2, d_vx, d_vy, d_vm, ctx->b_s1.p, ctx->b_s2.p, ctx->b_work.p,
+                                  ctx->b_ctr.p, ctx->b_r1.p, ctx->b_r2.p, ctx->b_re1.p, ctx->b_re2.p, ctx->b_b1.p,
+                                  ctx->b_b2.p, ctx->b_means.p, ctx->b_peaks.p, ctx->b_peaks_h.p, ctx->b_grid.p,
+                                  ctx->b_tc.p, ctx->hctr};
+            put(ints, sizeof(ints));
+            put(dbl, sizeof(dbl));
+            put(ptrs, sizeof(ptrs));
+        }
+        if (!key.empty() && ctx->dexec && key == ctx->dkey) {
+            CK(cudaGraphLaunch(ctx->dexec, st));
+            launches = ctx->dlaunches;
+        } else if (!key.empty() && key == ctx->dlast) {
+            if (ctx->dexec) {
+                cudaGraphExecDestroy(ctx->dexec);
+                ctx->dexec = nullptr;
+            }
+            ctx->dkey.clear();
+            cudaStream_t cs = ctx->stream;
+            CK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed));
+            s = enqueue_device_tail(ctx, j, b, form, grid_div, cs, true, &launches, true);
+            cudaGraph_t g = nullptr;
+            const cudaError_t ec = cudaStreamEndCapture(cs, &g);
+            if (s != FLCT_OK || ec != cudaSuccess) {
+                if (g) cudaGraphDestroy(g);
+                cudaGetLastError();
+                if (s != FLCT_OK) return s;
+                return fail(ctx, FLCT_ERR_CUDA, "capturing the velocity call failed: %s", cudaGetErrorString(ec));
+            }
+            const cudaError_t ei = cudaGraphInstantiate(&ctx->dexec, g, 0);
+            cudaGraphDestroy(g);
+            if (ei != cudaSuccess) {
+                ctx->dexec = nullptr;
+                return fail(ctx, FLCT_ERR_CUDA, "instantiating the velocity graph failed: %s", cudaGetErrorString(ei));
+            }
+            ctx->dkey = key;
+            ctx->dlaunches = launches;
+            CK(cudaGraphLaunch(ctx->dexec, st));
+        } else {
+            ctx->dlast = key;
+            s = enqueue_device_tail(ctx, j, b, form, grid_div, st, false, &launches, true);
+            if (s != FLCT_OK) return s;
+        }
     }
-    // work count and status to page-locked memory, complete with ev[3]
-    CK(cudaMemcpyAsync(ctx->hctr, b.ctr, 8, cudaMemcpyDeviceToHost, st));
-    CK(cudaEventRecord(ctx->ev[3], st));
     ctx->timing = flct_timing{};
     ctx->timing.launches = launches;
     ctx->timing.box = n;

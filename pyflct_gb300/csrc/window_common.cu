@@ -30,19 +30,22 @@ __device__ __forceinline__ void store_shift(const FitArgs& a, int w, double shx,
     if (a.vx) {
         const int pix = a.work[w];
         const int i = pix / a.ny, j = pix - (pix / a.ny) * a.ny;
-        // transposed storage: vx from the fast-axis shift (flct.c:901-905)
-        double vxx = dm(dm(shy, a.deltinv), a.deltas);
-        double vyy = dm(dm(shx, a.deltinv), a.deltas);
+        // transposed storage: vx from the fast-axis shift (flct.c:901-905),
+        // scaled by deltas / deltat in one product
+        double vxx = dm(shy, a.vscale);
+        double vyy = dm(shx, a.vscale);
         double vmm = 1.;
         if (a.grid) {
             const int ic = (i - a.xoff) / a.skip, jc = (j - a.yoff) / a.skip;
-            a.grid[(size_t)ic * a.jcnt + jc] = make_float2((float)vxx, (float)vyy);
+            a.grid[(size_t)ic * a.jcnt + jc] = make_float2(split_double_fast(vxx).x, split_double_fast(vyy).x);
         }
-        if (vxx == kXmiss) {
+        // xmiss tests on the bit patterns (xmiss is a normal number)
+        const long long xm = __double_as_longlong(kXmiss);
+        if (__double_as_longlong(vxx) == xm) {
             vmm = 0.;
             vxx = 0.;
         }
-        if (vyy == kXmiss) vyy = 0.;
+        if (__double_as_longlong(vyy) == xm) vyy = 0.;
         a.vx[pix] = vxx;
         a.vy[pix] = vyy;
         a.vm[pix] = vmm;
@@ -51,7 +54,8 @@ __device__ __forceinline__ void store_shift(const FitArgs& a, int w, double shx,
 
 // The 3x3 Taylor fit (flct.c:1536-1553, 1607-1630) of v[3p+q] = f at
 // (peak-1+p, peak-1+q), in the reference's operation order without FMA
-// contraction, so that identical inputs round exactly like the reference's.
+// contraction, except that both shifts multiply by one reciprocal of the
+// determinant (one FP64 division instead of two).
 __device__ __forceinline__ void fit3x3(const double* v, double* sx, double* sy) {
     const double fx = dm(0.5, ds(v[7], v[1]));
     const double fy = dm(0.5, ds(v[5], v[3]));
@@ -59,8 +63,9 @@ __device__ __forceinline__ void fit3x3(const double* v, double* sx, double* sy) 
     const double fyy = ds(da(v[5], v[3]), dm(2., v[4]));
     const double fxy = dm(0.25, ds(ds(da(v[8], v[0]), v[6]), v[2]));
     const double den = ds(dm(fxy, fxy), dm(fxx, fyy));
-    *sx = ds(dm(fyy, fx), dm(fy, fxy)) / den;
-    *sy = ds(dm(fxx, fy), dm(fx, fxy)) / den;
+    const double inv = 1.0 / den;  // one division for both shifts
+    *sx = dm(ds(dm(fyy, fx), dm(fy, fxy)), inv);
+    *sy = dm(ds(dm(fxx, fy), dm(fx, fxy)), inv);
 }
 
 __global__ void k_fit(FitArgs a) {
@@ -76,7 +81,7 @@ __global__ void k_fit(FitArgs a) {
             for (int k = 0; k < 9; ++k) v[k] = f2d(r.v[k]);
             fit3x3(v, &sx, &sy);
         }
-        store_shift(a, w, ds(da((double)I, sx), (double)half), ds(da((double)J, sy), (double)half1));
+        store_shift(a, w, da((double)(I - half), sx), da((double)(J - half1), sy));
     }
 }
 

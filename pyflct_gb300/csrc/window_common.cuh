@@ -63,7 +63,7 @@ struct FitArgs {
     int n;                 // box side (square boxes)
     int n1;                // fast-axis side when the box is not square (sigma 0), else 0
     int ny;
-    double deltinv, deltas;
+    double vscale;         // deltas / deltat (flct.c:343, 901-905)
     int skip, xoff, yoff, jcnt;
     double *vx, *vy, *vm;  // outputs [nx*ny] or null (window-only calls)
     float2* grid;          // skip-grid (vx, vy) for the interpolation, or null

@@ -228,6 +228,50 @@ def test_repeat_calls_are_identical():
         assert np.array_equal(x, y)
 
 
+def test_device_calls_replayed_as_graph():
+    """Device-buffer calls repeated with the same parameters and buffers are
+    replayed from a captured CUDA graph (the second call captures it): every
+    call gives the first call's output, the stage times are filled in, and a
+    call with other buffers or parameters is not served from the graph."""
+    import ctypes as C
+    import torch
+    from pyflct_gb300 import _lib, synth
+    from pyflct_gb300.flct import make_params
+    rng = np.random.default_rng(77)
+    f1 = synth.kfield((160, 144), rng)
+    f2 = synth.fourier_shift(f1, 0.7, -0.4)
+    dev = torch.device("cuda", 0)
+    d1, d2 = torch.from_numpy(f1).to(dev), torch.from_numpy(f2).to(dev)
+    ctx = _lib.Context(0)
+
+    def call(p, out):
+        ctx.check(ctx.lib.flct_gpu_velocity_device(ctx.h, C.byref(p), C.c_void_p(d1.data_ptr()),
+                                                   C.c_void_p(d2.data_ptr()), 160, 144,
+                                                   *[C.c_void_p(o.data_ptr()) for o in out], None))
+        t = ctx.timing()
+        return [o.cpu().numpy().copy() for o in out], t
+
+    p = make_params(1.0, 1.0, 5.0, skip="3i", form="fp32")
+    out = [torch.full((160, 144), -5.0, dtype=torch.float64, device=dev) for _ in range(3)]
+    first, t0 = call(p, out)
+    for _ in range(3):
+        for o in out:
+            o.fill_(-5.0)
+        got, t = call(p, out)
+        for a, b in zip(got, first):
+            assert np.array_equal(a, b)
+        assert t.windows == t0.windows and t.ms_window > 0 and t.ms_total >= t.ms_window
+    other = [torch.full((160, 144), -5.0, dtype=torch.float64, device=dev) for _ in range(3)]
+    got, _ = call(p, other)
+    for a, b in zip(got, first):
+        assert np.array_equal(a, b)
+    q = make_params(1.0, 1.0, 5.0, skip="3", form="fp32")  # no interpolation: other output
+    got, _ = call(q, out)
+    ref = po.velocity(f1, f2, sigma=5, skip=3)
+    compare(f1, f2, got, ref, dict(sigma=5, skip=3))
+    ctx.close()
+
+
 @pytest.mark.parametrize("shape,extra", [
     ((50, 40), {}), ((128, 96), {"kr": 0.4}), ((201, 101), {}), ((97, 130), {"hires": True}),
     ((256, 256), {"kr": 0.5, "hires": True}), ((33, 35), {"thresh": 0.5}),
