@@ -152,3 +152,14 @@ def config4_pairs(rng=None, count=64):
         out.append((f1, fourier_shift(f1, vx, vy), dict(deltat=1.0, deltas=1.0, sigma=sigma),
                     (vx, vy)))
     return out
+
+def config5(rng=None, n=4096):
+    """4096^2 float32 k^-2 field; image2 = image1 resampled along a k^-3
+    random displacement field of RMS 0.3 px (periodic bicubic spline, a
+    stand-in for the spectral warp, whose O(N^2) per pixel cost is out of
+    reach at this size); sigma 15 (box 64)."""
+    rng = rng or np.random.default_rng(20265)
+    f1 = kfield((n, n), rng).astype(np.float32).astype(np.float64)
+    dfast, dslow = smooth_shift((n, n), rng, rms=0.3, slope=3.0)
+    f2 = spline_warp(f1, dfast, dslow).astype(np.float32).astype(np.float64)
+    return f1, f2, dict(deltat=1.0, deltas=1.0, sigma=15.0), (dfast, dslow)
