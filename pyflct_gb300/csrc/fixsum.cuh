@@ -136,7 +136,13 @@ __device__ __forceinline__ double fx_to_double(const BoxSum& s, int ee) {
             ++p;
         }
     }
-    const double d = scalbn((double)mant, p - 52 + ee - 1137);
+    // mant * 2^(p - 52) units of 2^(ee - 1137): biased exponent p + ee - 114
+    const int E = p + ee - 114;
+    double d;
+    if (E >= 1 && E <= 2046)
+        d = __longlong_as_double((long long)(((unsigned long long)E << 52) | (mant & 0xfffffffffffffull)));
+    else
+        d = scalbn((double)mant, p - 52 + ee - 1137);  // subnormal or beyond the double range
     return neg ? -d : d;
 }
 
