@@ -37,9 +37,12 @@ __device__ __forceinline__ void sub128(unsigned long long& lo, unsigned long lon
     asm("sub.cc.u64 %0, %0, %2;\n\tsubc.u64 %1, %1, %3;" : "+l"(lo), "+l"(hi) : "l"(bl), "l"(bh));
 }
 
-// Arithmetic right shift of a two's-complement 128-bit value, 0 <= d < 128.
+// Arithmetic right shift of a two's-complement 128-bit value by d >= 0
+// (d >= 127 leaves the sign).
 __device__ __forceinline__ void sar128(unsigned long long& lo, unsigned long long& hi, int d) {
-    if (d >= 64) {
+    if (d >= 127) {
+        lo = hi = (unsigned long long)((long long)hi >> 63);
+    } else if (d >= 64) {
         lo = (unsigned long long)((long long)hi >> (d - 64));
         hi = (unsigned long long)((long long)hi >> 63);
     } else if (d > 0) {
