@@ -82,10 +82,16 @@ __global__ void __launch_bounds__(256) k_classify(ClassifyArgs a) {
     const bool thr_pos = (long long)tb > 0ll && tb <= 0x7ff0000000000000ull;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int tpr = (a.ny + 255) >> 8;  // tiles per row
-    const long ntile = (long)(a.r1 - a.r0) * tpr;
-    for (long t = blockIdx.x; t < ntile; t += gridDim.x) {
-        const int i = a.r0 + (int)(t / tpr);
-        const int j = (int)(t - (long)(i - a.r0) * tpr) * 256 + threadIdx.x;
+    const int ntile = (a.r1 - a.r0) * tpr;  // < 2^31: sides are limited to 2^31 pixels
+    // the grid test's column remainder: (j - yoff) mod skip = tile base + this thread's offset
+    const int sk = a.skip > 0 ? a.skip : 1;
+    const int tmod = (int)threadIdx.x % sk;
+    for (int t = blockIdx.x; t < ntile; t += gridDim.x) {
+        const int ti = t / tpr;
+        const int i = a.r0 + ti;
+        const int j0 = (t - ti * tpr) * 256, j = j0 + threadIdx.x;
+        int rj = ((j0 - a.yoff) % sk + sk) % sk + tmod;  // uniform part + per-thread part
+        rj = rj >= sk ? rj - sk : rj;
         const bool act = j < a.ny;
         const size_t k = (size_t)i * a.ny + j;
         bool comp = false, grid = false;
@@ -107,7 +113,9 @@ __global__ void __launch_bounds__(256) k_classify(ClassifyArgs a) {
                 else if (E == 0x7ffu) below = sb2 < tb;                         // inf / NaN
                 else below = __dmul_rn(0.5, __longlong_as_double((long long)sb2)) < thr;
             }
-            grid = (a.skip > 0) ? (!((i - a.xoff) % a.skip) && !((j - a.yoff) % a.skip)) : true;
+            // the reference's C test !((i-xoff)%skip) && !((j-yoff)%skip): an
+            // offset pixel (j < yoff) has a nonzero C remainder
+            grid = (a.skip > 0) ? (!((i - a.xoff) % a.skip) && j >= a.yoff && rj == 0) : true;
             comp = !below && grid;
         }
         const unsigned m = __ballot_sync(0xffffffffu, comp);
