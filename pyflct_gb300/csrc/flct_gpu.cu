@@ -128,16 +128,21 @@ struct flct_ctx {
     int host_bands_max = 4;        // FLCT_HOST_BANDS (0 or 1: one band)
     int host_bands = 0;            // bands of the pending host call (0: not banded)
     cudaStream_t cstream[2] = {};  // copy-in, copy-out
-    // the bands' prepass (highest priority), then per-band compute streams
-    // in falling priority: a band's windows fill the SMs the band before
-    // leaves idle at its tail, and a band's small kernels go ahead of the
-    // next band's windows
-    cudaStream_t prestream = nullptr;
+    // the prepass (highest priority) on three streams, classification, row
+    // sums and column sums, so that they overlap each other; then per-band
+    // compute streams in falling priority: a band's windows fill the SMs the
+    // band before leaves idle at its tail, and a band's small kernels go
+    // ahead of the next band's windows
+    static constexpr int kPre = 3;
+    cudaStream_t prestream[kPre] = {};
     cudaStream_t bandstream[kMaxBands] = {};
     // band b copied in: [b]; finished rows ready for copy-out: [kMaxBands + b];
-    // fitted: [2 kMaxBands + b]; prepass (means inputs) ready: [3 kMaxBands + b];
-    // start (fork): [4 kMaxBands]; copy-out done (join): [4 kMaxBands + 1]
-    cudaEvent_t hev[4 * kMaxBands + 2] = {};
+    // fitted: [2 kMaxBands + b]; box sums ready: [3 kMaxBands + b];
+    // classified: [4 kMaxBands + b]; row sums ready: [5 kMaxBands + b];
+    // start (fork): [6 kMaxBands]; join: [6 kMaxBands + 1]
+    cudaEvent_t hev[6 * kMaxBands + 2] = {};
+    // the device call's classification fork and join
+    cudaEvent_t pev[2] = {};
     // the last banded call with page-locked buffers, captured as a graph
     cudaGraphExec_t hexec = nullptr;
     std::vector<unsigned char> hkey;
@@ -558,7 +563,7 @@ JobSizes job_sizes(const Job& j) {
 // float split, the work list (b.work / b.ctr: the windows of those rows)
 // and the final values of pixels without a window (flct.c:684-755).
 flct_status enqueue_classify(flct_ctx* ctx, const Job& j, const JobBufs& b, int r0, int r1, const double* d_thr,
-                             cudaStream_t st, int* launches) {
+                             cudaStream_t st, int* launches, int blocks_per_sm = 8) {
     ClassifyArgs ca{};
     ca.f1 = j.f1;
     ca.f2 = j.f2;
@@ -583,7 +588,7 @@ flct_status enqueue_classify(flct_ctx* ctx, const Job& j, const JobBufs& b, int 
     ca.r0 = r0;
     ca.r1 = r1;
     const long tiles = (long)(r1 - r0) * ((j.ny + 255) / 256);
-    k_classify<<<(int)std::max(1l, std::min<long>(tiles, (long)ctx->nsm * 8)), 256, 0, st>>>(ca);
+    k_classify<<<(int)std::max(1l, std::min<long>(tiles, (long)ctx->nsm * blocks_per_sm)), 256, 0, st>>>(ca);
     ++*launches;
     CK(cudaGetLastError());
     return FLCT_OK;
@@ -672,8 +677,11 @@ flct_status enqueue_means(flct_ctx* ctx, const Job& j, const JobBufs& b, long ma
 }
 
 // The whole-frame prepass: counters, relative threshold (flct.c:594-629),
-// classification, box sums and means.
-flct_status enqueue_prepass(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaStream_t st, int* launches) {
+// classification, box sums and means.  With a side stream the
+// classification runs there, beside the box sums (both only read the
+// frames), on half the blocks so that the two kernels share the SMs.
+flct_status enqueue_prepass(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaStream_t st, int* launches,
+                            cudaStream_t side = nullptr) {
     const size_t npx = (size_t)j.nx * j.ny;
     unsigned long long* d_absmax = (unsigned long long*)(b.ctr + 8);
     double* d_thr = (double*)(b.ctr + 24);
@@ -683,9 +691,23 @@ flct_status enqueue_prepass(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaS
         k_thresh_final<<<1, 1, 0, st>>>(j.f1, j.f2, d_absmax, j.p->thresh, d_thr);
         *launches += 2;
     }
-    flct_status s = enqueue_classify(ctx, j, b, 0, j.nx, j.d.rel_thresh ? d_thr : nullptr, st, launches);
-    if (s == FLCT_OK) s = enqueue_box_rows(ctx, j, b, 0, j.nx, st, launches);
-    if (s == FLCT_OK) s = enqueue_box_cols(ctx, j, b, 0, j.gi, st, launches);
+    const double* thr = j.d.rel_thresh ? d_thr : nullptr;
+    flct_status s = FLCT_OK;
+    if (side) {
+        CK(cudaEventRecord(ctx->pev[0], st));
+        CK(cudaStreamWaitEvent(side, ctx->pev[0], 0));
+        // the box sums go first: their two passes are the longer chain
+        s = enqueue_box_rows(ctx, j, b, 0, j.nx, st, launches);
+        if (s == FLCT_OK) s = enqueue_classify(ctx, j, b, 0, j.nx, thr, side, launches, 4);
+        if (s != FLCT_OK) return s;
+        CK(cudaEventRecord(ctx->pev[1], side));
+        s = enqueue_box_cols(ctx, j, b, 0, j.gi, st, launches);
+        CK(cudaStreamWaitEvent(st, ctx->pev[1], 0));
+    } else {
+        s = enqueue_classify(ctx, j, b, 0, j.nx, thr, st, launches);
+        if (s == FLCT_OK) s = enqueue_box_rows(ctx, j, b, 0, j.nx, st, launches);
+        if (s == FLCT_OK) s = enqueue_box_cols(ctx, j, b, 0, j.gi, st, launches);
+    }
     if (s == FLCT_OK) s = enqueue_means(ctx, j, b, (long)npx, st, launches);
     return s;
 }
@@ -1290,7 +1312,7 @@ flct_status enqueue_device_tail(flct_ctx* ctx, const Job& j, const JobBufs& b, i
     flct_status s = FLCT_OK;
     if (from_start) {
         CK(cudaEventRecordWithFlags(ctx->ev[0], st, evf));
-        s = enqueue_prepass(ctx, j, b, st, launches);
+        s = enqueue_prepass(ctx, j, b, st, launches, ctx->prestream[0]);
         if (s != FLCT_OK) return s;
     }
     WinArgs wa;
@@ -1412,14 +1434,15 @@ flct_status enqueue_banded(flct_ctx* ctx, const Job& j, const Bands& bd, int for
         bb[b].peaks_h = z.peaks_h ? base.peaks_h + off : nullptr;
         bb[b].ctr = (unsigned char*)ctx->b_ctr.p + 64 * b;
     }
-    cudaStream_t st = ctx->stream, cin = ctx->cstream[0], cout = ctx->cstream[1], pre = ctx->prestream;
+    cudaStream_t st = ctx->stream, cin = ctx->cstream[0], cout = ctx->cstream[1];
+    // prepass streams: classification, row sums, column sums
+    cudaStream_t pc = ctx->prestream[0], pr = ctx->prestream[1], pb = ctx->prestream[2];
     cudaStream_t* bs = ctx->bandstream;
-    constexpr int kB = flct_ctx::kMaxBands, kC = kB, kF = 2 * kB, kP = 3 * kB, kFork = 4 * kB, kJoin = 4 * kB + 1;
+    constexpr int kB = flct_ctx::kMaxBands, kC = kB, kF = 2 * kB, kP = 3 * kB, kK = 4 * kB, kR = 5 * kB,
+                  kFork = 6 * kB, kJoin = 6 * kB + 1;
     double *d_f1 = (double*)j.f1, *d_f2 = (double*)j.f2;
     CK(cudaEventRecord(ctx->hev[kFork], st));
-    CK(cudaStreamWaitEvent(cin, ctx->hev[kFork], 0));
-    CK(cudaStreamWaitEvent(cout, ctx->hev[kFork], 0));
-    CK(cudaStreamWaitEvent(pre, ctx->hev[kFork], 0));
+    for (cudaStream_t x : {cin, cout, pc, pr, pb}) CK(cudaStreamWaitEvent(x, ctx->hev[kFork], 0));
     for (int b = 0; b < nb; ++b) {
         const size_t o = (size_t)bd.R[b] * ny, len = (size_t)(bd.R[b + 1] - bd.R[b]) * ny * sizeof(double);
         CK(cudaMemcpyAsync(d_f1 + o, f1 + o, len, cudaMemcpyHostToDevice, cin));
@@ -1429,24 +1452,34 @@ flct_status enqueue_banded(flct_ctx* ctx, const Job& j, const Bands& bd, int for
     int launches = 0;
     WinArgs wa;
     make_wargs(j, base, &wa);
-    // prepass, one band ahead: band b's box sums (and windows) read input
-    // rows of band b + 1, so they follow its classification and row sums
-    CK(cudaMemsetAsync(ctx->b_ctr.p, 0, 64 * nb, pre));
+    // the prepass runs a band ahead of the windows: band b's box sums (and
+    // windows) read input rows of band b + 1, so its column sums follow
+    // that band's row sums; the classification of a band and its row sums
+    // both read only the band's copied-in rows
+    CK(cudaMemsetAsync(ctx->b_ctr.p, 0, 64 * nb, pc));
     flct_status s = FLCT_OK;
     for (int b = 0; b <= nb && s == FLCT_OK; ++b) {
         if (b < nb) {
-            CK(cudaStreamWaitEvent(pre, ctx->hev[b], 0));
-            s = enqueue_classify(ctx, j, bb[b], bd.R[b], bd.R[b + 1], nullptr, pre, &launches);
-            if (s == FLCT_OK) s = enqueue_box_rows(ctx, j, base, bd.R[b], bd.R[b + 1], pre, &launches);
+            CK(cudaStreamWaitEvent(pc, ctx->hev[b], 0));
+            CK(cudaStreamWaitEvent(pr, ctx->hev[b], 0));
+            s = enqueue_box_rows(ctx, j, base, bd.R[b], bd.R[b + 1], pr, &launches);
+            if (s == FLCT_OK) s = enqueue_classify(ctx, j, bb[b], bd.R[b], bd.R[b + 1], nullptr, pc, &launches);
+            if (s != FLCT_OK) break;
+            CK(cudaEventRecord(ctx->hev[kR + b], pr));
+            CK(cudaEventRecord(ctx->hev[kK + b], pc));
         }
-        if (s == FLCT_OK && b > 0) {
-            s = enqueue_box_cols(ctx, j, base, bd.Q[b - 1], bd.Q[b], pre, &launches);
-            CK(cudaEventRecord(ctx->hev[kP + b - 1], pre));
+        if (b > 0) {
+            CK(cudaStreamWaitEvent(pb, ctx->hev[kR + std::min(b, nb - 1)], 0));
+            s = enqueue_box_cols(ctx, j, base, bd.Q[b - 1], bd.Q[b], pb, &launches);
+            CK(cudaEventRecord(ctx->hev[kP + b - 1], pb));
         }
     }
     for (int b = 0; b < nb && s == FLCT_OK; ++b) {
         cudaStream_t sb = bs[b];
+        // the band's box sums; the float split of its rows and of the rows
+        // below it that its windows read (the next band's classification)
         CK(cudaStreamWaitEvent(sb, ctx->hev[kP + b], 0));
+        CK(cudaStreamWaitEvent(sb, ctx->hev[kK + std::min(b + 1, nb - 1)], 0));
         // the band's windows: at most its grid points
         const long items = (long)(bd.Q[b + 1] - bd.Q[b]) * j.gj;
         s = enqueue_means(ctx, j, bb[b], items, sb, &launches);
@@ -1482,10 +1515,10 @@ flct_status enqueue_banded(flct_ctx* ctx, const Job& j, const Bands& bd, int for
     CK(cudaMemcpyAsync(ctx->hctr, ctx->b_ctr.p, 64 * nb, cudaMemcpyDeviceToHost, st));
     CK(cudaEventRecord(ctx->hev[kJoin], cout));
     CK(cudaStreamWaitEvent(st, ctx->hev[kJoin], 0));
-    CK(cudaEventRecord(ctx->hev[kJoin], cin));
-    CK(cudaStreamWaitEvent(st, ctx->hev[kJoin], 0));
-    CK(cudaEventRecord(ctx->hev[kJoin], pre));
-    CK(cudaStreamWaitEvent(st, ctx->hev[kJoin], 0));
+    for (cudaStream_t x : {cin, pc, pr, pb}) {
+        CK(cudaEventRecord(ctx->hev[kJoin], x));
+        CK(cudaStreamWaitEvent(st, ctx->hev[kJoin], 0));
+    }
     *nlaunch = launches;
     return FLCT_OK;
 }
@@ -1645,11 +1678,12 @@ flct_status flct_gpu_create(int device, flct_ctx** out) {
             flct_gpu_destroy(ctx);
             return FLCT_ERR_CUDA;
         }
-        if (cudaStreamCreateWithPriority(&ctx->prestream, cudaStreamNonBlocking, greatest) != cudaSuccess) {
-            ctx->prestream = nullptr;
-            flct_gpu_destroy(ctx);
-            return FLCT_ERR_CUDA;
-        }
+        for (auto& ps : ctx->prestream)
+            if (cudaStreamCreateWithPriority(&ps, cudaStreamNonBlocking, greatest) != cudaSuccess) {
+                ps = nullptr;
+                flct_gpu_destroy(ctx);
+                return FLCT_ERR_CUDA;
+            }
         for (int b = 0; b < flct_ctx::kMaxBands; ++b)
             if (cudaStreamCreateWithPriority(&ctx->bandstream[b], cudaStreamNonBlocking,
                                              std::min(least, greatest + 1 + b)) != cudaSuccess) {
@@ -1659,6 +1693,12 @@ flct_status flct_gpu_create(int device, flct_ctx** out) {
             }
     }
     for (auto& e : ctx->hev)
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+            e = nullptr;
+            flct_gpu_destroy(ctx);
+            return FLCT_ERR_CUDA;
+        }
+    for (auto& e : ctx->pev)
         if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
             e = nullptr;
             flct_gpu_destroy(ctx);
@@ -1686,7 +1726,8 @@ void flct_gpu_destroy(flct_ctx* ctx) {
         if (st) cudaStreamSynchronize(st);
     for (auto& st : ctx->bandstream)
         if (st) cudaStreamSynchronize(st);
-    if (ctx->prestream) cudaStreamSynchronize(ctx->prestream);
+    for (auto& st : ctx->prestream)
+        if (st) cudaStreamSynchronize(st);
     for (auto& st : ctx->bstream)
         if (st) cudaStreamSynchronize(st);
     if (ctx->bdone) cudaEventSynchronize(ctx->bdone);
@@ -1703,11 +1744,14 @@ void flct_gpu_destroy(flct_ctx* ctx) {
         if (e) cudaEventDestroy(e);
     for (auto& e : ctx->hev)
         if (e) cudaEventDestroy(e);
+    for (auto& e : ctx->pev)
+        if (e) cudaEventDestroy(e);
     for (auto& st : ctx->cstream)
         if (st) cudaStreamDestroy(st);
     for (auto& st : ctx->bandstream)
         if (st) cudaStreamDestroy(st);
-    if (ctx->prestream) cudaStreamDestroy(ctx->prestream);
+    for (auto& st : ctx->prestream)
+        if (st) cudaStreamDestroy(st);
     if (ctx->hctr) cudaFreeHost(ctx->hctr);
     if (ctx->bdone) cudaEventDestroy(ctx->bdone);
     for (auto& st : ctx->bstream)
@@ -1789,7 +1833,7 @@ flct_status flct_gpu_velocity_device(flct_ctx* ctx, const flct_params* p, const 
     // this work list, eagerly (not possible inside a stream capture)
     if (p->form == FLCT_FORM_AUTO && !ctx->tune.count(n) && !capturing(st)) {
         CK(cudaEventRecord(ctx->ev[0], st));
-        s = enqueue_prepass(ctx, j, b, st, &launches);
+        s = enqueue_prepass(ctx, j, b, st, &launches, ctx->prestream[0]);
         if (s != FLCT_OK) return s;
         WinArgs wa;
         make_wargs(j, b, &wa);
