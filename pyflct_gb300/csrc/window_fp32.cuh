@@ -207,11 +207,22 @@ k_window_fp32(WinArgs a) {
             team_sync();
         }
 
-        // separate A, B from Z and its mirror, C = conj(A) B filt^2
+        // separate A, B from Z and its mirror, C = conj(A) B filt^2.  C is
+        // the spectrum of a real image, C[-kx][-ky] = conj(C[kx][ky]), and
+        // the products below give exactly that (the mirror lane's operands
+        // are the same values with negated imaginary parts, and filt2 is even
+        // in k), so a lane forms columns 0..N/2 and takes the rest from the
+        // mirror lane: by shuffles in whole-warp teams, else through the
+        // buffer's columns 1..N/2-1, which no lane reads for its mirror Z
+        // (for n >= 24; below that the extra barrier costs more than the
+        // products it saves, measured).
+        constexpr int H = N / 2;
+        constexpr bool kMirror = kWarp || N >= 24;
+        constexpr int KC = kMirror ? H + 1 : N;
         float2 y[N];
         {
             const int mr = (N - ln) % N;
-            sfor<0, N>([&](auto kc) {
+            sfor<0, KC>([&](auto kc) {
                 constexpr int k = decltype(kc)::value;
                 constexpr int mk = (N - k) % N;
                 const float2 z = x[dif_pos<N>(k)];
@@ -228,10 +239,28 @@ k_window_fp32(WinArgs a) {
             });
             if (a.use_filter) {
                 const float fr = s_f[ln];
-                sfor<0, N>([&](auto kc) {
+                sfor<0, KC>([&](auto kc) {
                     constexpr int k = decltype(kc)::value;
                     const float f = fr * s_f[k];
                     y[k] = make_float2(f * y[k].x, f * y[k].y);
+                });
+            }
+            if constexpr (kWarp) {
+                sfor<KC, N>([&](auto kc) {
+                    constexpr int k = decltype(kc)::value;
+                    y[k].x = __shfl_sync(tmask, y[N - k].x, mr, N);
+                    y[k].y = -__shfl_sync(tmask, y[N - k].y, mr, N);
+                });
+            } else if constexpr (kMirror) {
+                sfor<1, H>([&](auto kc) {
+                    constexpr int k = decltype(kc)::value;
+                    buf[ln * (N + 1) + k] = y[k];
+                });
+                team_sync();
+                sfor<KC, N>([&](auto kc) {
+                    constexpr int k = decltype(kc)::value;
+                    const float2 c = buf[mr * (N + 1) + (N - k)];
+                    y[k] = make_float2(c.x, -c.y);
                 });
             }
         }
@@ -242,7 +271,6 @@ k_window_fp32(WinArgs a) {
         // b_k = (C[k] - C[k+H]) w^k (w = e^{2 pi i / N}); both halves have real
         // images, so one complex N x H transform of a + i b yields
         // c[i][2m] + i c[i][2m+1].  Rows: H-point transforms in registers.
-        constexpr int H = N / 2;
         float2 u[H];
         sfor<0, H>([&](auto kc) {
             constexpr int k = decltype(kc)::value;
