@@ -646,7 +646,7 @@ flct_status enqueue_box_cols(flct_ctx* ctx, const Job& j, const JobBufs& b, int 
     BoxArgs ba = box_args(j, b);
     ba.q0 = q0;
     ba.q1 = q1;
-    const long t = 2l * j.gj * ((q1 - q0 + kColRun - 1) / kColRun);
+    const long t = 2l * j.gj * ((q1 - q0 + kColRun - 1) / kColRun) * kColLanes;
     k_box_cols<<<(int)((t + 127) / 128), 128, 0, st>>>(ba);
     ++*launches;
     CK(cudaGetLastError());

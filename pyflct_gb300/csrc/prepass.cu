@@ -265,62 +265,79 @@ __global__ void __launch_bounds__(kBoxWarps * 32) k_box_rows(BoxArgs a) {
 }
 
 // Box sums B[q][m] = sum_{ii<n} RT[t_q + ii][m] at the grid's box rows
-// t_q = box_start(xo + q gs), exact.  A thread takes one line (frame, grid
-// column) and a run of kColRun grid rows starting at a multiple of kColRun;
-// the run's unit is the largest of the row sums' units it reads.
-// Consecutive threads take consecutive columns, so loads and stores are
-// coalesced.
+// t_q = box_start(xo + q gs), exact.  kColLanes consecutive lanes take one
+// line (frame, grid column) and a run of kColRun grid rows starting at a
+// multiple of kColRun; lane p reads the run's rows r with r - t = p mod
+// kColLanes, and the lanes' partial sums meet by shuffles (integer sums:
+// the order does not matter).  The run's unit is the largest of the row
+// sums' units it reads.  A warp's loads cover 32 / kColLanes consecutive
+// columns of kColLanes rows, and each lane stores one word of the box sum.
+__device__ __forceinline__ void col_reduce(unsigned long long& lo, unsigned long long& hi,
+                                           unsigned long long& cnt) {
+#pragma unroll
+    for (int o = 1; o < kColLanes; o <<= 1) {
+        const unsigned long long l2 = __shfl_xor_sync(0xffffffffu, lo, o, kColLanes);
+        const unsigned long long h2 = __shfl_xor_sync(0xffffffffu, hi, o, kColLanes);
+        cnt += __shfl_xor_sync(0xffffffffu, cnt, o, kColLanes);
+        add128(lo, hi, l2, h2);
+    }
+}
+
 __global__ void __launch_bounds__(128) k_box_cols(BoxArgs a) {
     const int lines = 2 * a.gj;
     const int runs = (a.q1 - a.q0 + kColRun - 1) / kColRun;
-    const long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (idx >= (long)lines * runs) return;
+    const long gid = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    const int p = (int)(gid & (kColLanes - 1));
+    long idx = gid / kColLanes;
+    // a group past the end repeats the last line (every lane of the warp
+    // takes part in the shuffles) and stores nothing
+    const bool act = idx < (long)lines * runs;
+    if (!act) idx = (long)lines * runs - 1;
     const int run = (int)(idx / lines), lam = (int)(idx - (long)run * lines);
     const int img = lam >= a.gj, m = lam - img * a.gj;
     const BoxSum* __restrict__ v = (img ? a.rt2 : a.rt1) + m;  // row r at v[r * gj]
     const int* __restrict__ ve = (img ? a.re2 : a.re1) + m;
-    BoxSum* __restrict__ o = (img ? a.b2 : a.b1) + m;
+    unsigned long long* __restrict__ o = reinterpret_cast<unsigned long long*>((img ? a.b2 : a.b1) + m);
     const size_t gj = (size_t)a.gj;
     const int q0 = a.q0 + run * kColRun, q1 = min(q0 + kColRun, a.q1);
     int t = box_start(a.xo + q0 * a.gs, a.nx, a.nsize);
     const int tend = box_start(a.xo + (q1 - 1) * a.gs, a.nx, a.nsize) + a.n;
     int eb = 1;
-    for (int r = t; r < tend; ++r) eb = max(eb, __ldg(ve + r * gj));
-    unsigned long long lo[4] = {0ull, 0ull, 0ull, 0ull}, hi[4] = {0ull, 0ull, 0ull, 0ull}, cnt = 0ull;
-    int d = 0;
-    for (; d + 8 <= a.n; d += 8) {
-        BoxSum r[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) r[u] = v[(t + d + u) * gj];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            sar128(r[u].lo, r[u].hi, eb - (int)r[u].e);
-            add128(lo[u & 3], hi[u & 3], r[u].lo, r[u].hi);
-            cnt += r[u].cnt;
-        }
-    }
-    for (; d < a.n; ++d) {
-        BoxSum r = v[(t + d) * gj];
-        sar128(r.lo, r.hi, eb - (int)r.e);
-        add128(lo[0], hi[0], r.lo, r.hi);
-        cnt += r.cnt;
-    }
-    add128(lo[0], hi[0], lo[1], hi[1]);
-    add128(lo[2], hi[2], lo[3], hi[3]);
-    add128(lo[0], hi[0], lo[2], hi[2]);
-    for (int q = q0;;) {
-        o[q * gj] = BoxSum{lo[0], hi[0], cnt, (unsigned long long)eb};
-        if (++q >= q1) break;
-        const int tn = box_start(a.xo + q * a.gs, a.nx, a.nsize);
 #pragma unroll 4
-        for (int r = t; r < tn; ++r) {
+    for (int r = t + p; r < tend; r += kColLanes) eb = max(eb, __ldg(ve + r * gj));
+#pragma unroll
+    for (int k = 1; k < kColLanes; k <<= 1) eb = max(eb, __shfl_xor_sync(0xffffffffu, eb, k, kColLanes));
+    unsigned long long lo = 0ull, hi = 0ull, cnt = 0ull;
+#pragma unroll 8
+    for (int r = t + p; r < t + a.n; r += kColLanes) {
+        BoxSum x = v[r * gj];
+        sar128(x.lo, x.hi, eb - (int)x.e);
+        add128(lo, hi, x.lo, x.hi);
+        cnt += x.cnt;
+    }
+    col_reduce(lo, hi, cnt);
+    for (int q = q0;;) {
+        if (act) {
+            const unsigned long long w = (p == 0) ? lo : (p == 1) ? hi : (p == 2) ? cnt : (unsigned long long)eb;
+            o[(size_t)q * gj * (sizeof(BoxSum) / 8) + p] = w;
+        }
+        if (++q >= q1) break;
+        // slide down to the next grid row's box: rows [t, tn) leave, rows
+        // [t + n, tn + n) enter
+        const int tn = box_start(a.xo + q * a.gs, a.nx, a.nsize);
+        unsigned long long dl = 0ull, dh = 0ull, dc = 0ull;
+#pragma unroll 2
+        for (int r = t + p; r < tn; r += kColLanes) {
             BoxSum in = v[(r + a.n) * gj], out = v[r * gj];
             sar128(in.lo, in.hi, eb - (int)in.e);
             sar128(out.lo, out.hi, eb - (int)out.e);
-            add128(lo[0], hi[0], in.lo, in.hi);
-            sub128(lo[0], hi[0], out.lo, out.hi);
-            cnt += in.cnt - out.cnt;
+            add128(dl, dh, in.lo, in.hi);
+            sub128(dl, dh, out.lo, out.hi);
+            dc += in.cnt - out.cnt;
         }
+        col_reduce(dl, dh, dc);
+        add128(lo, hi, dl, dh);
+        cnt += dc;
         t = tn;
     }
 }

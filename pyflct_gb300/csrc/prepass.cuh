@@ -29,6 +29,8 @@ constexpr int kRowSpan = 544;
 // Column pass: grid rows per thread, runs start at multiples of it (the
 // units of a run's box sums depend on the rows it reads)
 constexpr int kColRun = 4;
+// Column pass: lanes that share one run's rows (a power of two <= 32)
+constexpr int kColLanes = 4;
 
 // Local-mean box sums for the boxes the grid needs, exact (fixsum.cuh).
 // Grid point (q, m) is pixel (xo + q gs, yo + m gs) (gs = 1, xo = yo = 0
