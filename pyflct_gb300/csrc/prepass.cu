@@ -86,17 +86,40 @@ __global__ void __launch_bounds__(256) k_classify(ClassifyArgs a) {
     // the grid test's column remainder: (j - yoff) mod skip = tile base + this thread's offset
     const int sk = a.skip > 0 ? a.skip : 1;
     const int tmod = (int)threadIdx.x % sk;
-    for (int t = blockIdx.x; t < ntile; t += gridDim.x) {
+    // this thread's pixel of tile t, its frames' values loaded a tile ahead
+    auto pixel = [&](int t, int& i, int& j0) {
         const int ti = t / tpr;
-        const int i = a.r0 + ti;
-        const int j0 = (t - ti * tpr) * 256, j = j0 + threadIdx.x;
+        i = a.r0 + ti;
+        j0 = (t - ti * tpr) * 256;
+    };
+    double fa = 0., fb = 0.;
+    if (blockIdx.x < ntile) {
+        int i, j0;
+        pixel(blockIdx.x, i, j0);
+        if (j0 + (int)threadIdx.x < a.ny) {
+            fa = a.f1[(size_t)i * a.ny + j0 + threadIdx.x];
+            fb = a.f2[(size_t)i * a.ny + j0 + threadIdx.x];
+        }
+    }
+    for (int t = blockIdx.x; t < ntile; t += gridDim.x) {
+        int i, j0;
+        pixel(t, i, j0);
+        const int j = j0 + threadIdx.x;
+        double na = 0., nb = 0.;
+        if (t + (int)gridDim.x < ntile) {
+            int i2, j2;
+            pixel(t + gridDim.x, i2, j2);
+            if (j2 + (int)threadIdx.x < a.ny) {
+                na = a.f1[(size_t)i2 * a.ny + j2 + threadIdx.x];
+                nb = a.f2[(size_t)i2 * a.ny + j2 + threadIdx.x];
+            }
+        }
         int rj = ((j0 - a.yoff) % sk + sk) % sk + tmod;  // uniform part + per-thread part
         rj = rj >= sk ? rj - sk : rj;
         const bool act = j < a.ny;
         const size_t k = (size_t)i * a.ny + j;
         bool comp = false, grid = false;
         if (act) {
-            const double fa = a.f1[k], fb = a.f2[k];
             const float2 sa = split_double_fast(fa), sb = split_double_fast(fb);
             a.s1[k] = sa;
             a.s2[k] = sb;
@@ -153,6 +176,8 @@ __global__ void __launch_bounds__(256) k_classify(ClassifyArgs a) {
             }
         }
         __syncthreads();  // s_cnt / s_base are rewritten by the next tile
+        fa = na;
+        fb = nb;
     }
 }
 
@@ -188,23 +213,26 @@ __global__ void __launch_bounds__(kBoxWarps * 32) k_box_rows(BoxArgs a) {
         const int span = box_start(a.yo + (Mend - 1) * a.gs, a.ny, a.nsize) + a.n - base;  // <= kRowSpan
         const int C = max(3, ((span + 31) >> 5) | 1);  // odd, >= 3: the division below is exact
         const int e0 = min(lane * C, span), e1 = min(e0 + C, span);
-        // the chunk's doubles into words 0 and 1 of the stage, and the span's
-        // largest finite exponent (its unit)
+        // the span's doubles into words 0 and 1 of the stage (coalesced, all
+        // loads in flight at once), and its largest finite exponent (its unit)
         unsigned em = 0u;
-        for (int e = e0; e < e1; e += 4) {
-            double x[4];
+        {
+            constexpr int KL = (kRowSpan + 31) / 32;
+            double x[KL];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) x[u] = (e + u < e1) ? v[base + e + u] : 0.0;
+            for (int k = 0; k < KL; ++k) x[k] = (lane + 32 * k < span) ? v[base + lane + 32 * k] : 0.0;
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                if (e + u < e1) {
-                    const unsigned hw = (unsigned)__double2hiint(x[u]), xe = (hw >> 20) & 0x7ffu;
+            for (int k = 0; k < KL; ++k) {
+                const int e = lane + 32 * k;
+                if (e < span) {
+                    const unsigned hw = (unsigned)__double2hiint(x[k]), xe = (hw >> 20) & 0x7ffu;
                     em = (xe != 0x7ffu && xe > em) ? xe : em;
-                    sw[e + u] = (unsigned)__double2loint(x[u]);
-                    sw[SW + e + u] = hw;
+                    sw[e] = (unsigned)__double2loint(x[k]);
+                    sw[SW + e] = hw;
                 }
             }
         }
+        __syncwarp();  // lanes read each other's staged words below
         const int ee = max((int)__reduce_max_sync(0xffffffffu, em), 1);
         // running sums of the chunk, in place
         unsigned acc[4] = {0u, 0u, 0u, 0u}, cnt = 0u;
