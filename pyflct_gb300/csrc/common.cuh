@@ -68,6 +68,17 @@ __device__ __forceinline__ float2 split_double_fast(double x) {
     return make_float2(hi, lo);
 }
 
+// The call's work count and status word (final once this kernel starts: no
+// later kernel writes them) to mapped page-locked host memory, so that no
+// copy node ends the call.
+__device__ __forceinline__ void publish_counters(const unsigned* src, unsigned* dst) {
+    if (dst && blockIdx.x == 0 && threadIdx.x == 0) {
+        dst[0] = src[0];
+        dst[1] = src[1];
+        __threadfence_system();
+    }
+}
+
 // Exact float -> double with integer operations for normal floats and
 // zeros; subnormals, infinities and NaN take the conversion instruction.
 __device__ __forceinline__ double f2d(float f) {

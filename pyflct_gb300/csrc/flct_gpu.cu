@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -122,6 +123,7 @@ struct flct_ctx {
     int batch_launches = 0;
     int batch_box = 0, batch_form = 0;
     unsigned char* hctr = nullptr;  // page-locked copies of a call's work counts and status words
+    unsigned* hctr_dev = nullptr;   // the same memory, mapped: the last kernel of a call writes it
     // host-buffer calls in row bands, so that the copies overlap the
     // computation: copy-in and copy-out streams, per-band events
     static constexpr int kMaxBands = 8;
@@ -729,9 +731,17 @@ void make_wargs(const Job& j, const JobBufs& b, WinArgs* wa) {
 }
 
 // 3x3 fit, velocity, mask and skip-grid copy per work item (flct.c:901-942).
+// Where the last kernel of a call copies the call's counters (none: null).
+struct Pub {
+    const unsigned* src = nullptr;
+    unsigned* dst = nullptr;
+};
+
 flct_status enqueue_fit(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaStream_t st, int* launches,
-                        long max_items = -1) {
+                        long max_items = -1, Pub pub = Pub{}) {
     FitArgs fa{};
+    fa.pub_src = pub.src;
+    fa.pub_dst = pub.dst;
     fa.work = b.work;
     fa.nwork = (const int*)b.ctr;
     fa.peaks = b.peaks;
@@ -763,10 +773,12 @@ flct_status enqueue_fit(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaStrea
 // Cubic-convolution interpolation of the skip grid onto the skipped pixels,
 // mask and xmiss reset (flct.c:958-1133).
 flct_status enqueue_interp(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaStream_t st, int* launches,
-                           int i0 = 0, int i1 = -1) {
+                           int i0 = 0, int i1 = -1, Pub pub = Pub{}) {
     if (i1 < 0) i1 = j.nx;
     if (i1 <= i0) return FLCT_OK;
     InterpArgs ia{};
+    ia.pub_src = pub.src;
+    ia.pub_dst = pub.dst;
     ia.nx = j.nx;
     ia.ny = j.ny;
     ia.skip = j.d.skip;
@@ -780,6 +792,8 @@ flct_status enqueue_interp(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaSt
     ia.vm = j.vm;
     ia.i0 = i0;
     ia.i1 = i1;
+    // pixel pairs (j even) start on 16-byte boundaries when ny is even
+    ia.pairs = (j.ny % 2 == 0) && ((((uintptr_t)j.vx) | ((uintptr_t)j.vy) | ((uintptr_t)j.vm)) & 15u) == 0u;
     const long tiles = (long)((i1 - i0 + kTileR - 1) / kTileR) * ((j.ny + kTileC - 1) / kTileC);
     k_interp_grid<<<(int)std::max(1l, std::min<long>(tiles, (long)ctx->nsm * 8)), kInterpThreads, 0, st>>>(ia);
     ++*launches;
@@ -1322,15 +1336,16 @@ flct_status enqueue_device_tail(flct_ctx* ctx, const Job& j, const JobBufs& b, i
     if (s != FLCT_OK) return s;
     ++*launches;
     CK(cudaEventRecordWithFlags(ctx->ev[2], st, evf));
-    s = enqueue_fit(ctx, j, b, st, launches);
+    // the last kernel copies the work count and status to page-locked
+    // memory; they are there once ev[3] completes
+    const Pub pub{(const unsigned*)b.ctr, ctx->hctr_dev};
+    s = enqueue_fit(ctx, j, b, st, launches, -1, j.interp ? Pub{} : pub);
     if (s != FLCT_OK) return s;
     CK(cudaEventRecordWithFlags(ctx->ev[7], st, evf));
     if (j.interp) {
-        s = enqueue_interp(ctx, j, b, st, launches);
+        s = enqueue_interp(ctx, j, b, st, launches, 0, -1, pub);
         if (s != FLCT_OK) return s;
     }
-    // work count and status to page-locked memory, complete with ev[3]
-    CK(cudaMemcpyAsync(ctx->hctr, b.ctr, 8, cudaMemcpyDeviceToHost, st));
     CK(cudaEventRecordWithFlags(ctx->ev[3], st, evf));
     return FLCT_OK;
 }
@@ -1492,12 +1507,15 @@ flct_status enqueue_banded(flct_ctx* ctx, const Job& j, const Bands& bd, int for
         wb.peaks_h = j.p->hires ? bb[b].peaks_h : nullptr;
         s = launch_windows(ctx, form, j.we, j.n, wb, (unsigned*)(bb[b].ctr + 4), sb, grid_div, items);
         ++launches;
-        if (s == FLCT_OK) s = enqueue_fit(ctx, j, bb[b], sb, &launches, items);
+        // the band's last kernel copies its counters to page-locked memory
+        const Pub pub{(const unsigned*)bb[b].ctr, ctx->hctr_dev + 16 * b};
+        const bool interp = j.interp && bd.O[b + 1] > bd.O[b];
+        if (s == FLCT_OK) s = enqueue_fit(ctx, j, bb[b], sb, &launches, items, interp ? Pub{} : pub);
         if (s != FLCT_OK) break;
         CK(cudaEventRecord(ctx->hev[kF + b], sb));
         // the band's first output rows interpolate from the band before's grid
         if (b > 0) CK(cudaStreamWaitEvent(sb, ctx->hev[kF + b - 1], 0));
-        if (j.interp) s = enqueue_interp(ctx, j, base, sb, &launches, bd.O[b], bd.O[b + 1]);
+        if (interp) s = enqueue_interp(ctx, j, base, sb, &launches, bd.O[b], bd.O[b + 1], pub);
         if (s != FLCT_OK) break;
         CK(cudaEventRecord(ctx->hev[kC + b], sb));
         CK(cudaStreamWaitEvent(cout, ctx->hev[kC + b], 0));
@@ -1510,9 +1528,7 @@ flct_status enqueue_banded(flct_ctx* ctx, const Job& j, const Bands& bd, int for
         CK(cudaStreamWaitEvent(st, ctx->hev[kC + b], 0));
     }
     if (s != FLCT_OK) return s;
-    // every band's work count and status to page-locked memory; the
-    // copy-out and the copy-in stream join the call's stream
-    CK(cudaMemcpyAsync(ctx->hctr, ctx->b_ctr.p, 64 * nb, cudaMemcpyDeviceToHost, st));
+    // the copy-out, copy-in and prepass streams join the call's stream
     CK(cudaEventRecord(ctx->hev[kJoin], cout));
     CK(cudaStreamWaitEvent(st, ctx->hev[kJoin], 0));
     for (cudaStream_t x : {cin, pc, pr, pb}) {
@@ -1706,10 +1722,15 @@ flct_status flct_gpu_create(int device, flct_ctx** out) {
         }
     if (const char* nb = getenv("FLCT_HOST_BANDS"))
         ctx->host_bands_max = std::max(0, std::min(flct_ctx::kMaxBands, atoi(nb)));
-    if (cudaHostAlloc((void**)&ctx->hctr, 64 * flct_ctx::kMaxBands, cudaHostAllocDefault) != cudaSuccess) {
+    if (cudaHostAlloc((void**)&ctx->hctr, 64 * flct_ctx::kMaxBands, cudaHostAllocMapped) != cudaSuccess) {
         ctx->hctr = nullptr;
         flct_gpu_destroy(ctx);
         return FLCT_ERR_ALLOC;
+    }
+    memset(ctx->hctr, 0, 64 * flct_ctx::kMaxBands);
+    if (cudaHostGetDevicePointer((void**)&ctx->hctr_dev, ctx->hctr, 0) != cudaSuccess) {
+        flct_gpu_destroy(ctx);
+        return FLCT_ERR_CUDA;
     }
     ctx->device_name = prop.name;
     if (const char* path = getenv("FLCT_AUTOTUNE_CACHE")) ctx->tune_path = path;

@@ -506,9 +506,12 @@ __device__ __noinline__ float2 cdata_f(const float2* __restrict__ g, int gx, int
 // every tile row, V[r][b] = sum_p rx_r[p] patch[izr + p][b] (with per-column
 // y stencils tabulated alongside); then each pixel contracts four V values
 // with its y weights.  xmiss flags travel with the values (bit 0: vx,
-// bit 1: vy).
-constexpr int kTileRT = kInterpThreads / kTileC;  // thread rows; a thread takes tile rows ti + kTileRT k
+// bit 1: vy).  The patch and V items are spread over all threads (row =
+// item / width by a multiply-high); a thread writes two adjacent pixels,
+// as 16-byte stores when the rows allow.
 constexpr int kPatchR = kTileR + 4, kPatchC = kTileC + 4;  // cdata rows / columns at skip 1
+constexpr int kPairCols = kTileC / 2;                       // threads per tile row in the output step
+constexpr int kPairRows = kInterpThreads / kPairCols;       // tile rows per output pass
 
 __global__ void __launch_bounds__(kInterpThreads) k_interp_grid(InterpArgs a) {
     __shared__ float2 s_p[kPatchR * kPatchC];
@@ -525,7 +528,8 @@ __global__ void __launch_bounds__(kInterpThreads) k_interp_grid(InterpArgs a) {
     const int ntr = (a.i1 - a.i0 + kTileR - 1) / kTileR;
     const float inv = 1.0f / (float)a.skip;
     const int imax = (a.gx - 1) * a.skip, jmax = (a.gy - 1) * a.skip;
-    const int ti = threadIdx.x / kTileC, tj = threadIdx.x - (threadIdx.x / kTileC) * kTileC;
+    const int tc = (threadIdx.x % kPairCols) * 2, tr = threadIdx.x / kPairCols;
+    publish_counters(a.pub_src, a.pub_dst);
     for (int tile = blockIdx.x; tile < ntr * ntc; tile += gridDim.x) {
         const int i0 = a.i0 + (tile / ntc) * kTileR, j0 = (tile - (tile / ntc) * ntc) * kTileC;
         // cdata rows / columns the tile's in-range pixels use
@@ -534,19 +538,20 @@ __global__ void __launch_bounds__(kInterpThreads) k_interp_grid(InterpArgs a) {
         const bool any = dlo <= dhi && elo <= ehi;
         const int r0 = any ? min(dlo / a.skip, a.gx - 2) : 0, r1 = any ? min(dhi / a.skip, a.gx - 2) + 3 : -1;
         const int c0 = any ? min(elo / a.skip, a.gy - 2) : 0, c1 = any ? min(ehi / a.skip, a.gy - 2) + 3 : -1;
-        const int pw = c1 - c0 + 1, ph = r1 - r0 + 1;
+        const int pw = c1 - c0 + 1, ph = r1 - r0 + 1;  // pw >= 4 when any
+        // item / pw = umulhi(item, ceil(2^32 / pw)), exact for items below 2^32 / pw
+        const unsigned mpw = 0xffffffffu / (unsigned)max(pw, 1) + 1u;
         __syncthreads();  // the previous tile's tables are consumed
-        // patch: row pr = t / 32 (+ 8 k), column pc = t % 32 (+ 32 k)
-        for (int pr = ti; pr < ph; pr += kTileRT)
-            for (int pc = tj; pc < pw; pc += kTileC) {
-                const int ra = r0 + pr, cb = c0 + pc;
-                const float2 v = (ra >= 1 && ra <= a.gx && cb >= 1 && cb <= a.gy)
-                                     ? __ldg(a.grid + (size_t)(ra - 1) * a.gy + (cb - 1))
-                                     : cdata_f(a.grid, a.gx, a.gy, ra, cb);
-                const int e = pr * kPatchC + pc;
-                s_p[e] = v;
-                s_pb[e] = (v.x == kXmissF ? 1 : 0) | (v.y == kXmissF ? 2 : 0);
-            }
+        for (int e = threadIdx.x; e < ph * pw; e += kInterpThreads) {
+            const int pr = (int)__umulhi((unsigned)e, mpw), pc = e - pr * pw;
+            const int ra = r0 + pr, cb = c0 + pc;
+            const float2 v = (ra >= 1 && ra <= a.gx && cb >= 1 && cb <= a.gy)
+                                 ? __ldg(a.grid + (size_t)(ra - 1) * a.gy + (cb - 1))
+                                 : cdata_f(a.grid, a.gx, a.gy, ra, cb);
+            const int pe = pr * kPatchC + pc;
+            s_p[pe] = v;
+            s_pb[pe] = (v.x == kXmissF ? 1 : 0) | (v.y == kXmissF ? 2 : 0);
+        }
         // per-column and per-row stencil tables
         if (threadIdx.x < kTileC) {
             const int dj = j0 + threadIdx.x - a.yoff;
@@ -570,57 +575,85 @@ __global__ void __launch_bounds__(kInterpThreads) k_interp_grid(InterpArgs a) {
         }
         __syncthreads();
         // V[r][b] = sum_p rx[r][p] patch[iz_r - r0 + p][b]
-        for (int r = ti; r < kTileR; r += kTileRT)
-            for (int b = tj; b < pw; b += kTileC) {
-                const int iz = s_iz[r];
-                float2 v = make_float2(0.f, 0.f);
-                unsigned char bad = 3;
-                if (iz >= 0) {
-                    bad = 0;
+        for (int e = threadIdx.x; e < kTileR * pw; e += kInterpThreads) {
+            const int r = (int)__umulhi((unsigned)e, mpw), b = e - r * pw;
+            const int iz = s_iz[r];
+            float2 v = make_float2(0.f, 0.f);
+            unsigned char bad = 3;
+            if (iz >= 0) {
+                bad = 0;
 #pragma unroll
-                    for (int p = 0; p < 4; ++p) {
-                        const float rx = s_rx[r][p];
-                        const int pe = (iz - r0 + p) * kPatchC + b;
-                        const float2 c = s_p[pe];
-                        bad |= s_pb[pe];
-                        v.x = fmaf(rx, c.x, v.x);
-                        v.y = fmaf(rx, c.y, v.y);
+                for (int p = 0; p < 4; ++p) {
+                    const float rx = s_rx[r][p];
+                    const int pe = (iz - r0 + p) * kPatchC + b;
+                    const float2 c = s_p[pe];
+                    bad |= s_pb[pe];
+                    v.x = fmaf(rx, c.x, v.x);
+                    v.y = fmaf(rx, c.y, v.y);
+                }
+            }
+            s_v[r * kPatchC + b] = v;
+            s_vb[r * kPatchC + b] = bad;
+        }
+        __syncthreads();
+        // pixels (i, j) and (i, j + 1); a column past ny has jz = -1
+        const int j = j0 + tc;
+        if (j >= a.ny) continue;
+        const bool two = j + 1 < a.ny;
+        int jz[2];
+        bool gj[2];
+        float ry[2][4];
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+            jz[c] = s_jz[tc + c];
+            gj[c] = s_gj[tc + c];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) ry[c][q] = s_ry[tc + c][q];
+        }
+#pragma unroll
+        for (int k2 = 0; k2 < kTileR / kPairRows; ++k2) {
+            const int r = tr + kPairRows * k2, i = i0 + r;
+            if (i >= a.i1) break;
+            const bool gi = s_gi[r] && i - a.xoff >= 0;
+            const int iz = s_iz[r];
+            double ox[2], oy[2], om[2];
+            bool wr[2];
+#pragma unroll
+            for (int c = 0; c < 2; ++c) {
+                wr[c] = (c == 0 || two) && !(gj[c] && gi);  // grid points keep their computed value
+                float sx = 0.f, sy = 0.f;
+                unsigned bad = 3;
+                if (jz[c] >= 0 && iz >= 0) {
+                    bad = 0;
+                    const int vb = r * kPatchC + (jz[c] - c0);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const float2 v = s_v[vb + q];
+                        bad |= s_vb[vb + q];
+                        sx = fmaf(ry[c][q], v.x, sx);
+                        sy = fmaf(ry[c][q], v.y, sy);
                     }
                 }
-                s_v[r * kPatchC + b] = v;
-                s_vb[r * kPatchC + b] = bad;
-            }
-        __syncthreads();
-        const int j = j0 + tj;
-        if (j >= a.ny) continue;
-        const int jz = s_jz[tj];
-        const bool gj = s_gj[tj];
-        float ry[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) ry[q] = s_ry[tj][q];
-#pragma unroll
-        for (int k4 = 0; k4 < kTileR / kTileRT; ++k4) {
-            const int r = ti + kTileRT * k4, i = i0 + r;
-            if (i >= a.i1) break;
-            if (gj && s_gi[r] && i - a.xoff >= 0) continue;  // grid points keep their computed value
-            float sx = 0.f, sy = 0.f;
-            unsigned bad = 3;
-            if (jz >= 0 && s_iz[r] >= 0) {
-                bad = 0;
-                const int vb = r * kPatchC + (jz - c0);
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const float2 v = s_v[vb + q];
-                    bad |= s_vb[vb + q];
-                    sx = fmaf(ry[q], v.x, sx);
-                    sy = fmaf(ry[q], v.y, sy);
-                }
+                // xmiss reset: a missing vx clears the mask, a missing vy only vy
+                ox[c] = (bad & 1) ? 0. : f2d(sx);
+                oy[c] = (bad & 2) ? 0. : f2d(sy);
+                om[c] = (bad & 1) ? 0. : 0.5;
             }
             const size_t k = (size_t)i * a.ny + j;
-            // xmiss reset: a missing vx clears the mask, a missing vy only vy
-            a.vx[k] = (bad & 1) ? 0. : f2d(sx);
-            a.vy[k] = (bad & 2) ? 0. : f2d(sy);
-            a.vm[k] = (bad & 1) ? 0. : 0.5;
+            if (a.pairs && wr[0] && wr[1]) {
+                *reinterpret_cast<double2*>(a.vx + k) = make_double2(ox[0], ox[1]);
+                *reinterpret_cast<double2*>(a.vy + k) = make_double2(oy[0], oy[1]);
+                *reinterpret_cast<double2*>(a.vm + k) = make_double2(om[0], om[1]);
+            } else {
+#pragma unroll
+                for (int c = 0; c < 2; ++c) {
+                    if (wr[c]) {
+                        a.vx[k + c] = ox[c];
+                        a.vy[k + c] = oy[c];
+                        a.vm[k + c] = om[c];
+                    }
+                }
+            }
         }
     }
 }

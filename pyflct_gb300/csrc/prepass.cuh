@@ -58,6 +58,9 @@ struct InterpArgs {
     const float2* grid;       // (vx, vy) per grid point [gx][gy]
     double *vx, *vy, *vm;
     int i0, i1;               // output rows to interpolate
+    int pairs;                // ny even and vx, vy, vm 16-byte aligned: pixel pairs as 16-byte stores
+    const unsigned* pub_src;  // the call's counters to host memory (publish_counters)
+    unsigned* pub_dst;
 };
 
 __global__ void k_absmax(const double* f1, const double* f2, long n, unsigned long long* out);

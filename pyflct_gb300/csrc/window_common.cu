@@ -69,6 +69,7 @@ __device__ __forceinline__ void fit3x3(const double* v, double* sx, double* sy) 
 }
 
 __global__ void k_fit(FitArgs a) {
+    publish_counters(a.pub_src, a.pub_dst);
     const int nw = *a.nwork;
     const int half = a.n / 2, half1 = (a.n1 ? a.n1 : a.n) / 2;
     for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < nw; w += gridDim.x * blockDim.x) {
@@ -136,6 +137,7 @@ __global__ void __launch_bounds__(128) k_fit_hires(FitArgs a) {
     __shared__ float s_pk[4][NI * NI];
     __shared__ float s_rx[4][NI][4];
     __shared__ int s_iz[4][NI];
+    publish_counters(a.pub_src, a.pub_dst);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nw = *a.nwork;
     const int n = a.n, m = a.n1 ? a.n1 : a.n;

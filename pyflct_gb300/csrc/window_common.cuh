@@ -69,7 +69,10 @@ struct FitArgs {
     float2* grid;          // skip-grid (vx, vy) for the interpolation, or null
     double *shx, *shy;     // raw shifts per work item or null
     const PeakRecH* peaks_h;  // -h: patches instead of peaks (k_fit_hires)
+    const unsigned* pub_src;  // when pub_dst is set: the call's work count and status,
+    unsigned* pub_dst;        // copied to page-locked host memory by one thread
 };
+
 
 // One image pair of a batched window launch.  The pair's work items,
 // means and peak records sit at [base, base + its work count) of the
