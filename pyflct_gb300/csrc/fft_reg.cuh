@@ -1,11 +1,15 @@
 // fft_reg.cuh -- register-resident mixed-radix FFT for one thread.
 //
 // A length-L complex transform of an array held in a thread's registers,
-// fully unrolled at compile time: decimation in frequency, L = R * M with
-// R in {4, 2, 3, 5, 7, ...} (a prime R > 5 uses a direct R-point DFT), so
-// every box size the sliding window can take (n = 2*nsize, a multiple of 4)
-// has a kernel.  Output frequency k lands in register dif_pos<L>(k); every
-// index is a compile-time constant, so the permutation costs nothing.
+// fully unrolled at compile time: decimation in time, L = R * M with R in
+// {4, 2, 3, 5, 7, ...} (a prime R > 5 uses a direct R-point DFT), so every
+// box size the sliding window can take (n = 2*nsize, a multiple of 4) has a
+// kernel.  Input n sits in register dit_in<L>(n) (a digit reversal), output
+// frequency k in register k; every index is a compile-time constant, so the
+// permutation costs nothing.  The combining butterflies of radix 4 and 2
+// fuse their twiddle products into their sums with FMAs (a + w b in four
+// FMAs, a - w b = 2a - (a + w b) in two), ~8% fewer FP32 operations than
+// twiddling after the butterflies.
 //
 // Twiddles are compile-time constants: the angle 2*pi*k/L is reduced exactly
 // with integer arithmetic to the first octant and evaluated by a Taylor
@@ -78,17 +82,6 @@ constexpr int radix_of() {
     else if constexpr (L % 11 == 0) return 11;
     else if constexpr (L % 13 == 0) return 13;
     else return L;
-}
-
-// Register position of output frequency k after dif<L>.
-template <int L>
-constexpr int dif_pos(int k) {
-    if constexpr (L == 1) {
-        return 0;
-    } else {
-        constexpr int R = radix_of<L>(), M = L / R;
-        return M * (k % R) + dif_pos<M>(k / R);
-    }
 }
 
 // ------------------------------------------------------ complex helpers --
@@ -164,16 +157,6 @@ FLCT_HD float2 twmul(float2 a) {
     }
 }
 
-// a + d * exp(DIR * 2*pi*i * NUM/DEN): the sum is packed unless the twiddle
-// is a quarter turn (then the product is a swap / negation, free in scalar
-// form).
-template <int DIR, long NUM, long DEN>
-FLCT_HD float2 tw_add(float2 a, float2 d) {
-    constexpr long r = ((NUM % DEN) + DEN) % DEN;
-    if constexpr ((4 * r) % DEN == 0) return cadd_s(a, twmul<DIR, NUM, DEN>(d));
-    else return cadd(a, twmul<DIR, NUM, DEN>(d));
-}
-
 // ----------------------------------------------------------- butterflies --
 
 template <int R, int DIR>
@@ -233,30 +216,118 @@ FLCT_HD void small_dft(float2* t) {
     }
 }
 
-// In-place DIF transform of x[OFF .. OFF+L): out freq k at x[OFF + dif_pos<L>(k)].
-// DIR = -1 forward (exp(-i...)), +1 backward; unnormalised.
+// ------------------------------------------------- DIT, fused twiddles --
+
+// a + b w, w = exp(DIR * 2*pi*i * NUM/DEN), with the product fused into
+// the sum: FMAs for a general twiddle, two adds and two FMAs at odd
+// multiples of pi/4, a packed add or a swap for the exact cases.
+template <int DIR, long NUM, long DEN>
+FLCT_HD float2 tw_fma_add(float2 a, float2 b) {
+    constexpr long r = ((NUM % DEN) + DEN) % DEN;
+    if constexpr (r == 0) {
+        return cadd(a, b);
+    } else if constexpr ((4 * r) % DEN == 0) {
+        return cadd_s(a, twmul<DIR, NUM, DEN>(b));
+    } else if constexpr (8 * r == DEN || 8 * r == 3 * DEN || 8 * r == 5 * DEN || 8 * r == 7 * DEN) {
+        constexpr CS w = ct_cossin(r, DEN);
+        constexpr float c = (float)w.c, s = (float)(DIR * w.s);
+        constexpr float h = c;
+        if constexpr ((c > 0) == (s > 0)) {
+            return make_float2(fmaf(h, b.x - b.y, a.x), fmaf(h, b.x + b.y, a.y));
+        } else {
+            return make_float2(fmaf(h, b.x + b.y, a.x), fmaf(h, b.y - b.x, a.y));
+        }
+    } else {
+        constexpr CS w = ct_cossin(r, DEN);
+        constexpr float c = (float)w.c, s = (float)(DIR * w.s);
+        return make_float2(fmaf(c, b.x, fmaf(-s, b.y, a.x)), fmaf(c, b.y, fmaf(s, b.x, a.y)));
+    }
+}
+
+// p = a + b w, m = a - b w; with a non-trivial twiddle m = 2a - p (one
+// FMA per component instead of a second product).
+template <int DIR, long NUM, long DEN>
+FLCT_HD void tw_pair(float2 a, float2 b, float2& p, float2& m) {
+    constexpr long r = ((NUM % DEN) + DEN) % DEN;
+    if constexpr (r == 0) {
+        p = cadd(a, b);
+        m = csub(a, b);
+    } else if constexpr ((4 * r) % DEN == 0) {
+        const float2 tb = twmul<DIR, NUM, DEN>(b);
+        p = cadd_s(a, tb);
+        m = csub_s(a, tb);
+    } else {
+        p = tw_fma_add<DIR, NUM, DEN>(a, b);
+        m = make_float2(fmaf(2.0f, a.x, -p.x), fmaf(2.0f, a.y, -p.y));
+    }
+}
+
+// Register position of input n for dit<L>: the mixed-radix digit reversal
+// (input r + R m of a level goes to sub-transform r, position m).
+template <int L>
+constexpr int dit_in(int n) {
+    if constexpr (L == 1) {
+        return 0;
+    } else {
+        constexpr int R = radix_of<L>(), M = L / R;
+        return (n % R) * M + dit_in<M>(n / R);
+    }
+}
+
+// In-place decimation-in-time transform of x[OFF .. OFF+L): input n at
+// x[OFF + dit_in<L>(n)], output k at x[OFF + k].  The R sub-transforms of
+// length M = L/R come first; the combining butterflies take their inputs
+// times the twiddles w_L^(r k), fused into the butterflies' sums for
+// radix 4 and 2.  DIR = -1 forward, +1 backward; unnormalised.
 template <int L, int OFF, int DIR>
-FLCT_HD void dif(float2* x) {
+FLCT_HD void dit(float2* x) {
     if constexpr (L > 1) {
         constexpr int R = radix_of<L>(), M = L / R;
-        sfor<0, M>([&](auto mc) {
-            constexpr int m = decltype(mc)::value;
-            float2 t[R];
-            sfor<0, R>([&](auto rc) {
-                constexpr int r = decltype(rc)::value;
-                t[r] = x[OFF + m + M * r];
-            });
-            small_dft<R, DIR>(t);
-            sfor<0, R>([&](auto sc) {
-                constexpr int s = decltype(sc)::value;
-                x[OFF + m + M * s] = twmul<DIR, (long)m * s, L>(t[s]);
-            });
+        sfor<0, R>([&](auto rc) {
+            constexpr int r = decltype(rc)::value;
+            dit<M, OFF + r * M, DIR>(x);
         });
-        sfor<0, R>([&](auto sc) {
-            constexpr int s = decltype(sc)::value;
-            dif<M, OFF + M * s, DIR>(x);
+        sfor<0, M>([&](auto kc) {
+            constexpr int k = decltype(kc)::value;
+            if constexpr (R == 4) {
+                float2 t0, t1, t2, t3;
+                tw_pair<DIR, 2L * k, L>(x[OFF + k], x[OFF + k + 2 * M], t0, t1);
+                const float2 a1 = twmul<DIR, (long)k, L>(x[OFF + k + M]);
+                tw_pair<DIR, 3L * k, L>(a1, x[OFF + k + 3 * M], t2, t3);
+                const float2 r3 = mul_i<DIR>(t3);
+                x[OFF + k] = cadd(t0, t2);
+                x[OFF + k + 2 * M] = csub(t0, t2);
+                x[OFF + k + M] = cadd_s(t1, r3);
+                x[OFF + k + 3 * M] = csub_s(t1, r3);
+            } else if constexpr (R == 2) {
+                float2 t0, t1;
+                tw_pair<DIR, (long)k, L>(x[OFF + k], x[OFF + k + M], t0, t1);
+                x[OFF + k] = t0;
+                x[OFF + k + M] = t1;
+            } else {
+                float2 t[R];
+                t[0] = x[OFF + k];
+                sfor<1, R>([&](auto rc) {
+                    constexpr int r = decltype(rc)::value;
+                    t[r] = twmul<DIR, (long)r * k, L>(x[OFF + k + r * M]);
+                });
+                small_dft<R, DIR>(t);
+                sfor<0, R>([&](auto sc) {
+                    constexpr int s = decltype(sc)::value;
+                    x[OFF + k + s * M] = t[s];
+                });
+            }
         });
     }
 }
+
+// The transform the window kernel uses: input n at x[fft_in<L>(n)], output
+// k at x[fft_out<L>(k)].
+template <int L>
+constexpr int fft_in(int n) { return dit_in<L>(n); }
+template <int L>
+constexpr int fft_out(int k) { return k; }
+template <int L, int OFF, int DIR>
+FLCT_HD void fft(float2* x) { dit<L, OFF, DIR>(x); }
 
 }  // namespace flct

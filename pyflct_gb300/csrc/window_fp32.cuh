@@ -145,16 +145,17 @@ k_window_fp32(WinArgs a) {
             const float2* p2 = f2s + (size_t)imin * ny + jmin + ln;
             const float* gr = a.gauss + (imin - i + N);  // row weights: uniform, from the parameter bank
             float mx1 = 0.f, mx2 = 0.f;
-#pragma unroll
-            for (int ii = 0; ii < N; ++ii) {
+            sfor<0, N>([&](auto ic) {
+                constexpr int ii = decltype(ic)::value;
                 // (hi - mean hi) + (lo - mean lo), the hi and lo halves packed
                 const float2 u = csub(__ldg(p1 + (size_t)ii * ny), m1);
                 const float2 v = csub(__ldg(p2 + (size_t)ii * ny), m2);
                 const float wgt = wc * gr[ii];
-                x[ii] = make_float2(wgt * (u.x + u.y), wgt * (v.x + v.y));
-                mx1 = fmaxf(mx1, fabsf(x[ii].x));
-                mx2 = fmaxf(mx2, fabsf(x[ii].y));
-            }
+                const float2 z = make_float2(wgt * (u.x + u.y), wgt * (v.x + v.y));
+                x[fft_in<N>(ii)] = z;  // row ii where the column transform takes it
+                mx1 = fmaxf(mx1, fabsf(z.x));
+                mx2 = fmaxf(mx2, fabsf(z.y));
+            });
             unsigned b1, b2;
             if constexpr (kWarp) {
                 b1 = __reduce_max_sync(tmask, __float_as_uint(mx1));
@@ -178,10 +179,10 @@ k_window_fp32(WinArgs a) {
         }
 
         // forward 2-D FFT: columns in registers, transpose, rows in registers
-        dif<N, 0, -1>(x);
+        fft<N, 0, -1>(x);
         sfor<0, N>([&](auto kc) {
             constexpr int k = decltype(kc)::value;
-            buf[k * (N + 1) + ln] = x[dif_pos<N>(k)];
+            buf[k * (N + 1) + ln] = x[fft_out<N>(k)];
         });
         team_sync();
         if constexpr (!kWarp) {
@@ -195,14 +196,14 @@ k_window_fp32(WinArgs a) {
         }
         sfor<0, N>([&](auto jc) {
             constexpr int jj = decltype(jc)::value;
-            x[jj] = buf[ln * (N + 1) + jj];
+            x[fft_in<N>(jj)] = buf[ln * (N + 1) + jj];
         });
         if constexpr (!kWarp) team_sync();
-        dif<N, 0, -1>(x);  // thread ln now holds Z[kx = ln][ky]
+        fft<N, 0, -1>(x);  // thread ln now holds Z[kx = ln][ky] at x[fft_out<N>(ky)]
         if constexpr (!kWarp) {
             sfor<0, N>([&](auto kc) {
                 constexpr int k = decltype(kc)::value;
-                buf[ln * (N + 1) + k] = x[dif_pos<N>(k)];
+                buf[ln * (N + 1) + k] = x[fft_out<N>(k)];
             });
             team_sync();
         }
@@ -225,11 +226,11 @@ k_window_fp32(WinArgs a) {
             sfor<0, KC>([&](auto kc) {
                 constexpr int k = decltype(kc)::value;
                 constexpr int mk = (N - k) % N;
-                const float2 z = x[dif_pos<N>(k)];
+                const float2 z = x[fft_out<N>(k)];
                 float2 zm;
                 if constexpr (kWarp) {
-                    zm.x = __shfl_sync(tmask, x[dif_pos<N>(mk)].x, mr, N);
-                    zm.y = __shfl_sync(tmask, x[dif_pos<N>(mk)].y, mr, N);
+                    zm.x = __shfl_sync(tmask, x[fft_out<N>(mk)].x, mr, N);
+                    zm.y = __shfl_sync(tmask, x[fft_out<N>(mk)].y, mr, N);
                 } else {
                     zm = buf[mr * (N + 1) + mk];
                 }
@@ -277,9 +278,9 @@ k_window_fp32(WinArgs a) {
             const float2 ak = cadd(y[k], y[k + H]);
             const float2 dk = csub(y[k], y[k + H]);
             // + i w^k dk = dk e^{2 pi i (4k + N) / 4N}
-            u[k] = tw_add<+1, 4L * k + N, 4L * N>(ak, dk);
+            u[fft_in<H>(k)] = tw_fma_add<+1, 4L * k + N, 4L * N>(ak, dk);
         });
-        dif<H, 0, +1>(u);  // u[dif_pos<H>(m)] = row kx = ln, column m
+        fft<H, 0, +1>(u);  // u[fft_out<H>(m)] = row kx = ln, column m
         // Columns (kx -> i), split by the parity h of i over two lanes: with
         // P0 = Y and P1 = Y w^kx stored side by side, lane (m, h) transforms
         // P_h[kx'] + P_h[kx' + H] (kx' < H), which is the first radix-2 stage
@@ -289,7 +290,7 @@ k_window_fp32(WinArgs a) {
             const float2 tw = s_tw[ln];
             sfor<0, H>([&](auto mc) {
                 constexpr int m = decltype(mc)::value;
-                const float2 v = u[dif_pos<H>(m)];
+                const float2 v = u[fft_out<H>(m)];
                 buf[ln * (N + 1) + m] = v;
                 buf[ln * (N + 1) + H + m] = make_float2(v.x * tw.x - v.y * tw.y, v.x * tw.y + v.y * tw.x);
             });
@@ -298,9 +299,9 @@ k_window_fp32(WinArgs a) {
         const int cm = ln % H, ch = ln / H;
         sfor<0, H>([&](auto kc) {
             constexpr int k = decltype(kc)::value;
-            u[k] = cadd(buf[k * (N + 1) + ch * H + cm], buf[(k + H) * (N + 1) + ch * H + cm]);
+            u[fft_in<H>(k)] = cadd(buf[k * (N + 1) + ch * H + cm], buf[(k + H) * (N + 1) + ch * H + cm]);
         });
-        dif<H, 0, +1>(u);  // u[dif_pos<H>(i')] = c[2i'+h][2m] + i c[2i'+h][2m+1]
+        fft<H, 0, +1>(u);  // u[fft_out<H>(i')] = c[2i'+h][2m] + i c[2i'+h][2m+1]
         team_sync();  // |c| overwrites the transform buffer
 
         unsigned long long key;  // max over the team of (|c|, -index)
@@ -314,7 +315,7 @@ k_window_fp32(WinArgs a) {
             sfor<0, H>([&](auto Ic) {
                 constexpr int I2 = decltype(Ic)::value;
                 constexpr int ip = (I2 + H / 2) % H;
-                const float2 c = u[dif_pos<H>(ip)];
+                const float2 c = u[fft_out<H>(ip)];
                 const float v0 = fabsf(c.x), v1 = fabsf(c.y);
                 *reinterpret_cast<float2*>(ab + (2 * I2 + ch) * N + J) = make_float2(v0, v1);
                 if (v0 > bv) {
