@@ -565,8 +565,14 @@ JobSizes job_sizes(const Job& j) {
 // float split, the work list (b.work / b.ctr: the windows of those rows)
 // and the final values of pixels without a window (flct.c:684-755).
 flct_status enqueue_classify(flct_ctx* ctx, const Job& j, const JobBufs& b, int r0, int r1, const double* d_thr,
-                             cudaStream_t st, int* launches, int blocks_per_sm = 8) {
+                             cudaStream_t st, int* launches, int blocks_per_sm = 8, const JobBufs* b2 = nullptr,
+                             int rsplit = 0) {
     ClassifyArgs ca{};
+    if (b2) {  // windows of rows >= rsplit to b2's list
+        ca.work2 = b2->work;
+        ca.nwork2 = (int*)b2->ctr;
+        ca.rsplit = rsplit;
+    }
     ca.f1 = j.f1;
     ca.f2 = j.f2;
     ca.nx = j.nx;
@@ -1352,15 +1358,19 @@ flct_status enqueue_device_tail(flct_ctx* ctx, const Job& j, const JobBufs& b, i
 
 // ------------------------------------------------ banded host calls --
 
-// Row bands of a host-buffer call.  Band b classifies pixel rows
-// [R[b], R[b+1]) (its windows are the grid rows [Q[b], Q[b+1])) and
-// completes output rows [O[b], O[b+1]).  Its box sums and windows read
-// input rows up to a box below the band, so a band must be taller than a
-// box; the interpolation of an output row reads two grid rows below it, so
-// O[b+1] trails Q[b+1] by two.
+// Row bands of a host-buffer call.  Band b owns pixel rows [R[b], R[b+1])
+// (its windows are the grid rows [Q[b], Q[b+1])) and completes output rows
+// [O[b], O[b+1]).  Its box sums and windows read input rows up to C[b+1],
+// the end of its last grid row's box, so the input is copied, classified
+// and row-summed in chunks [C[b], C[b+1]): band b can start as soon as
+// chunk b has arrived.  A chunk's windows go to the work list of the band
+// that owns their row (chunk b spans bands b and b + 1), so a band must be
+// taller than a box; the interpolation of an output row reads two grid
+// rows below it, so O[b+1] trails Q[b+1] by two.
 struct Bands {
     int nb = 0;
     int R[flct_ctx::kMaxBands + 1], Q[flct_ctx::kMaxBands + 1], O[flct_ctx::kMaxBands + 1];
+    int C[flct_ctx::kMaxBands + 1];
 };
 
 bool plan_bands(const flct_ctx* ctx, const Job& j, Bands* bd) {
@@ -1375,12 +1385,15 @@ bool plan_bands(const flct_ctx* ctx, const Job& j, Bands* bd) {
         bd->O[nb] = j.nx;
         for (int b = 1; b < nb; ++b)
             bd->O[b] = j.interp ? std::min(std::max(j.xo + (bd->Q[b] - 2) * j.gs, bd->O[b - 1]), j.nx) : bd->R[b];
+        bd->C[0] = 0;
+        bd->C[nb] = j.nx;
         for (int b = 0; b < nb && ok; ++b) {
             if (bd->Q[b + 1] <= bd->Q[b]) ok = false;
             // input rows the band's box sums and windows read lie in bands <= b + 1
             const int last = j.xo + (bd->Q[b + 1] - 1) * j.gs;
             const int need = box_start(last, j.nx, j.d.nsize) + j.n;
             if (b + 2 <= nb && need > bd->R[b + 2]) ok = false;
+            if (b + 1 < nb) bd->C[b + 1] = std::min(std::max(need, bd->R[b + 1]), j.nx);
         }
         if (ok) {
             bd->nb = nb;
@@ -1458,43 +1471,45 @@ flct_status enqueue_banded(flct_ctx* ctx, const Job& j, const Bands& bd, int for
     double *d_f1 = (double*)j.f1, *d_f2 = (double*)j.f2;
     CK(cudaEventRecord(ctx->hev[kFork], st));
     for (cudaStream_t x : {cin, cout, pc, pr, pb}) CK(cudaStreamWaitEvent(x, ctx->hev[kFork], 0));
+    // input chunk b = rows [C[b], C[b+1]): everything band b's box sums and
+    // windows read beyond the chunks before it
     for (int b = 0; b < nb; ++b) {
-        const size_t o = (size_t)bd.R[b] * ny, len = (size_t)(bd.R[b + 1] - bd.R[b]) * ny * sizeof(double);
-        CK(cudaMemcpyAsync(d_f1 + o, f1 + o, len, cudaMemcpyHostToDevice, cin));
-        CK(cudaMemcpyAsync(d_f2 + o, f2 + o, len, cudaMemcpyHostToDevice, cin));
+        const size_t o = (size_t)bd.C[b] * ny, len = (size_t)(bd.C[b + 1] - bd.C[b]) * ny * sizeof(double);
+        if (len) {
+            CK(cudaMemcpyAsync(d_f1 + o, f1 + o, len, cudaMemcpyHostToDevice, cin));
+            CK(cudaMemcpyAsync(d_f2 + o, f2 + o, len, cudaMemcpyHostToDevice, cin));
+        }
         CK(cudaEventRecord(ctx->hev[b], cin));
     }
     int launches = 0;
     WinArgs wa;
     make_wargs(j, base, &wa);
-    // the prepass runs a band ahead of the windows: band b's box sums (and
-    // windows) read input rows of band b + 1, so its column sums follow
-    // that band's row sums; the classification of a band and its row sums
-    // both read only the band's copied-in rows
+    // the prepass follows the chunks: chunk b's classification (its windows
+    // to the lists of bands b and b + 1, split at R[b+1]) and row sums as
+    // soon as it arrives, then band b's column sums, whose rows are all in
+    // chunks <= b
     CK(cudaMemsetAsync(ctx->b_ctr.p, 0, 64 * nb, pc));
     flct_status s = FLCT_OK;
-    for (int b = 0; b <= nb && s == FLCT_OK; ++b) {
-        if (b < nb) {
-            CK(cudaStreamWaitEvent(pc, ctx->hev[b], 0));
-            CK(cudaStreamWaitEvent(pr, ctx->hev[b], 0));
-            s = enqueue_box_rows(ctx, j, base, bd.R[b], bd.R[b + 1], pr, &launches);
-            if (s == FLCT_OK) s = enqueue_classify(ctx, j, bb[b], bd.R[b], bd.R[b + 1], nullptr, pc, &launches);
-            if (s != FLCT_OK) break;
-            CK(cudaEventRecord(ctx->hev[kR + b], pr));
-            CK(cudaEventRecord(ctx->hev[kK + b], pc));
-        }
-        if (b > 0) {
-            CK(cudaStreamWaitEvent(pb, ctx->hev[kR + std::min(b, nb - 1)], 0));
-            s = enqueue_box_cols(ctx, j, base, bd.Q[b - 1], bd.Q[b], pb, &launches);
-            CK(cudaEventRecord(ctx->hev[kP + b - 1], pb));
-        }
+    for (int b = 0; b < nb && s == FLCT_OK; ++b) {
+        CK(cudaStreamWaitEvent(pc, ctx->hev[b], 0));
+        CK(cudaStreamWaitEvent(pr, ctx->hev[b], 0));
+        s = enqueue_box_rows(ctx, j, base, bd.C[b], bd.C[b + 1], pr, &launches);
+        if (s == FLCT_OK && bd.C[b + 1] > bd.C[b])
+            s = enqueue_classify(ctx, j, bb[b], bd.C[b], bd.C[b + 1], nullptr, pc, &launches, 8,
+                                 b + 1 < nb ? &bb[b + 1] : nullptr, bd.R[b + 1]);
+        if (s != FLCT_OK) break;
+        CK(cudaEventRecord(ctx->hev[kR + b], pr));
+        CK(cudaEventRecord(ctx->hev[kK + b], pc));
+        CK(cudaStreamWaitEvent(pb, ctx->hev[kR + b], 0));
+        s = enqueue_box_cols(ctx, j, base, bd.Q[b], bd.Q[b + 1], pb, &launches);
+        CK(cudaEventRecord(ctx->hev[kP + b], pb));
     }
     for (int b = 0; b < nb && s == FLCT_OK; ++b) {
         cudaStream_t sb = bs[b];
-        // the band's box sums; the float split of its rows and of the rows
-        // below it that its windows read (the next band's classification)
+        // the band's box sums, its work list and the float split of every
+        // row its windows read: chunks <= b
         CK(cudaStreamWaitEvent(sb, ctx->hev[kP + b], 0));
-        CK(cudaStreamWaitEvent(sb, ctx->hev[kK + std::min(b + 1, nb - 1)], 0));
+        CK(cudaStreamWaitEvent(sb, ctx->hev[kK + b], 0));
         // the band's windows: at most its grid points
         const long items = (long)(bd.Q[b + 1] - bd.Q[b]) * j.gj;
         s = enqueue_means(ctx, j, bb[b], items, sb, &launches);

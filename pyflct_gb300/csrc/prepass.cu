@@ -143,6 +143,9 @@ __global__ void __launch_bounds__(256) k_classify(ClassifyArgs a) {
         }
         const unsigned m = __ballot_sync(0xffffffffu, comp);
         if (lane == 0) s_cnt[warp] = __popc(m);
+        // a tile is one row: its windows go to one list
+        const bool second = a.work2 && i >= a.rsplit;
+        int* const wl = second ? a.work2 : a.work;
         __syncthreads();
         if (threadIdx.x == 0) {
             int tot = 0;
@@ -152,11 +155,11 @@ __global__ void __launch_bounds__(256) k_classify(ClassifyArgs a) {
                 s_cnt[w] = tot;
                 tot += c;
             }
-            s_base = tot ? atomicAdd(a.nwork, tot) : 0;
+            s_base = tot ? atomicAdd(second ? a.nwork2 : a.nwork, tot) : 0;
         }
         __syncthreads();
         if (comp) {
-            a.work[s_base + s_cnt[warp] + __popc(m & ((1u << lane) - 1u))] = (int)k;
+            wl[s_base + s_cnt[warp] + __popc(m & ((1u << lane) - 1u))] = (int)k;
         } else if (act) {
             // pixels without a window: (xmiss, xmiss, 0) then the reset gives
             // (0, 0, 0); skipped pixels that will be interpolated are left to

@@ -20,6 +20,9 @@ struct ClassifyArgs {
     float2* grid;             // skip-grid (vx, vy) for the interpolation, or null
     unsigned* status;
     int r0, r1;               // rows to classify (the work list gets their windows)
+    int* work2;               // when set: windows of rows >= rsplit go to this list
+    int* nwork2;
+    int rsplit;
 };
 
 // Row pass of the box sums: warps per block, and the longest input span a
