@@ -626,7 +626,7 @@ BoxArgs box_args(const Job& j, const JobBufs& b) {
 
 // Exact row sums of frame rows [r0, r1) at the grid's box columns.
 flct_status enqueue_box_rows(flct_ctx* ctx, const Job& j, const JobBufs& b, int r0, int r1, cudaStream_t st,
-                             int* launches) {
+                             int* launches, int blocks_per_sm = 4) {
     if (r1 <= r0) return FLCT_OK;
     BoxArgs ba = box_args(j, b);
     ba.r0 = r0;
@@ -639,7 +639,7 @@ flct_status enqueue_box_rows(flct_ctx* ctx, const Job& j, const JobBufs& b, int 
         CK(cudaFuncSetAttribute(k_box_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         ctx->box_attr = true;
     }
-    const long blocks = std::min<long>((tasks + kBoxWarps - 1) / kBoxWarps, (long)ctx->nsm * 4);
+    const long blocks = std::min<long>((tasks + kBoxWarps - 1) / kBoxWarps, (long)ctx->nsm * blocks_per_sm);
     k_box_rows<<<(int)std::max(1l, blocks), kBoxWarps * 32, smem, st>>>(ba);
     ++*launches;
     CK(cudaGetLastError());
@@ -1502,18 +1502,21 @@ flct_status enqueue_banded(flct_ctx* ctx, const Job& j, const Bands& bd, int for
         CK(cudaEventRecord(ctx->hev[kK + b], pc));
         CK(cudaStreamWaitEvent(pb, ctx->hev[kR + b], 0));
         s = enqueue_box_cols(ctx, j, base, bd.Q[b], bd.Q[b + 1], pb, &launches);
+        // the band's means at the prepass priority too (on a band stream
+        // they waited behind the next chunks' prepass): they need its box
+        // sums and its complete work list (chunk b's classification)
+        CK(cudaStreamWaitEvent(pb, ctx->hev[kK + b], 0));
+        if (s == FLCT_OK) s = enqueue_means(ctx, j, bb[b], (long)(bd.Q[b + 1] - bd.Q[b]) * j.gj, pb, &launches);
         CK(cudaEventRecord(ctx->hev[kP + b], pb));
     }
     for (int b = 0; b < nb && s == FLCT_OK; ++b) {
         cudaStream_t sb = bs[b];
-        // the band's box sums, its work list and the float split of every
-        // row its windows read: chunks <= b
+        // the band's means (after its box sums and work list), and the
+        // float split of every row its windows read: chunks <= b
         CK(cudaStreamWaitEvent(sb, ctx->hev[kP + b], 0));
         CK(cudaStreamWaitEvent(sb, ctx->hev[kK + b], 0));
         // the band's windows: at most its grid points
         const long items = (long)(bd.Q[b + 1] - bd.Q[b]) * j.gj;
-        s = enqueue_means(ctx, j, bb[b], items, sb, &launches);
-        if (s != FLCT_OK) break;
         WinArgs wb = wa;
         wb.means = bb[b].means;
         wb.work = bb[b].work;
