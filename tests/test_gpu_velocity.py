@@ -430,3 +430,66 @@ def test_host_bands_match_one_band(shape, sigma, extra, monkeypatch):
         assert nwin == nref, (nb, nwin, nref)
         for a, b in zip(got, ref):
             assert np.array_equal(a, b), (nb, np.abs(a - b).max())
+
+
+def test_status_word_reaches_the_host_on_every_path(monkeypatch):
+    """The device sets the status word's range bit for a finite input beyond
+    the FP32 range; the last kernel of a call copies the status to mapped
+    host memory.  Every call path reports it as FLCT_ERR_UNSUPPORTED: device
+    buffers (eager, captured, replayed), host buffers page-locked (banded,
+    replayed graph) and in one band, and pageable buffers; the same context
+    then computes a clean frame with the right window count."""
+    import ctypes as C
+    import torch
+    from pyflct_gb300 import _lib, synth
+    from pyflct_gb300.flct import make_params
+    shape = (256, 256)
+    rng = np.random.default_rng(99)
+    good1 = synth.kfield(shape, rng)
+    good2 = synth.fourier_shift(good1, 0.3, -0.2)
+    bad1 = good1.copy()
+    bad1[100, 120] = 1e39
+    p = make_params(1.0, 1.0, 4.0, skip="4i")
+
+    def run_host(ctx, f1, f2, pinned):
+        if pinned:
+            buf = [torch.empty(shape, dtype=torch.float64, pin_memory=True) for _ in range(5)]
+            buf[0].copy_(torch.from_numpy(f1))
+            buf[1].copy_(torch.from_numpy(f2))
+            ptr = [C.cast(C.c_void_p(x.data_ptr()), C.POINTER(C.c_double)) for x in buf]
+            out = buf[2:]
+        else:
+            arrs = [np.ascontiguousarray(f1), np.ascontiguousarray(f2)] + [np.zeros(shape) for _ in range(3)]
+            ptr = [a.ctypes.data_as(C.POINTER(C.c_double)) for a in arrs]
+            out = arrs[2:]
+        rc = ctx.lib.flct_gpu_velocity(ctx.h, C.byref(p), ptr[0], ptr[1], shape[0], shape[1], *ptr[2:])
+        return rc, out
+
+    for nb in ("4", "0"):
+        monkeypatch.setenv("FLCT_HOST_BANDS", nb)
+        ctx = _lib.Context(0)
+        for pinned in (True, False):
+            for _ in range(3):  # the second page-locked call captures, the third replays
+                rc, _ = run_host(ctx, bad1, good2, pinned)
+                assert rc == _lib.ERR_UNSUPPORTED, (nb, pinned, rc)
+            rc, out = run_host(ctx, good1, good2, pinned)
+            assert rc == _lib.OK, (nb, pinned, rc)
+            vm = np.asarray(out[2])
+            assert ctx.timing().windows == int((vm == 1).sum()) > 0
+        # device buffers: eager, captured, replayed
+        dev = torch.device("cuda", 0)
+        d_bad, d_good = torch.from_numpy(bad1).to(dev), torch.from_numpy(good1).to(dev)
+        d2 = torch.from_numpy(good2).to(dev)
+        outs = [torch.empty(shape, dtype=torch.float64, device=dev) for _ in range(3)]
+        optr = [C.c_void_p(o.data_ptr()) for o in outs]
+        for _ in range(4):
+            ctx.check(ctx.lib.flct_gpu_velocity_device(ctx.h, C.byref(p), C.c_void_p(d_bad.data_ptr()),
+                                                       C.c_void_p(d2.data_ptr()), shape[0], shape[1], *optr, None))
+            t = _lib.Timing()
+            assert ctx.lib.flct_gpu_last_timing(ctx.h, C.byref(t)) == _lib.ERR_UNSUPPORTED
+        for _ in range(3):
+            ctx.check(ctx.lib.flct_gpu_velocity_device(ctx.h, C.byref(p), C.c_void_p(d_good.data_ptr()),
+                                                       C.c_void_p(d2.data_ptr()), shape[0], shape[1], *optr, None))
+            t = ctx.timing()
+            assert t.windows == int((outs[2] == 1).sum().item()) > 0
+        ctx.close()
