@@ -16,6 +16,9 @@ value  = correlation windows per second with inputs resident in HBM
 e2e    = the same metric through flct_gpu_velocity with pinned host
          buffers: both input frames copied in and vx, vy, vm copied out
          every step.
+Beside the headline line's keys: the 64-pair heterogeneous batch
+(batch_64_pairs) and the warp entry points' Mpixel/s at 512^2 (warp_512);
+--no-batch skips both.
 """
 from __future__ import annotations
 
@@ -218,6 +221,32 @@ def run_batch(a, dev, flush):
             "note": "inputs resident in HBM (179 MB > L2), L2 flushed between steps, form auto"}
 
 
+def run_warp(a, dev):
+    """The warp entry points on a 512^2 k^-2 field (the crop size the
+    large-frame configuration checks the warp on): shift_frac2d with one
+    uniform shift and warp_frac2d with a smooth per-pixel displacement
+    (RMS 0.3 px), Mpixel/s per call through the host-buffer C ABI (copies
+    included; the spectral warp is O(N^2) per pixel, so it dominates)."""
+    from pyflct_gb300 import synth
+    from pyflct_gb300.flct import shift_frac2d, warp_frac2d
+    rng = np.random.default_rng(20265)
+    img = synth.kfield((512, 512), rng)
+    dfast, dslow = synth.smooth_shift(img.shape, rng, rms=0.3)
+    out = {}
+    for name, fn in (("shift_frac2d", lambda: shift_frac2d(img, 0.37, -2.6, device=dev.index or 0)),
+                     ("warp_frac2d", lambda: warp_frac2d(img, dfast, dslow, device=dev.index or 0))):
+        fn()
+        reps = 3
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        dt = (time.perf_counter() - t0) / reps
+        out[name] = {"mpix_s": img.size / dt / 1e6, "ms_per_call": dt * 1e3}
+    out["size"] = list(img.shape)
+    out["note"] = "host buffers in and out, wall clock per call"
+    return out
+
+
 def run_ours(a):
     import torch
     from pyflct_gb300 import _lib
@@ -323,6 +352,7 @@ def run_ours(a):
     e2e_val = windows * a.steps * ws / max(1e-9, reduce_max(e2e_s - flush_s, dev))
 
     batch = None if a.no_batch else run_batch(a, dev, flush)
+    warp = None if (a.no_batch or rank != 0) else run_warp(a, dev)
 
     if rank != 0:
         if ws > 1:
@@ -399,6 +429,7 @@ def run_ours(a):
         "forms": {f: {"value": r["value"], "ms_per_step": r["ms_per_step"], "window_ms": r["window_ms"],
                       "used": r["used"]} for f, r in res.items()},
         "batch_64_pairs": batch,
+        "warp_512": warp,
         "cpu_baseline": cpu,
         "accuracy_vs_fp64_oracle": acc,
         "gpu_launches": launches * a.steps,
@@ -421,7 +452,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--form", default="auto", choices=["auto", "fp32", "tc_fp16", "tc_bf16"])
-    ap.add_argument("--no-batch", action="store_true", help="skip the 64-pair batched workload")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 64-pair batched workload and the warp timing")
     ap.add_argument("--only", action="store_true", help="time only --form (skip the other forms)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the oracle accuracy and CPU baseline")
     a = ap.parse_args()
