@@ -493,3 +493,40 @@ def test_status_word_reaches_the_host_on_every_path(monkeypatch):
             t = ctx.timing()
             assert t.windows == int((outs[2] == 1).sum().item()) > 0
         ctx.close()
+
+
+@pytest.mark.parametrize("shape", [(257, 300), (240, 333)])
+def test_interpolation_output_alignment(shape):
+    """The interpolation writes pixel pairs as 16-byte stores only when ny is
+    even and the outputs are 16-byte aligned; outputs that start 8 bytes off
+    a 16-byte boundary, and odd ny, take the one-pixel stores and give the
+    same fields as aligned outputs."""
+    import ctypes as C
+    import torch
+    from pyflct_gb300 import _lib, synth
+    from pyflct_gb300.flct import make_params
+    rng = np.random.default_rng(sum(shape))
+    f1 = synth.kfield(shape, rng)
+    f2 = synth.fourier_shift(f1, 0.4, -0.3)
+    ctx = _lib.context(0)
+    p = make_params(1.0, 1.0, 5.0, skip="3p1q2i")
+    dev = torch.device("cuda", 0)
+    d1, d2 = torch.from_numpy(f1).to(dev), torch.from_numpy(f2).to(dev)
+    n = shape[0] * shape[1]
+    results = []
+    for off in (0, 1):  # element offset into a larger buffer: 0 aligned, 1 = 8 bytes off
+        raw = [torch.full((n + 2,), -9.0, dtype=torch.float64, device=dev) for _ in range(3)]
+        outs = [r[off:off + n] for r in raw]
+        assert all(o.data_ptr() % 16 == 8 * off for o in outs)
+        ctx.check(ctx.lib.flct_gpu_velocity_device(ctx.h, C.byref(p), C.c_void_p(d1.data_ptr()),
+                                                   C.c_void_p(d2.data_ptr()), shape[0], shape[1],
+                                                   *[C.c_void_p(o.data_ptr()) for o in outs], None))
+        ctx.timing()
+        results.append([o.cpu().numpy().reshape(shape) for o in outs])
+        # nothing written outside the outputs
+        for r in raw:
+            rr = r.cpu().numpy()
+            assert (rr[:off] == -9.0).all() and (rr[off + n:] == -9.0).all()
+    for a, b in zip(*results):
+        assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
+    assert (results[0][2] == 0.5).sum() > 0  # interpolated pixels present
