@@ -63,15 +63,16 @@ __device__ __forceinline__ void fx_accum(double x, int ee, unsigned (&acc)[4], u
     const unsigned mh = (bh & 0xfffffu) | (e ? 0x100000u : 0u);
     int t = min((e ? e : 1) - ee + 126, 126);  // shift in the window; < 0: below the unit
     if (nf) t = -1;
-    const int q = t >> 5;
+    const int q = t >> 5;  // -1 .. 3
     const unsigned r = (unsigned)t & 31u;
     const unsigned t0 = bl << r, t1 = __funnelshift_l(bl, mh, r), t2 = __funnelshift_l(mh, 0u, r);
+    // t0, t1, t2 sit at window words q, q + 1, q + 2; the value is words 2..5
+    const bool q3 = q == 3, q2 = q == 2, q1 = q == 1, q0 = q == 0;
     unsigned w[4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        const int k = j + 2 - q;  // t0, t1, t2 sit at window words q, q + 1, q + 2
-        w[j] = (k == 0) ? t0 : (k == 1) ? t1 : (k == 2) ? t2 : 0u;
-    }
+    w[0] = q2 ? t0 : q1 ? t1 : q0 ? t2 : 0u;
+    w[1] = q3 ? t0 : q2 ? t1 : q1 ? t2 : 0u;
+    w[2] = q3 ? t1 : q2 ? t2 : 0u;
+    w[3] = q3 ? t2 : 0u;
     const unsigned sg = (unsigned)((int)bh >> 31);
     asm("{\n.reg .u32 c;\n"
         "add.cc.u32 c, %4, 0xffffffff;\n"
