@@ -145,6 +145,10 @@ struct flct_ctx {
     cudaEvent_t hev[6 * kMaxBands + 2] = {};
     // the device call's classification fork and join
     cudaEvent_t pev[2] = {};
+    // the captured device call's stage events branch off its kernel chain
+    // on this stream (fork and join events)
+    cudaStream_t tstream = nullptr;
+    cudaEvent_t tfork = nullptr, tjoin = nullptr;
     // the last banded call with page-locked buffers, captured as a graph
     cudaGraphExec_t hexec = nullptr;
     std::vector<unsigned char> hkey;
@@ -1328,31 +1332,47 @@ flct_status rebuild_batch(flct_ctx* ctx, int npairs, const flct_pair* pairs, cud
 // page-locked memory.
 flct_status enqueue_device_tail(flct_ctx* ctx, const Job& j, const JobBufs& b, int form, int grid_div,
                                 cudaStream_t st, bool graph, int* launches, bool from_start = false) {
-    const unsigned evf = graph ? cudaEventRecordExternal : cudaEventRecordDefault;
+    // Stage events.  Eager: plain records.  Captured: ev[0] and ev[3] are
+    // recorded on the caller's stream around the graph launch, and the
+    // others become external event nodes on a side branch off the kernel
+    // chain (a node inside the chain would delay the next kernel by its own
+    // latency, ~2 us each).
+    auto stamp = [&](cudaEvent_t ev) -> cudaError_t {
+        if (!graph) return cudaEventRecord(ev, st);
+        cudaError_t e = cudaEventRecord(ctx->tfork, st);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->tstream, ctx->tfork, 0);
+        if (e == cudaSuccess) e = cudaEventRecordWithFlags(ev, ctx->tstream, cudaEventRecordExternal);
+        return e;
+    };
     flct_status s = FLCT_OK;
     if (from_start) {
-        CK(cudaEventRecordWithFlags(ctx->ev[0], st, evf));
+        if (!graph) CK(cudaEventRecord(ctx->ev[0], st));
         s = enqueue_prepass(ctx, j, b, st, launches, ctx->prestream[0]);
         if (s != FLCT_OK) return s;
     }
     WinArgs wa;
     make_wargs(j, b, &wa);
-    CK(cudaEventRecordWithFlags(ctx->ev[1], st, evf));
+    CK(stamp(ctx->ev[1]));
     s = launch_windows(ctx, form, j.we, j.n, wa, (unsigned*)(b.ctr + 4), st, grid_div);
     if (s != FLCT_OK) return s;
     ++*launches;
-    CK(cudaEventRecordWithFlags(ctx->ev[2], st, evf));
+    CK(stamp(ctx->ev[2]));
     // the last kernel copies the work count and status to page-locked
     // memory; they are there once ev[3] completes
     const Pub pub{(const unsigned*)b.ctr, ctx->hctr_dev};
     s = enqueue_fit(ctx, j, b, st, launches, -1, j.interp ? Pub{} : pub);
     if (s != FLCT_OK) return s;
-    CK(cudaEventRecordWithFlags(ctx->ev[7], st, evf));
+    CK(stamp(ctx->ev[7]));
     if (j.interp) {
         s = enqueue_interp(ctx, j, b, st, launches, 0, -1, pub);
         if (s != FLCT_OK) return s;
     }
-    CK(cudaEventRecordWithFlags(ctx->ev[3], st, evf));
+    if (graph) {  // the side branch joins the chain's end
+        CK(cudaEventRecord(ctx->tjoin, ctx->tstream));
+        CK(cudaStreamWaitEvent(st, ctx->tjoin, 0));
+    } else {
+        CK(cudaEventRecord(ctx->ev[3], st));
+    }
     return FLCT_OK;
 }
 
@@ -1738,6 +1758,17 @@ flct_status flct_gpu_create(int device, flct_ctx** out) {
             flct_gpu_destroy(ctx);
             return FLCT_ERR_CUDA;
         }
+    for (auto* e : {&ctx->tfork, &ctx->tjoin})
+        if (cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess) {
+            *e = nullptr;
+            flct_gpu_destroy(ctx);
+            return FLCT_ERR_CUDA;
+        }
+    if (cudaStreamCreateWithFlags(&ctx->tstream, cudaStreamNonBlocking) != cudaSuccess) {
+        ctx->tstream = nullptr;
+        flct_gpu_destroy(ctx);
+        return FLCT_ERR_CUDA;
+    }
     if (const char* nb = getenv("FLCT_HOST_BANDS"))
         ctx->host_bands_max = std::max(0, std::min(flct_ctx::kMaxBands, atoi(nb)));
     if (cudaHostAlloc((void**)&ctx->hctr, 64 * flct_ctx::kMaxBands, cudaHostAllocMapped) != cudaSuccess) {
@@ -1767,6 +1798,7 @@ void flct_gpu_destroy(flct_ctx* ctx) {
         if (st) cudaStreamSynchronize(st);
     for (auto& st : ctx->prestream)
         if (st) cudaStreamSynchronize(st);
+    if (ctx->tstream) cudaStreamSynchronize(ctx->tstream);
     for (auto& st : ctx->bstream)
         if (st) cudaStreamSynchronize(st);
     if (ctx->bdone) cudaEventSynchronize(ctx->bdone);
@@ -1785,6 +1817,9 @@ void flct_gpu_destroy(flct_ctx* ctx) {
         if (e) cudaEventDestroy(e);
     for (auto& e : ctx->pev)
         if (e) cudaEventDestroy(e);
+    if (ctx->tfork) cudaEventDestroy(ctx->tfork);
+    if (ctx->tjoin) cudaEventDestroy(ctx->tjoin);
+    if (ctx->tstream) cudaStreamDestroy(ctx->tstream);
     for (auto& st : ctx->cstream)
         if (st) cudaStreamDestroy(st);
     for (auto& st : ctx->bandstream)
@@ -1910,7 +1945,9 @@ flct_status flct_gpu_velocity_device(flct_ctx* ctx, const flct_params* p, const 
             put(ptrs, sizeof(ptrs));
         }
         if (!key.empty() && ctx->dexec && key == ctx->dkey) {
+            CK(cudaEventRecord(ctx->ev[0], st));
             CK(cudaGraphLaunch(ctx->dexec, st));
+            CK(cudaEventRecord(ctx->ev[3], st));
             launches = ctx->dlaunches;
         } else if (!key.empty() && key == ctx->dlast) {
             if (ctx->dexec) {
@@ -1937,7 +1974,9 @@ flct_status flct_gpu_velocity_device(flct_ctx* ctx, const flct_params* p, const 
             }
             ctx->dkey = key;
             ctx->dlaunches = launches;
+            CK(cudaEventRecord(ctx->ev[0], st));
             CK(cudaGraphLaunch(ctx->dexec, st));
+            CK(cudaEventRecord(ctx->ev[3], st));
         } else {
             ctx->dlast = key;
             s = enqueue_device_tail(ctx, j, b, form, grid_div, st, false, &launches, true);
