@@ -68,11 +68,18 @@ __device__ __forceinline__ void fit3x3(const double* v, double* sx, double* sy) 
     *sy = dm(ds(dm(fxx, fy), dm(fx, fxy)), inv);
 }
 
+// Work items go to warps in 32-item chunks dealt round the blocks (chunk c
+// to block c mod gridDim), so every SM gets about the same number of fits:
+// the kernel is bound by each SM's FP64 pipe, and a plain grid-stride
+// mapping leaves the low blocks (and the SMs holding them) with the most.
 __global__ void k_fit(FitArgs a) {
     publish_counters(a.pub_src, a.pub_dst);
     const int nw = *a.nwork;
     const int half = a.n / 2, half1 = (a.n1 ? a.n1 : a.n) / 2;
-    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < nw; w += gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+    for (long c = blockIdx.x + (long)gridDim.x * (threadIdx.x >> 5); c * 32 < nw; c += (long)gridDim.x * wpb) {
+        const int w = (int)(c * 32) + lane;
+        if (w >= nw) continue;
         const PeakRec r = a.peaks[w];
         const int I = meta_I(r.meta), J = meta_J(r.meta);
         double sx = 0., sy = 0.;
