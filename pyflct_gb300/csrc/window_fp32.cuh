@@ -18,7 +18,10 @@
 // register FFTs along the other axis.  The correlation image is real, so the
 // inverse runs as one complex n x n/2 transform (even and odd output columns
 // as real and imaginary parts), half the work of a complex n x n one.  The
-// butterflies' complex adds use the packed FP32 pipe (fft_reg.cuh).  A
+// register transforms run by decimation in time with the twiddle products
+// fused into the butterflies' sums, exact adds on the packed FP32 pipe
+// (fft_reg.cuh), and C is formed for half the frequencies, the rest taken
+// from the mirror lane (C of a real image is Hermitian).  A
 // sub-image whose maximum is far from 1 is scaled by an exact power of two
 // so FP32 never over- or under-flows; scaling changes neither the argmax
 // nor the fit.
