@@ -88,7 +88,7 @@ typedef struct flct_ctx flct_ctx;
 /* Timing of the most recent compute call on a context (device time from
  * CUDA events on the context's stream). */
 typedef struct {
-    float ms_total;      /* first to last kernel of the call */
+    float ms_total;      /* the whole call on its stream, first to last operation */
     float ms_window;     /* the window-correlation kernel(s) */
     float ms_prepass;    /* threshold, mask, split and box-sum passes */
     float ms_interp;     /* skip-grid interpolation */
