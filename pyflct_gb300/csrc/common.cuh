@@ -68,6 +68,32 @@ __device__ __forceinline__ float2 split_double_fast(double x) {
     return make_float2(hi, lo);
 }
 
+// kern<<<grid, block, smem, st>>>(args...), launched as a programmatic
+// dependent of the stream's previous kernel when pdl is set (the kernel
+// then calls grid_dep_wait before it reads that kernel's results).
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_kernel(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                                 bool pdl, Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = pdl ? at : nullptr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kern, static_cast<Args&&>(args)...);
+}
+
+// A kernel launched as a programmatic dependent (its launch overlaps the
+// tail of the kernel before it on the stream) waits here until that kernel
+// has finished and its writes are visible; launched normally, this returns
+// at once.  Every kernel that may be so launched calls it before it reads
+// anything an earlier kernel wrote.
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // The call's work count and status word (final once this kernel starts: no
 // later kernel writes them) to mapped page-locked host memory, so that no
 // copy node ends the call.

@@ -36,7 +36,7 @@ constexpr double kTol = 1e-2;  // flct.c:278
 
 struct WinEntry {
     int n;
-    cudaError_t (*launch)(const WinArgs&, int, cudaStream_t);
+    cudaError_t (*launch)(const WinArgs&, int, cudaStream_t, bool);
     int (*bps)();
     int teams;  // windows per CTA iteration
 };
@@ -322,12 +322,12 @@ flct_status pick_form(flct_ctx* ctx, int requested, int n, int* form) {
 // instead of a persistent grid, so that CTAs retire often and kernels of
 // higher-priority streams get SMs in between (banded host calls).
 flct_status launch_windows(flct_ctx* ctx, int form, const WinEntry* we, int n, const WinArgs& wa, unsigned* status,
-                           cudaStream_t st, int grid_div = 1, long max_items = -1) {
+                           cudaStream_t st, int grid_div = 1, long max_items = -1, bool pdl = false) {
     if (grid_div < 1) grid_div = 1;
     if (form == FLCT_FORM_FP32) {
         int grid = std::max(ctx->nsm, win_grid(ctx, n) / grid_div);
         if (max_items >= 0) grid = (int)std::max<long>(1, (max_items + we->teams - 1) / we->teams);
-        CK(we->launch(wa, grid, st));
+        CK(we->launch(wa, grid, st, pdl));
         return FLCT_OK;
     }
     flct_status s = ensure_tc_tables(ctx);
@@ -668,7 +668,7 @@ flct_status enqueue_box_cols(flct_ctx* ctx, const Job& j, const JobBufs& b, int 
 // FP64 local means of the work list b.work / b.ctr (flct.c:815-827), one
 // window per lane.
 flct_status enqueue_means(flct_ctx* ctx, const Job& j, const JobBufs& b, long max_items, cudaStream_t st,
-                          int* launches) {
+                          int* launches, bool pdl = false) {
     MeansArgs ma{};
     ma.work = b.work;
     ma.nwork = (const int*)b.ctr;
@@ -682,7 +682,7 @@ flct_status enqueue_means(flct_ctx* ctx, const Job& j, const JobBufs& b, long ma
     ma.inv_n2 = 1. / ((double)j.n * j.n);
     ma.means = b.means;
     long blocks = std::min<long>((max_items + 255) / 256, (long)ctx->nsm * 8);
-    k_means<<<(int)std::max(1l, blocks), 256, 0, st>>>(ma);
+    CK(launch_kernel(k_means, dim3((unsigned)std::max(1l, blocks)), dim3(256), 0, st, pdl, ma));
     ++*launches;
     CK(cudaGetLastError());
     return FLCT_OK;
@@ -720,7 +720,8 @@ flct_status enqueue_prepass(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaS
         if (s == FLCT_OK) s = enqueue_box_rows(ctx, j, b, 0, j.nx, st, launches);
         if (s == FLCT_OK) s = enqueue_box_cols(ctx, j, b, 0, j.gi, st, launches);
     }
-    if (s == FLCT_OK) s = enqueue_means(ctx, j, b, (long)npx, st, launches);
+    // device calls (with a side stream): the means overlap the column sums' tail
+    if (s == FLCT_OK) s = enqueue_means(ctx, j, b, (long)npx, st, launches, side != nullptr);
     return s;
 }
 
@@ -748,7 +749,7 @@ struct Pub {
 };
 
 flct_status enqueue_fit(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaStream_t st, int* launches,
-                        long max_items = -1, Pub pub = Pub{}) {
+                        long max_items = -1, Pub pub = Pub{}, bool pdl = false) {
     FitArgs fa{};
     fa.pub_src = pub.src;
     fa.pub_dst = pub.dst;
@@ -770,10 +771,10 @@ flct_status enqueue_fit(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaStrea
     if (j.p->hires) {
         fa.peaks_h = b.peaks_h;
         long blocks = std::min<long>((long)(npx + 3) / 4, (long)ctx->nsm * 16);
-        k_fit_hires<<<(int)std::max(1l, blocks), 128, 0, st>>>(fa);
+        CK(launch_kernel(k_fit_hires, dim3((unsigned)std::max(1l, blocks)), dim3(128), 0, st, pdl, fa));
     } else {
         long blocks = std::min<long>((long)(npx + 127) / 128, (long)ctx->nsm * 8);
-        k_fit<<<(int)std::max(1l, blocks), 128, 0, st>>>(fa);
+        CK(launch_kernel(k_fit, dim3((unsigned)std::max(1l, blocks)), dim3(128), 0, st, pdl, fa));
     }
     ++*launches;
     CK(cudaGetLastError());
@@ -783,7 +784,7 @@ flct_status enqueue_fit(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaStrea
 // Cubic-convolution interpolation of the skip grid onto the skipped pixels,
 // mask and xmiss reset (flct.c:958-1133).
 flct_status enqueue_interp(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaStream_t st, int* launches,
-                           int i0 = 0, int i1 = -1, Pub pub = Pub{}) {
+                           int i0 = 0, int i1 = -1, Pub pub = Pub{}, bool pdl = false) {
     if (i1 < 0) i1 = j.nx;
     if (i1 <= i0) return FLCT_OK;
     InterpArgs ia{};
@@ -805,7 +806,8 @@ flct_status enqueue_interp(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaSt
     // pixel pairs (j even) start on 16-byte boundaries when ny is even
     ia.pairs = (j.ny % 2 == 0) && ((((uintptr_t)j.vx) | ((uintptr_t)j.vy) | ((uintptr_t)j.vm)) & 15u) == 0u;
     const long tiles = (long)((i1 - i0 + kTileR - 1) / kTileR) * ((j.ny + kTileC - 1) / kTileC);
-    k_interp_grid<<<(int)std::max(1l, std::min<long>(tiles, (long)ctx->nsm * 8)), kInterpThreads, 0, st>>>(ia);
+    CK(launch_kernel(k_interp_grid, dim3((unsigned)std::max(1l, std::min<long>(tiles, (long)ctx->nsm * 8))),
+                     dim3(kInterpThreads), 0, st, pdl, ia));
     ++*launches;
     CK(cudaGetLastError());
     return FLCT_OK;
@@ -1353,18 +1355,20 @@ flct_status enqueue_device_tail(flct_ctx* ctx, const Job& j, const JobBufs& b, i
     WinArgs wa;
     make_wargs(j, b, &wa);
     CK(stamp(ctx->ev[1]));
-    s = launch_windows(ctx, form, j.we, j.n, wa, (unsigned*)(b.ctr + 4), st, grid_div);
+    // the window, fit and interpolation kernels launch as programmatic
+    // dependents: each one's launch overlaps the tail of the kernel before it
+    s = launch_windows(ctx, form, j.we, j.n, wa, (unsigned*)(b.ctr + 4), st, grid_div, -1, true);
     if (s != FLCT_OK) return s;
     ++*launches;
     CK(stamp(ctx->ev[2]));
     // the last kernel copies the work count and status to page-locked
     // memory; they are there once ev[3] completes
     const Pub pub{(const unsigned*)b.ctr, ctx->hctr_dev};
-    s = enqueue_fit(ctx, j, b, st, launches, -1, j.interp ? Pub{} : pub);
+    s = enqueue_fit(ctx, j, b, st, launches, -1, j.interp ? Pub{} : pub, true);
     if (s != FLCT_OK) return s;
     CK(stamp(ctx->ev[7]));
     if (j.interp) {
-        s = enqueue_interp(ctx, j, b, st, launches, 0, -1, pub);
+        s = enqueue_interp(ctx, j, b, st, launches, 0, -1, pub, true);
         if (s != FLCT_OK) return s;
     }
     if (graph) {  // the side branch joins the chain's end

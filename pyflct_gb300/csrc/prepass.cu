@@ -532,6 +532,7 @@ __global__ void __launch_bounds__(kInterpThreads) k_interp_grid(InterpArgs a) {
     const float inv = 1.0f / (float)a.skip;
     const int imax = (a.gx - 1) * a.skip, jmax = (a.gy - 1) * a.skip;
     const int tc = (threadIdx.x % kPairCols) * 2, tr = threadIdx.x / kPairCols;
+    grid_dep_wait();
     publish_counters(a.pub_src, a.pub_dst);
     for (int tile = blockIdx.x; tile < ntr * ntc; tile += gridDim.x) {
         const int i0 = a.i0 + (tile / ntc) * kTileR, j0 = (tile - (tile / ntc) * ntc) * kTileC;

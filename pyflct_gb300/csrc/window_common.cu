@@ -8,6 +8,7 @@ __device__ __forceinline__ double da(double a, double b) { return __dadd_rn(a, b
 __device__ __forceinline__ double ds(double a, double b) { return __dsub_rn(a, b); }
 
 __global__ void k_means(MeansArgs a) {
+    grid_dep_wait();
     const int nw = *a.nwork;
     for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < nw; w += gridDim.x * blockDim.x) {
         const int pix = a.work[w];
@@ -73,6 +74,7 @@ __device__ __forceinline__ void fit3x3(const double* v, double* sx, double* sy) 
 // the kernel is bound by each SM's FP64 pipe, and a plain grid-stride
 // mapping leaves the low blocks (and the SMs holding them) with the most.
 __global__ void k_fit(FitArgs a) {
+    grid_dep_wait();
     publish_counters(a.pub_src, a.pub_dst);
     const int nw = *a.nwork;
     const int half = a.n / 2, half1 = (a.n1 ? a.n1 : a.n) / 2;
@@ -144,6 +146,7 @@ __global__ void __launch_bounds__(128) k_fit_hires(FitArgs a) {
     __shared__ float s_pk[4][NI * NI];
     __shared__ float s_rx[4][NI][4];
     __shared__ int s_iz[4][NI];
+    grid_dep_wait();
     publish_counters(a.pub_src, a.pub_dst);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nw = *a.nwork;

@@ -100,6 +100,7 @@ k_window_fp32(WinArgs a) {
     }
     float2* buf = s_buf + team * S::BUF;
     float* ab = reinterpret_cast<float*>(buf);  // |c|, after the last transform
+    grid_dep_wait();  // the tables above come from the kernel's arguments
     const int nwork = *a.nwork;
     if (ln == 0) {
         s_max[2 * team] = 0u;
@@ -389,9 +390,10 @@ k_window_fp32(WinArgs a) {
     }
 }
 
-// Host-side launcher for one box size (defined in the per-size .cu files).
+// Host-side launcher for one box size (defined in the per-size .cu files);
+// pdl: launch as a programmatic dependent of the stream's previous kernel.
 template <int N>
-cudaError_t launch_window_fp32(const WinArgs& a, int grid, cudaStream_t st);
+cudaError_t launch_window_fp32(const WinArgs& a, int grid, cudaStream_t st, bool pdl);
 template <int N>
 int window_fp32_blocks_per_sm();
 

@@ -7,14 +7,13 @@
 #define FLCT_INSTANTIATE_WINDOW_FP32(N)                                                        \
     namespace flct {                                                                           \
     template <>                                                                                \
-    cudaError_t launch_window_fp32<N>(const WinArgs& a, int grid, cudaStream_t st) {           \
+    cudaError_t launch_window_fp32<N>(const WinArgs& a, int grid, cudaStream_t st, bool pdl) { \
         using S = WinShape<N>;                                                                 \
         cudaError_t e = cudaFuncSetAttribute(k_window_fp32<N>,                                 \
                                              cudaFuncAttributeMaxDynamicSharedMemorySize,      \
                                              (int)S::smem);                                    \
         if (e != cudaSuccess) return e;                                                        \
-        k_window_fp32<N><<<grid, S::THREADS, S::smem, st>>>(a);                                \
-        return cudaGetLastError();                                                             \
+        return launch_kernel(k_window_fp32<N>, dim3(grid), dim3(S::THREADS), S::smem, st, pdl, a); \
     }                                                                                          \
     template <>                                                                                \
     int window_fp32_blocks_per_sm<N>() {                                                       \
