@@ -188,13 +188,20 @@ FLCT_API flct_status flct_gpu_warp_frac2d(flct_ctx *ctx, const double *arr,
  * nothing: its only scratch is a fixed 1.2 MB array inside the library that
  * every GPU which loads the library keeps until the process exits.
  *   - nxi or nyi above FLCT_NOALLOC_MAX_AXIS: FLCT_ERR_UNSUPPORTED;
- *     nx or ny below 3: FLCT_ERR_GRID_TOO_SMALL.
- *   - The first call on a device looks up that array's device address once
- *     (with that device current); make that first call before any stream
- *     capture begins.
+ *     nx or ny below 3: FLCT_ERR_GRID_TOO_SMALL; no sm_103 device current:
+ *     FLCT_ERR_NO_DEVICE; a device pointer that lives on another device
+ *     than the current one: FLCT_ERR_ARG.
+ *   - The first call in a CUDA context (the device's primary context, a
+ *     context the caller made, or the new primary context after a
+ *     cudaDeviceReset) looks up that array's device address once, with
+ *     that context current; make that first call before any stream capture
+ *     begins.
  *   - All calls share the one array: calls that overlap on the GPU (other
  *     streams, other host threads) race and must be serialised by the
  *     caller.
+ *   - An error the caller's earlier work left pending is neither reported
+ *     nor cleared; a launch error of this call is returned as
+ *     FLCT_ERR_CUDA.
  *   - Asynchronous: returns once the work is enqueued. */
 FLCT_API flct_status flct_gpu_interpcc2d_noalloc(const double *d_fdata, double xmiss,
                                                  int nx, int ny,

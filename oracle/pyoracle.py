@@ -50,10 +50,20 @@ def build(force: bool = False) -> str:
     return LIB_PATH
 
 
+def reference_source() -> str:
+    """The reference's source/ directory: $FLCT_REFERENCE_SOURCE, else
+    source/ of a checkout named `reference` beside this repository, else ''."""
+    env = os.environ.get("FLCT_REFERENCE_SOURCE", "")
+    if env:
+        return env
+    sib = os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference", "source")
+    return sib if os.path.isdir(sib) else ""
+
+
 def build_ref() -> bool:
     """Compile the reference in place into _ref/ when its sources exist."""
-    src = os.environ.get("FLCT_REFERENCE_SOURCE", "/root/reference/source")
-    if not os.path.exists(os.path.join(src, "flct.c")):
+    src = reference_source()
+    if not src or not os.path.exists(os.path.join(src, "flct.c")):
         return False
     subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + src], check=True)
     return True

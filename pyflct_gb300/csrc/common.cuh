@@ -90,8 +90,11 @@ inline cudaError_t launch_kernel(void (*kern)(KArgs...), dim3 grid, dim3 block, 
 // A kernel launched as a programmatic dependent (its launch overlaps the
 // tail of the kernel before it on the stream) waits here until that kernel
 // has finished and its writes are visible; launched normally, this returns
-// at once.  Every kernel that may be so launched calls it before it reads
-// anything an earlier kernel wrote.
+// at once.  Every kernel that may be so launched calls it before its first
+// global read or write of anything an earlier operation on the stream
+// touches.  The rule carries the ordering when the operation before the
+// launch is not a kernel (an event wait joining another stream, a memset)
+// and in captured graphs, where the programmatic edge becomes a graph edge.
 __device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
 // The call's work count and status word (final once this kernel starts: no

@@ -720,7 +720,10 @@ flct_status enqueue_prepass(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaS
         if (s == FLCT_OK) s = enqueue_box_rows(ctx, j, b, 0, j.nx, st, launches);
         if (s == FLCT_OK) s = enqueue_box_cols(ctx, j, b, 0, j.gi, st, launches);
     }
-    // device calls (with a side stream): the means overlap the column sums' tail
+    // device calls (with a side stream): the means launch as a programmatic
+    // dependent; the operation just before them on st is the wait for the
+    // classification, and k_means' grid_dep_wait (before any global access)
+    // keeps both the column sums and that join ordered, eager and captured
     if (s == FLCT_OK) s = enqueue_means(ctx, j, b, (long)npx, st, launches, side != nullptr);
     return s;
 }

@@ -47,7 +47,12 @@ def f32(a):
     return np.asarray(a, dtype=np.float32).astype(np.float64)
 
 
-def main(refroot="/root/reference"):
+def main(refroot=""):
+    """refroot: the reference checkout (holding source/ and tests/); default
+    $FLCT_REFERENCE_ROOT, else a checkout named `reference` beside this
+    repository."""
+    refroot = refroot or os.environ.get("FLCT_REFERENCE_ROOT", "") or \
+        os.path.join(os.path.dirname(ROOT), "reference")
     os.environ["FLCT_REFERENCE_SOURCE"] = os.path.join(refroot, "source")
     if not po.build_ref():
         raise SystemExit("reference sources not found under " + refroot)

@@ -274,7 +274,11 @@ def test_device_calls_replayed_as_graph():
     """Device-buffer calls repeated with the same parameters and buffers are
     replayed from a captured CUDA graph (the second call captures it): every
     call gives the first call's output, the stage times are filled in, and a
-    call with other buffers or parameters is not served from the graph."""
+    call with other buffers or parameters is not served from the graph.  The
+    first call runs eagerly, its means, window, fit and interpolation
+    kernels launched as programmatic dependents on the stream; the later
+    ones replay those edges from the graph, so both forms of the
+    programmatic ordering are compared bit for bit."""
     import ctypes as C
     import torch
     from pyflct_gb300 import _lib, synth

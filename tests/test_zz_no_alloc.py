@@ -57,6 +57,26 @@ def test_noalloc_matches_allocating_entry_point():
         # tolerance of the interpolation tests is exact equality
         assert np.array_equal(got, want)
 
+    # the largest accepted axes fill the fixed array to its end (each axis
+    # at FLCT_NOALLOC_MAX_AXIS once), and a call on a non-default stream
+    side = torch.cuda.Stream(device=dev)
+    for gx, gy, nxi, nyi, st in ((12, 9, 16384, 3, None), (8, 13, 5, 16384, side)):
+        f, xw, yw = _case(rng, gx, gy, nxi, nyi)
+        want = interpcc2d(f, XMISS, xw, yw)
+        d_f = torch.from_numpy(f).to(dev)
+        d_x = torch.from_numpy(xw).to(dev)
+        d_y = torch.from_numpy(yw).to(dev)
+        d_o = torch.full((nxi, nyi), np.nan, dtype=torch.float64, device=dev)
+        torch.cuda.synchronize()
+        handle = C.c_void_p(st.cuda_stream) if st is not None else None
+        rc = lib.flct_gpu_interpcc2d_noalloc(ptr(d_f), XMISS, gx, gy, ptr(d_x), nxi, ptr(d_y), nyi,
+                                             ptr(d_o), handle)
+        if st is not None:
+            st.synchronize()
+        torch.cuda.synchronize()
+        assert rc == _lib.OK
+        assert np.array_equal(d_o.cpu().numpy(), want)
+
     # sizes beyond the fixed scratch are refused, small grids too
     d_big = torch.zeros(1, dtype=torch.float64, device=dev)
     too_many = _lib.load().flct_gpu_interpcc2d_noalloc(
