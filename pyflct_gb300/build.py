@@ -82,7 +82,28 @@ def build(force: bool = False, jobs: int | None = None, verbose: bool = False) -
             raise RuntimeError("link failed:\n" + r.stderr)
         os.replace(tmp, LIB)
     build_cli(verbose)
+    build_probe(verbose)
     return LIB
+
+
+PROBE_SRC = os.path.join(PKG, "probe", "fp32_peak.cu")
+PROBE_LIB = os.path.join(PKG, "libflctprobe.so")
+
+
+def build_probe(verbose: bool = False) -> str:
+    """libflctprobe.so: the FP32-pipe throughput microbenchmark the bench
+    uses as the FP32 form's roofline denominator (not part of the C ABI)."""
+    if os.path.exists(PROBE_LIB) and os.path.getmtime(PROBE_LIB) >= os.path.getmtime(PROBE_SRC):
+        return PROBE_LIB
+    tmp = PROBE_LIB + ".tmp"
+    cmd = [nvcc()] + ARCH + ["-O3", "-Xcompiler", "-fPIC", "-shared", "-cudart", "static", PROBE_SRC, "-o", tmp]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("building the FP32 probe failed:\n" + r.stderr)
+    if verbose and r.stderr.strip():
+        print(r.stderr)
+    os.replace(tmp, PROBE_LIB)
+    return PROBE_LIB
 
 
 CLI = os.path.join(PKG, "cli")

@@ -116,5 +116,55 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
     for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
 }
 
+// tcgen05.ld without the wait: 8 / 16 consecutive fp32 columns of this
+// thread's TMEM lane into r (warp-collective); tmem_wait_ld() makes them
+// usable, so several loads can be in flight at once.
+__device__ __forceinline__ void tmem_ld8_nw(uint32_t taddr, uint32_t (&r)[8]) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_ld16_nw(uint32_t taddr, uint32_t (&r)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// W consecutive fp32 columns (W a multiple of 8, at most 128) of this
+// thread's TMEM lane into v, with one wait for all of them.
+template <int W>
+__device__ __forceinline__ void tmem_ld(uint32_t taddr, float (&v)[W]) {
+    static_assert(W % 8 == 0 && W <= 128, "tmem_ld width");
+    uint32_t r[W];
+    if constexpr (W % 16 == 0) {
+#pragma unroll
+        for (int b = 0; b < W / 16; ++b) tmem_ld16_nw(taddr + 16 * b, *reinterpret_cast<uint32_t(*)[16]>(r + 16 * b));
+    } else {
+#pragma unroll
+        for (int b = 0; b < W / 8; ++b) tmem_ld8_nw(taddr + 8 * b, *reinterpret_cast<uint32_t(*)[8]>(r + 8 * b));
+    }
+    tmem_wait_ld();
+#pragma unroll
+    for (int k = 0; k < W; ++k) v[k] = __uint_as_float(r[k]);
+}
+
+// One-dimensional bulk copy (TMA engine) of `bytes` (a multiple of 16, both
+// addresses 16-byte aligned) from global to this CTA's shared memory,
+// completing `bytes` of transaction count on the mbarrier.
+__device__ __forceinline__ void bulk_g2s(void* smem_dst, const void* gsrc, uint32_t bytes, uint64_t* mbar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(smem_dst)),
+        "l"(gsrc), "r"(bytes), "r"(smem_u32(mbar))
+        : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* mbar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes)
+                 : "memory");
+}
+
 }  // namespace tc
 }  // namespace flct
