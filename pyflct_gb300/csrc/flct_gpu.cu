@@ -54,6 +54,32 @@ const WinEntry* find_win(int n) {
     return nullptr;
 }
 
+// The tensor-core form per box size: launchers and occupancy per split type
+// (0 = FP16, 1 = BF16).
+struct TcEntry {
+    int n;
+    cudaError_t (*launch[2])(const TcArgs&, int, cudaStream_t, bool);
+    int (*bps[2])();
+    int wit;  // windows per CTA iteration
+};
+
+#define FLCT_TC(N)                                                                          \
+    {N,                                                                                     \
+     {&launch_window_tc<N, __half>, &launch_window_tc<N, __nv_bfloat16>},                   \
+     {&window_tc_blocks_per_sm<N, __half>, &window_tc_blocks_per_sm<N, __nv_bfloat16>},     \
+     TcCfg<N>::WIT}
+const TcEntry kTc[] = {FLCT_TC(4),  FLCT_TC(8),  FLCT_TC(12), FLCT_TC(16), FLCT_TC(20), FLCT_TC(24),
+                       FLCT_TC(28), FLCT_TC(32), FLCT_TC(36), FLCT_TC(40), FLCT_TC(44), FLCT_TC(48),
+                       FLCT_TC(52), FLCT_TC(56), FLCT_TC(60), FLCT_TC(64)};
+#undef FLCT_TC
+constexpr int kNumTc = sizeof(kTc) / sizeof(kTc[0]);
+
+int tc_index(int n) {
+    for (int k = 0; k < kNumTc; ++k)
+        if (kTc[k].n == n) return k;
+    return -1;
+}
+
 // ------------------------------------------------ parameter derivation --
 
 struct Derived {
@@ -95,8 +121,9 @@ struct flct_ctx {
                 &bb_work, &bb_means, &bb_peaks, &bb_ctr, &bb_meta, &b_peaks_h, &bb_peaks_h, &b_re1, &b_re2};
     }
     int bps[sizeof(kWin) / sizeof(kWin[0])] = {0};
-    int bps_tc[2] = {0, 0};
-    Buf b_tc;              // tensor-core DFT matrices (b1 32x32, b2 64x64 floats)
+    int bps_tc[kNumTc][2] = {};
+    Buf b_tc;              // tensor-core DFT matrices of every box size and split type
+    size_t tc_off[kNumTc][2] = {};
     bool tc_ready = false;
     bool box_attr = false;  // k_box_rows' shared-memory size is set
     bool pending = false;  // a velocity call's events await collection
@@ -271,35 +298,35 @@ int win_grid(flct_ctx* ctx, int n) {
     return ctx->nsm * ctx->bps[k];
 }
 
-// The tensor-core form's constant matrices, built once per context in FP64:
-// b1[c][j] (S1: real input -> half spectrum columns) and b2[n][k] (S2:
-// complex DFT along the other axis, re/im by halves, columns in tc_kx order).
+// The tensor-core form's constant matrices, built once per context in FP64
+// and split into 16-bit hi / lo halves in their shared-memory layouts, for
+// every box size and both split types at once (one allocation that never
+// moves, so captured graphs keep pointing at valid tables).
 flct_status ensure_tc_tables(flct_ctx* ctx) {
     if (ctx->tc_ready) return FLCT_OK;
-    ENSURE(ctx->b_tc, (32 * 32 + 64 * 64) * sizeof(float));
-    std::vector<float> t(32 * 32 + 64 * 64);
-    const double tw = 2.0 * 3.14159265358979323846 / 32.0;
-    for (int c = 0; c < 32; ++c)
-        for (int j = 0; j < 32; ++j) {
-            const double v = (c <= 16) ? std::cos(tw * ((c * j) % 32)) : -std::sin(tw * (((c - 16) * j) % 32));
-            t[c * 32 + j] = (float)v;
+    size_t total = 0;
+    for (int k = 0; k < kNumTc; ++k)
+        for (int f = 0; f < 2; ++f) {
+            ctx->tc_off[k][f] = total;
+            total += ((size_t)tc_bmat_bytes(kTc[k].n) + 255) & ~(size_t)255;
         }
-    float* b2 = t.data() + 32 * 32;
-    for (int n = 0; n < 64; ++n)
-        for (int k = 0; k < 64; ++k) {
-            // output column q holds wavenumber tc_kx(q): mirror pairs adjacent
-            const int pp = n / 32, kx = tc_kx(n % 32), pk = k / 32, i = k % 32;
-            const double th = tw * ((kx * i) % 32);
-            double v;
-            if (pk == 0 && pp == 0) v = std::cos(th);
-            else if (pk == 1 && pp == 0) v = std::sin(th);
-            else if (pk == 0 && pp == 1) v = -std::sin(th);
-            else v = std::cos(th);
-            b2[n * 64 + k] = (float)v;
+    ENSURE(ctx->b_tc, total);
+    std::vector<unsigned char> host(total, 0);
+    std::vector<uint16_t> m;
+    for (int k = 0; k < kNumTc; ++k)
+        for (int f = 0; f < 2; ++f) {
+            tc_build_bmat(kTc[k].n, f, &m);
+            memcpy(host.data() + ctx->tc_off[k][f], m.data(), m.size() * sizeof(uint16_t));
         }
-    CK(cudaMemcpy(ctx->b_tc.p, t.data(), t.size() * sizeof(float), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->b_tc.p, host.data(), total, cudaMemcpyHostToDevice));
     ctx->tc_ready = true;
     return FLCT_OK;
+}
+
+// CTAs per SM of the tensor-core form for box size n (index k of kTc).
+int tc_bps(flct_ctx* ctx, int k, int which) {
+    if (ctx->bps_tc[k][which] == 0) ctx->bps_tc[k][which] = std::max(1, kTc[k].bps[which]());
+    return ctx->bps_tc[k][which];
 }
 
 // Resolve FLCT_FORM_AUTO (the autotuner's choice once it has measured box
@@ -310,8 +337,8 @@ flct_status pick_form(flct_ctx* ctx, int requested, int n, int* form) {
         auto it = ctx->tune.find(n);
         f = (it != ctx->tune.end()) ? it->second.form : FLCT_FORM_FP32;
     }
-    if ((f == FLCT_FORM_TC_FP16 || f == FLCT_FORM_TC_BF16) && n != 32)
-        return fail(ctx, FLCT_ERR_UNSUPPORTED, "the tensor-core form is built for 32x32 boxes (sigma 8); box %d", n);
+    if ((f == FLCT_FORM_TC_FP16 || f == FLCT_FORM_TC_BF16) && tc_index(n) < 0)
+        return fail(ctx, FLCT_ERR_UNSUPPORTED, "the tensor-core form has no kernel for box %d", n);
     if (f < 0 || f > FLCT_FORM_TC_BF16) return fail(ctx, FLCT_ERR_ARG, "unknown window form %d", requested);
     *form = f;
     return FLCT_OK;
@@ -332,6 +359,8 @@ flct_status launch_windows(flct_ctx* ctx, int form, const WinEntry* we, int n, c
     }
     flct_status s = ensure_tc_tables(ctx);
     if (s != FLCT_OK) return s;
+    const int k = tc_index(n);
+    if (k < 0) return fail(ctx, FLCT_ERR_UNSUPPORTED, "the tensor-core form has no kernel for box %d", n);
     TcArgs ta{};
     ta.s1 = wa.s1;
     ta.s2 = wa.s2;
@@ -348,21 +377,16 @@ flct_status launch_windows(flct_ctx* ctx, int form, const WinEntry* we, int n, c
     ta.segs = wa.segs;
     ta.seg_start = wa.seg_start;
     ta.nseg = wa.nseg;
-    ta.b1 = (const float*)ctx->b_tc.p;
-    ta.b2 = (const float*)ctx->b_tc.p + 32 * 32;
+    const int which = (form == FLCT_FORM_TC_BF16) ? 1 : 0;
+    ta.bmat = reinterpret_cast<const uint16_t*>(static_cast<const unsigned char*>(ctx->b_tc.p) + ctx->tc_off[k][which]);
     ta.status = status;
     // failure-path test hook: stage waits that run out after this many ns
     if (const char* w = getenv("FLCT_TEST_TC_STALL_NS")) ta.stall_ns = strtoull(w, nullptr, 10);
-    for (int k = 0; k < 2 * kMaxBox + 1; ++k) ta.gauss[k] = wa.gauss[k];
-    for (int k = 0; k < kMaxBox; ++k) ta.filt2[k] = wa.filt2[k];
-    const int which = (form == FLCT_FORM_TC_BF16) ? 1 : 0;
-    if (ctx->bps_tc[which] == 0)
-        ctx->bps_tc[which] = std::max(1, which ? window_tc32_blocks_per_sm<__nv_bfloat16>()
-                                               : window_tc32_blocks_per_sm<__half>());
-    int grid = std::max(ctx->nsm, ctx->nsm * ctx->bps_tc[which] / grid_div);
-    if (max_items >= 0) grid = (int)std::max<long>(1, (max_items + 7) / 8);  // 8 windows per CTA iteration
-    if (which) CK(launch_window_tc32<__nv_bfloat16>(ta, grid, st));
-    else CK(launch_window_tc32<__half>(ta, grid, st));
+    for (int q = 0; q < 2 * kMaxBox + 1; ++q) ta.gauss[q] = wa.gauss[q];
+    for (int q = 0; q < kMaxBox; ++q) ta.filt2[q] = wa.filt2[q];
+    int grid = std::max(ctx->nsm, ctx->nsm * tc_bps(ctx, k, which) / grid_div);
+    if (max_items >= 0) grid = (int)std::max<long>(1, (max_items + kTc[k].wit - 1) / kTc[k].wit);
+    CK(kTc[k].launch[which](ta, grid, st, pdl));
     return FLCT_OK;
 }
 
@@ -420,9 +444,9 @@ flct_status tune_windows(flct_ctx* ctx, const WinEntry* we, int n, const WinArgs
     // radix form and the split-FP16 tensor-core form (the BF16 split keeps
     // fewer mantissa bits and is only used when asked for)
     std::vector<Cand> cands = {{FLCT_FORM_FP32, 1}, {FLCT_FORM_FP32, 2}};
-    if (n == 32) {
+    if (tc_index(n) >= 0) {
         cands.push_back({FLCT_FORM_TC_FP16, 1});
-        cands.push_back({FLCT_FORM_TC_FP16, 2});
+        if (tc_bps(ctx, tc_index(n), 0) > 1) cands.push_back({FLCT_FORM_TC_FP16, 2});
     }
     int nwork = 0;
     CK(cudaMemcpyAsync(&nwork, d_nwork, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -825,10 +849,9 @@ flct_status prime_form(flct_ctx* ctx, int form, int n) {
     }
     flct_status s = ensure_tc_tables(ctx);
     if (s != FLCT_OK) return s;
-    const int which = (form == FLCT_FORM_TC_BF16) ? 1 : 0;
-    if (ctx->bps_tc[which] == 0)
-        ctx->bps_tc[which] = std::max(1, which ? window_tc32_blocks_per_sm<__nv_bfloat16>()
-                                               : window_tc32_blocks_per_sm<__half>());
+    const int k = tc_index(n);
+    if (k < 0) return fail(ctx, FLCT_ERR_UNSUPPORTED, "the tensor-core form has no kernel for box %d", n);
+    tc_bps(ctx, k, (form == FLCT_FORM_TC_BF16) ? 1 : 0);
     return FLCT_OK;
 }
 
@@ -1267,7 +1290,7 @@ flct_status tune_batch(flct_ctx* ctx, BatchPlan& bp, cudaStream_t bs) {
         group_wargs(ctx, bp, g, &wa);
         unsigned* status = (unsigned*)(bp.bufs[G.pairs[0]].ctr + 4);
         for (int f : {FLCT_FORM_FP32, FLCT_FORM_TC_FP16}) {
-            if (f != FLCT_FORM_FP32 && G.n != 32) continue;
+            if (f != FLCT_FORM_FP32 && tc_index(G.n) < 0) continue;
             flct_status s = prime_form(ctx, f, G.n);
             if (s != FLCT_OK) return s;
         }
@@ -1919,7 +1942,7 @@ flct_status flct_gpu_velocity_device(flct_ctx* ctx, const flct_params* p, const 
         WinArgs wa;
         make_wargs(j, b, &wa);
         for (int f : {FLCT_FORM_FP32, FLCT_FORM_TC_FP16}) {
-            if (f != FLCT_FORM_FP32 && n != 32) continue;
+            if (f != FLCT_FORM_FP32 && tc_index(n) < 0) continue;
             s = prime_form(ctx, f, n);
             if (s != FLCT_OK) return s;
         }

@@ -1,0 +1,3 @@
+// Tensor-core window kernel, box 64 (FP16 and BF16 split).
+#include "window_tc_inst.cuh"
+FLCT_TC_INST(64)

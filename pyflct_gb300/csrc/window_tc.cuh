@@ -1,38 +1,59 @@
 // window_tc.cuh -- the tensor-core window-correlation kernel (DFT-matrix
-// form, split precision) for 32 x 32 boxes.
+// form, split precision) for every box size n = 4..64 (multiples of 4).
 //
 // Same contract as k_window_fp32 (source/flct.c:829-876, 1325-1532: window,
 // transforms, conj product with the optional filter, inverse, |c| in the
 // half-shifted frame, first strict maximum), but every transform is a dense
-// DFT-matrix product on tcgen05 tensor cores.  Operands are split into a
+// DFT-matrix product on the tcgen05 tensor cores.  Operands are split into a
 // 16-bit high part and a 16-bit remainder (FP16 or BF16); each product is
 // hi*hi + hi*lo + lo*hi accumulated in FP32 in tensor memory, which keeps
-// ~21 significant bits (FP16) of each 16-bit-by-16-bit product.
+// ~21 significant bits (FP16) of every 16-bit-by-16-bit product.
 //
-// Eight windows per CTA iteration, 128 threads (4 warps), four GEMM stages,
-// each M = 128 (rows of data), B = a constant DFT matrix in shared memory:
-//   S1  along j, real input -> half spectrum T[i][c]:
-//       c = 0..16 real parts (ky = c), c = 17..31 imaginary parts (ky = c-16)
-//       rows (window, image, i), K = j (32), N = c (32)            4 tiles
-//   S2  along i on 16 packed complex columns per image:
-//       column 0 = T[:,0] + i T[:,16] (separated later by Hermitian symmetry),
-//       column kc = T[:,kc] (kc = 1..15); rows (window, kc), one N = 64 GEMM
-//       per image into adjacent TMEM columns, K = (re/im, i) (64),
-//       N = (re/im, kx) (64)                                        1 tile
-//   product conj(A) B filt^2 per (kx, ky): one lane holds both images'
-//       spectra of its (window, kc) row
-//   S3  inverse along kx on 16 packed columns per window (ky = 0 and 16
-//       share column 0: both inverse transforms are real),
-//       rows (window, kc), K = (re/im, kx), N = (re/im, i)          1 tile
-//   S4  complex-to-real along ky: rows (window, i), K = 32 spectral terms
-//       (weights 1 or 2 folded into the data), N = j               2 tiles
-// S3 reuses S2's matrix and S4 reuses S1's, transposed through the
-// descriptors' MN-major mode.  The transposes between stages are free: each
-// thread writes its TMEM row straight into the next stage's operand layout
-// (MN-major where the contraction index changes).
+// A CTA of 256 threads (8 warps) runs WIT windows per iteration through four
+// GEMM stages, each M = 128 rows of data against a constant DFT matrix held
+// in shared memory (H = n/2, n8 = n rounded up to 8, k1 = n rounded up to 16):
+//   S1  along j, real input -> real-form half spectrum T[i][c]
+//       (c = 0..H: cosine sums, ky = c; c = H+1..n-1: minus sine sums,
+//       ky = c - H); rows (window, image, i), n8 rows per sub-image,
+//       A MN-major (the box columns are loaded coalesced, one per lane),
+//       K = j (k1), N = c (k1)                                      T1 tiles
+//   S2  complex DFT along i: rows (window, ky), one row per complex column
+//       of the half spectrum, A MN-major, K = (re/im, i) (2 n8),
+//       N = (re/im, kx) (2 n8), both images into adjacent TMEM columns
+//   product C = conj(A) B filt^2 per (kx, ky) in the row's lane: both
+//       images' spectra sit in the same TMEM lane
+//   S3  inverse complex DFT along kx: rows (window, ky), A K-major,
+//       K = (re/im, kx), N = (re/im, i)               (S2's matrix, transposed)
+//   S4  complex-to-real along ky: rows (window, i), A MN-major, K = the
+//       spectral terms (weights 1 or 2 folded into the data), N = j
+//                                                 (S1's matrix, transposed)
+// then |c| in the half-shifted frame, the first strict maximum, the peak
+// record.  S3 reuses S2's matrix and S4 reuses S1's through the descriptors'
+// MN-major mode, so each stage's transpose is free: each thread writes its
+// TMEM row straight into the next stage's operand layout, in 16-byte chunks.
+//
+// Half-spectrum columns: with H a multiple of 8 (n = 16, 32, 48, 64) the two
+// real columns ky = 0 and ky = H share one complex row ("packed": T[:,0] +
+// i T[:,H]) and the product separates them by Hermitian symmetry; otherwise
+// the rows per window are padded to a multiple of 8 anyway and ky = H gets a
+// row of its own.  In packed mode the S2 output columns hold kx and -kx next
+// to each other (tc_kx order) so a lane has both halves of every mirror pair.
+//
+// Scaling: each sub-image is scaled by an exact power of two that brings its
+// largest |value| into [1, 4) (FP16 holds it without overflow); the
+// conj(A) B product and the inverse along kx by fixed powers of two from
+// a-priori bounds (|C| <= 16 n^4, |u| <= n max |C|), so no FP16 operand can
+// overflow; none of these changes the argmax or the fit.
+//
+// Every wait on the tensor cores is bounded (2 s); a wait that runs out
+// sets the status word's timeout bit, the CTA waits (bounded) for its own
+// MMAs, frees its tensor memory and returns.
 #pragma once
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
+
+#include <type_traits>
+#include <vector>
 
 #include "common.cuh"
 #include "fft_reg.cuh"
@@ -55,8 +76,9 @@ struct TcArgs {
     const WinSeg* segs;   // batched launch (see WinArgs), else null
     const int* seg_start;
     int nseg;
-    const float* b1;      // [c][j] 32 x 32: S1 matrix, row = output column c
-    const float* b2;      // [n][k] 64 x 64: S2 matrix, n = (re/im, q), k = (re/im, i), kx = tc_kx(q)
+    // the DFT matrices as split 16-bit hi / lo halves, already in their
+    // shared-memory layouts: B1 hi, B1 lo, B2 hi, B2 lo (TcCfg<n>::BB bytes)
+    const uint16_t* bmat;
     unsigned* status;
     // failure-path test hook: when nonzero, every stage waits this many ns
     // on a barrier that nothing completes (instead of the MMA barrier), so
@@ -66,14 +88,69 @@ struct TcArgs {
     float filt2[kMaxBox];
 };
 
-// Column order of S2's output (and S3's input): kx and -kx adjacent, so each
-// half of a spectrum row holds complete mirror pairs:
-//   q = 0 -> kx 0, q = 1 -> kx 16, q = 2j -> kx j, q = 2j+1 -> kx 32-j.
-__host__ __device__ constexpr int tc_kx(int q) {
-    return q == 0 ? 0 : (q == 1 ? 16 : ((q % 2 == 0) ? q / 2 : 32 - q / 2));
+__host__ __device__ constexpr int tc_r8(int x) { return (x + 7) / 8 * 8; }
+__host__ __device__ constexpr int tc_r16(int x) { return (x + 15) / 16 * 16; }
+__host__ __device__ constexpr int tc_max(int a, int b) { return a > b ? a : b; }
+__host__ __device__ constexpr int tc_pow2(int x) { return x <= 32 ? 32 : x <= 64 ? 64 : x <= 128 ? 128 : x <= 256 ? 256 : 512; }
+
+// Compile-time geometry of the tensor-core form for box side N.
+template <int N>
+struct TcCfg {
+    static_assert(N % 4 == 0 && N >= 4 && N <= kMaxBox, "box side");
+    static constexpr int H = N / 2;
+    static constexpr bool PACK = (H % 8) == 0;
+    static constexpr int KYN = PACK ? H : H + 1;              // spectrum rows per window
+    static constexpr int R2 = PACK ? H : tc_r8(H + 1);        // S2 / S3 rows per window
+    static constexpr int G2 = R2 / 8;                         // 8-row groups per window
+    static constexpr int WIT = 128 / R2;                      // windows per CTA iteration
+    static constexpr int N8 = tc_r8(N);
+    static constexpr int K1 = tc_r16(N);                      // S1 K and N, S4 K and N
+    static constexpr int K2 = 2 * N8;                         // S2 K and N, S3 K and N
+    static constexpr int SUBS = 2 * WIT;                      // sub-images per iteration
+    static constexpr int T1 = (SUBS * N8 + 127) / 128;        // S1 tiles
+    static constexpr int T4 = (WIT * N8 + 127) / 128;         // S4 tiles
+    static constexpr int LW = K1 <= 16 ? 16 : 32;             // lanes per sub-image column block
+    static constexpr int SPW = 32 / LW;                       // sub-images per warp pass
+    static constexpr int CB = (K1 + 31) / 32;                 // column blocks (K1 > 32)
+    static constexpr int QC = N8 / 8;                         // 8-column chunks of a spectrum row
+    // shared memory, bytes (each operand as hi then lo)
+    static constexpr int A1B = T1 * 128 * K1 * 2;
+    static constexpr int A2B = 128 * K2 * 2;                  // per image
+    static constexpr int A3B = 128 * K2 * 2;
+    static constexpr int A4B = T4 * 128 * K1 * 2;
+    static constexpr int SROW = N + 1;                        // staged c row, floats (odd: no bank conflicts)
+    static constexpr int STGB = WIT * N * SROW * 4;
+    static constexpr int AREG =
+        (tc_max(tc_max(2 * A1B, 4 * A2B), tc_max(tc_max(2 * A3B, 2 * A4B), STGB)) + 1023) / 1024 * 1024;
+    static constexpr int B1B = K1 * K1 * 2;
+    static constexpr int B2B = K2 * K2 * 2;
+    static constexpr int BB = 2 * B1B + 2 * B2B;
+    static constexpr int MISC = 2048;
+    static constexpr int SMEM = AREG + BB + MISC + 1024;      // + 1024 to align the base
+    static constexpr int TCOLS = tc_pow2(tc_max(tc_max(T1 * K1, 2 * K2), tc_max(K2, T4 * K1)));
+    static constexpr int MINB = N <= 32 ? 2 : 1;
+    // fixed power-of-two scales: sub-images are scaled into |x| < 4, so
+    // |A|, |B| <= 4 n^2 and |C| <= 16 n^4; 2^-CSH1 brings that bound to
+    // 2^15 (below the FP16 maximum).  The inverse along kx sums n of those
+    // and the c2r weight doubles it: 2^-CSH2 brings 2 n 2^15 back to 2^15.
+    static constexpr int LOG2N = N <= 4 ? 2 : N <= 8 ? 3 : N <= 16 ? 4 : N <= 32 ? 5 : 6;
+    static constexpr int CSH1 = 4 * LOG2N + 4 - 15;
+    static constexpr int CSH2 = LOG2N + 1;
+    static_assert(SMEM <= 232448, "shared memory");
+    static_assert(BB % 16 == 0 && B1B % 16 == 0, "bulk copy granularity");
+};
+
+// S2 output column q of a packed spectrum row holds wavenumber tc_kx(q):
+// kx and -kx adjacent, q = 0 -> 0, q = 1 -> H, q = 2j -> j, q = 2j+1 -> N - j.
+__host__ __device__ constexpr int tc_kx(int q, int n) {
+    return q == 0 ? 0 : (q == 1 ? n / 2 : ((q % 2 == 0) ? q / 2 : n - q / 2));
 }
-// Position of -kx for the column at position q.
 __host__ __device__ constexpr int tc_mirror(int q) { return q < 2 ? q : ((q % 2 == 0) ? q + 1 : q - 1); }
+// Column order of S2's output: tc_kx order in packed mode, natural otherwise.
+template <int N>
+__host__ __device__ constexpr int tc_kxq(int q) {
+    return TcCfg<N>::PACK ? tc_kx(q, N) : q;
+}
 
 template <typename T>
 struct Split16;
@@ -94,13 +171,6 @@ struct Split16<__half> {
         hi = make_uint4(h[0], h[1], h[2], h[3]);
         lo = make_uint4(l[0], l[1], l[2], l[3]);
     }
-    __device__ static __forceinline__ void pair(float v0, float v1, uint32_t& hi, uint32_t& lo) {
-        const __half2 a = __floats2half2_rn(v0, v1);
-        const float2 b = __half22float2(a);
-        const __half2 c = __floats2half2_rn(v0 - b.x, v1 - b.y);
-        hi = *reinterpret_cast<const uint32_t*>(&a);
-        lo = *reinterpret_cast<const uint32_t*>(&c);
-    }
 };
 template <>
 struct Split16<__nv_bfloat16> {
@@ -118,130 +188,99 @@ struct Split16<__nv_bfloat16> {
         hi = make_uint4(h[0], h[1], h[2], h[3]);
         lo = make_uint4(l[0], l[1], l[2], l[3]);
     }
-    __device__ static __forceinline__ void pair(float v0, float v1, uint32_t& hi, uint32_t& lo) {
-        const __nv_bfloat162 a = __floats2bfloat162_rn(v0, v1);
-        const float2 b = __bfloat1622float2(a);
-        const __nv_bfloat162 c = __floats2bfloat162_rn(v0 - b.x, v1 - b.y);
-        hi = *reinterpret_cast<const uint32_t*>(&a);
-        lo = *reinterpret_cast<const uint32_t*>(&c);
-    }
 };
 
-struct TcSmem {
-    static constexpr int A = 32768;            // per hi / lo
-    static constexpr int B1 = 2048;            // 32 x 32 x 2 B
-    static constexpr int B2 = 8192;            // 64 x 64 x 2 B
-    static constexpr int off_ahi = 0;
-    static constexpr int off_alo = A;
-    static constexpr int off_b1hi = 2 * A;
-    static constexpr int off_b1lo = off_b1hi + B1;
-    static constexpr int off_b2hi = off_b1lo + B1;
-    static constexpr int off_b2lo = off_b2hi + B2;
-    static constexpr int off_misc = off_b2lo + B2;  // 86016
-    static constexpr int misc = 1024;
-    // + 1024 for aligning the base
-    static constexpr int bytes = off_misc + misc + 1024;
-};
-
-__device__ __forceinline__ float warp_max(float v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
-    return v;
-}
-
-__device__ __forceinline__ unsigned long long warp_max_key(unsigned long long v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
-        v = w > v ? w : v;
-    }
-    return v;
-}
-
+// Split 8 floats (times `s`) and store the hi / lo chunks at byte offset
+// `off` of the hi and lo planes.
 template <typename T>
-__global__ void __launch_bounds__(128) k_window_tc32(TcArgs a) {
-    constexpr int N = 32, H = 16, WIT = 8;
+__device__ __forceinline__ void tc_put8(unsigned char* hi_plane, unsigned char* lo_plane, int off, const float* v,
+                                        float s) {
+    float w[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) w[k] = v[k] * s;
+    uint4 hi, lo;
+    Split16<T>::run(w, hi, lo);
+    *reinterpret_cast<uint4*>(hi_plane + off) = hi;
+    *reinterpret_cast<uint4*>(lo_plane + off) = lo;
+}
+
+template <int N, typename T>
+__global__ void __launch_bounds__(256, TcCfg<N>::MINB) k_window_tc(TcArgs a) {
+    using C = TcCfg<N>;
+    constexpr int H = C::H, N8 = C::N8, K1 = C::K1, K2 = C::K2, WIT = C::WIT, R2 = C::R2;
     constexpr uint64_t kLimit = 2000000000ull;  // 2 s per wait
-    using SP = Split16<T>;
     extern __shared__ unsigned char sm_raw[];
-    // 1024-byte aligned base for the operand buffers
     unsigned char* sm = reinterpret_cast<unsigned char*>(
         (reinterpret_cast<uintptr_t>(sm_raw) + 1023) & ~static_cast<uintptr_t>(1023));
-    unsigned char* Ahi = sm + TcSmem::off_ahi;
-    unsigned char* Alo = sm + TcSmem::off_alo;
-    unsigned char* B1hi = sm + TcSmem::off_b1hi;
-    unsigned char* B1lo = sm + TcSmem::off_b1lo;
-    unsigned char* B2hi = sm + TcSmem::off_b2hi;
-    unsigned char* B2lo = sm + TcSmem::off_b2lo;
-    float* s_g = reinterpret_cast<float*>(sm + TcSmem::off_misc);  // 65 (+pad)
-    float* s_f = s_g + 80;                                         // 32
-    int* s_pix = reinterpret_cast<int*>(s_f + 32);                 // 8
-    float4* s_mean = reinterpret_cast<float4*>(sm + TcSmem::off_misc + 512);  // 8
-    uint64_t* s_mbar = reinterpret_cast<uint64_t*>(sm + TcSmem::off_misc + 640);
-    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(sm + TcSmem::off_misc + 648);
-    uint64_t* s_never = reinterpret_cast<uint64_t*>(sm + TcSmem::off_misc + 696);  // test hook only
-    int* s_gi = reinterpret_cast<int*>(sm + TcSmem::off_misc + 656);                    // 8
-    const float2** s_src = reinterpret_cast<const float2**>(sm + TcSmem::off_misc + 704);  // 8 x 2
-    int2* s_dim = reinterpret_cast<int2*>(sm + TcSmem::off_misc + 832);                 // 8
+    unsigned char* Ahi = sm;
+    unsigned char* Bm = sm + C::AREG;  // B1 hi, B1 lo, B2 hi, B2 lo
+    unsigned char* B1hi = Bm;
+    unsigned char* B1lo = Bm + C::B1B;
+    unsigned char* B2hi = Bm + 2 * C::B1B;
+    unsigned char* B2lo = B2hi + C::B2B;
+    unsigned char* misc = Bm + C::BB;
+    float* s_g = reinterpret_cast<float*>(misc);                            // 2 kMaxBox + 1
+    float* s_f = s_g + 2 * kMaxBox + 4;                                      // kMaxBox
+    uint64_t* s_mbar = reinterpret_cast<uint64_t*>(misc + 800);             // MMA completion
+    uint64_t* s_never = s_mbar + 1;                                          // test hook only
+    uint64_t* s_bbar = s_mbar + 2;                                           // matrix copy
+    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(misc + 832);
+    int* s_gi = reinterpret_cast<int*>(misc + 848);                          // WIT
+    int4* s_geo = reinterpret_cast<int4*>(misc + 912);                       // WIT: imin, jmin, gr off, gc off
+    float4* s_mean = reinterpret_cast<float4*>(misc + 1168);                 // WIT
+    const float2** s_src = reinterpret_cast<const float2**>(misc + 1424);   // 2 WIT: box origins
+    int* s_ny = reinterpret_cast<int*>(misc + 1680);                         // WIT
+    unsigned* s_wmax = reinterpret_cast<unsigned*>(misc + 1744);             // WIT
+    int* s_widx = reinterpret_cast<int*>(misc + 1808);                       // WIT
+    int* s_wnan = reinterpret_cast<int*>(misc + 1872);                       // WIT
+    int* s_valid = reinterpret_cast<int*>(misc + 1936);                      // WIT
+    static_assert(WIT <= 16, "window slots in the misc region");
 
-    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    const int t = threadIdx.x, wp = t >> 5, lane = t & 31;
+    const int qd = wp & 3, hf = wp >> 2;  // TMEM lane quadrant, half of the stage's columns
+    const uint32_t lane_base = (uint32_t)(qd * 32) << 16;
 
-    // ---- constant DFT matrices, split, K-major (n, k) layout --------------
-    for (int e = t; e < 32 * 32 / 8; e += 128) {  // B1: n = c, k = j; 8 k per store
-        const int n = e / 4, kc = e % 4;
-        float v[8];
-#pragma unroll
-        for (int q = 0; q < 8; ++q) v[q] = a.b1[n * 32 + kc * 8 + q];
-        uint4 hi, lo;
-        SP::run(v, hi, lo);
-        const int off = (n % 8) * 16 + (n / 8) * 512 + kc * 128;
-        *reinterpret_cast<uint4*>(B1hi + off) = hi;
-        *reinterpret_cast<uint4*>(B1lo + off) = lo;
-    }
-    for (int e = t; e < 64 * 64 / 8; e += 128) {  // B2: n = (p', kx), k = (p, i)
-        const int n = e / 8, kc = e % 8;
-        float v[8];
-#pragma unroll
-        for (int q = 0; q < 8; ++q) v[q] = a.b2[n * 64 + kc * 8 + q];
-        uint4 hi, lo;
-        SP::run(v, hi, lo);
-        const int off = (n % 8) * 16 + (n / 8) * 1024 + kc * 128;
-        *reinterpret_cast<uint4*>(B2hi + off) = hi;
-        *reinterpret_cast<uint4*>(B2lo + off) = lo;
-    }
-    for (int k = t; k < 2 * N + 1; k += 128) s_g[k] = a.gauss[k];
-    for (int k = t; k < N; k += 128) s_f[k] = a.use_filter ? a.filt2[k] : 1.0f;
-    if (warp == 0) tc::tmem_alloc(s_tmem, 256);
+    for (int k = t; k < 2 * kMaxBox + 1; k += 256) s_g[k] = a.gauss[k];
+    for (int k = t; k < kMaxBox; k += 256) s_f[k] = a.use_filter ? a.filt2[k] : 1.0f;
+    if (wp == 0) tc::tmem_alloc(s_tmem, C::TCOLS);
     if (t == 0) {
         tc::mbar_init(s_mbar, 1);
         tc::mbar_init(s_never, 1);
+        tc::mbar_init(s_bbar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    tc::fence_async_smem();
+    __syncthreads();
+    // the constant matrices: two bulk copies by the TMA engine
+    if (t == 0) {
+        tc::mbar_expect_tx(s_bbar, (uint32_t)C::BB);
+        tc::bulk_g2s(Bm, a.bmat, (uint32_t)(2 * C::B1B), s_bbar);
+        tc::bulk_g2s(Bm + 2 * C::B1B, reinterpret_cast<const unsigned char*>(a.bmat) + 2 * C::B1B,
+                     (uint32_t)(2 * C::B2B), s_bbar);
+    }
+    const bool bok = tc::mbar_wait(s_bbar, 0u, kLimit);
     tc::fence_before();
     __syncthreads();
     tc::fence_after();
     const uint32_t tmem = *s_tmem;
-    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
 
-    constexpr uint32_t id1 = tc::idesc(SP::fmt, 128, 32, false, false);
-    constexpr uint32_t id2 = tc::idesc(SP::fmt, 128, 64, true, false);
-    constexpr uint32_t id3 = tc::idesc(SP::fmt, 128, 64, false, true);
-    constexpr uint32_t id4 = tc::idesc(SP::fmt, 128, 32, true, true);
-    const uint32_t ahi = tc::smem_u32(Ahi), alo = tc::smem_u32(Alo);
+    constexpr uint32_t id1 = tc::idesc(Split16<T>::fmt, 128, K1, true, false);
+    constexpr uint32_t id2 = tc::idesc(Split16<T>::fmt, 128, K2, true, false);
+    constexpr uint32_t id3 = tc::idesc(Split16<T>::fmt, 128, K2, false, true);
+    constexpr uint32_t id4 = tc::idesc(Split16<T>::fmt, 128, K1, true, true);
+    const uint32_t ahi = tc::smem_u32(Ahi);
     const uint32_t b1hi = tc::smem_u32(B1hi), b1lo = tc::smem_u32(B1lo);
     const uint32_t b2hi = tc::smem_u32(B2hi), b2lo = tc::smem_u32(B2lo);
 
+    grid_dep_wait();  // work list, means and counters come from earlier kernels
     const int nwork = *a.nwork;
     uint32_t phase = 0;
-    bool ok = true;
+    bool ok = __syncthreads_and(bok ? 1 : 0) != 0;
 
-    // issue hi*hi + hi*lo + lo*hi for one K step of 16
     auto mma3 = [&](uint32_t d, uint64_t ah, uint64_t al, uint64_t bh, uint64_t bl, uint32_t id, uint32_t acc) {
         tc::mma(d, ah, bh, id, acc);
         tc::mma(d, ah, bl, id, 1u);
         tc::mma(d, al, bh, id, 1u);
     };
-    // all threads: wait for the stage's MMAs; any timeout stops the kernel
     auto wait_stage = [&]() -> bool {
         const bool done =
             a.stall_ns ? tc::mbar_wait(s_never, 0u, a.stall_ns) : tc::mbar_wait(s_mbar, phase, kLimit);
@@ -257,76 +296,102 @@ __global__ void __launch_bounds__(128) k_window_tc32(TcArgs a) {
     };
 
     for (int base = blockIdx.x * WIT; base < nwork && ok; base += gridDim.x * WIT) {
+        // ---- window table --------------------------------------------------
         if (t < WIT) {
-            int w = min(base + t, nwork - 1);
+            const bool valid = base + t < nwork;
+            int w = valid ? base + t : nwork - 1;
             const float2* f1s = a.s1;
             const float2* f2s = a.s2;
-            int2 dim = make_int2(a.nx, a.ny);
+            int nx = a.nx, ny = a.ny;
             if (a.nseg > 0) {
                 const int k = seg_find(a.seg_start, a.nseg, w);
                 const WinSeg sg = a.segs[k];
                 f1s = sg.s1;
                 f2s = sg.s2;
-                dim = make_int2(sg.nx, sg.ny);
+                nx = sg.nx;
+                ny = sg.ny;
                 w = sg.base + (w - __ldg(a.seg_start + k));
             }
+            const int pix = a.work[w];
+            int ic, jc, imin, jmin;
+            if (a.direct) {
+                imin = pix / ny;
+                jmin = 0;
+                ic = imin;
+                jc = 0;
+            } else {
+                ic = pix / ny;
+                jc = pix - ic * ny;
+                imin = box_start(ic, nx, a.nsize);
+                jmin = box_start(jc, ny, a.nsize);
+            }
             s_gi[t] = w;
-            s_src[2 * t] = f1s;
-            s_src[2 * t + 1] = f2s;
-            s_dim[t] = dim;
-            s_pix[t] = a.work[w];
+            s_valid[t] = valid ? 1 : 0;
+            s_geo[t] = make_int4(imin, jmin, imin - ic + N, jmin - jc + N);
+            s_src[2 * t] = f1s + (size_t)imin * ny + jmin;
+            s_src[2 * t + 1] = f2s + (size_t)imin * ny + jmin;
+            s_ny[t] = ny;
             s_mean[t] = a.means ? a.means[w] : make_float4(0.f, 0.f, 0.f, 0.f);
+            s_wmax[t] = 0u;
+            s_widx[t] = 0x7fffffff;
+            s_wnan[t] = 0;
         }
         __syncthreads();
 
-        // ---- phase 0: windows -> A1 (K-major, 4 tiles of 128 rows) -------
+        // ---- stage 0: boxes -> A1 (MN-major; lane = box column) ------------
         {
-            // warp (wl, img) of each tile; lane = column j, rows read
-            // cooperatively (coalesced), values scattered into the K-major rows
-            const int wl = warp >> 1, img = warp & 1;
+            unsigned char* A1lo = Ahi + C::A1B;
 #pragma unroll 1
-            for (int tile = 0; tile < 4; ++tile) {
-                const int w = 2 * tile + wl;
-                const int pix = s_pix[w];
-                const int2 dim = s_dim[w];
-                int ic, jc, imin, jmin;
-                if (a.direct) {
-                    imin = pix / dim.y;
-                    jmin = 0;
-                    ic = imin;
-                    jc = 0;
-                } else {
-                    ic = pix / dim.y;
-                    jc = pix - ic * dim.y;
-                    imin = box_start(ic, dim.x, a.nsize);
-                    jmin = box_start(jc, dim.y, a.nsize);
-                }
+            for (int sp = wp * C::SPW; sp < C::SUBS; sp += 8 * C::SPW) {
+                const int s = sp + lane / C::LW;
+                const int jl = lane % C::LW;
+                const bool sval = s < C::SUBS;
+                const int w = sval ? (s >> 1) : 0, img = s & 1;
+                const int4 geo = s_geo[w];
+                const int ny = s_ny[w];
                 const float4 mm = s_mean[w];
                 const float mh = img ? mm.z : mm.x, ml = img ? mm.w : mm.y;
-                const float2* src = s_src[2 * w + img] + (size_t)imin * dim.y + jmin + lane;
-                const float* gr = s_g + (imin - ic + N);
-                const float gc = s_g[lane + jmin - jc + N];
-                float x[32];
+                const float2* src = s_src[2 * w + img];
+                const float* gr = s_g + geo.z;
+                float x[C::CB][N8];
                 float mx = 0.f;
 #pragma unroll
-                for (int i = 0; i < 32; ++i) {
-                    const float2 u = __ldg(src + (size_t)i * dim.y);
-                    x[i] = ((u.x - mh) + (u.y - ml)) * (gr[i] * gc);
-                    mx = fmaxf(mx, fabsf(x[i]));
-                }
-                const float sc = pow2_scale(__float_as_uint(warp_max(mx)));
-                // even lanes store (j, j+1) as one 32-bit hi and one lo word
-                const int rowbase = tile * 8192 + (wl * 64 + img * 32) / 8 * 512 + (lane % 8) * 2 + (lane / 8) * 128;
+                for (int cb = 0; cb < C::CB; ++cb) {
+                    const int j = cb * 32 + jl;
+                    const bool jv = sval && j < N;
+                    const float gc = jv ? s_g[geo.w + j] : 0.f;
+                    if (jv) {
 #pragma unroll
-                for (int i = 0; i < 32; ++i) {
-                    const float v = x[i] * sc;
-                    const float vn = __shfl_down_sync(0xffffffffu, v, 1);
-                    if ((lane & 1) == 0) {
-                        uint32_t hi, lo;
-                        SP::pair(v, vn, hi, lo);
-                        const int off = rowbase + (i % 8) * 16 + (i / 8) * 512;
-                        *reinterpret_cast<uint32_t*>(Ahi + off) = hi;
-                        *reinterpret_cast<uint32_t*>(Alo + off) = lo;
+                        for (int i = 0; i < N8; ++i) {
+                            if (i < N) {
+                                const float2 u = __ldg(src + (size_t)i * ny + j);
+                                x[cb][i] = ((u.x - mh) + (u.y - ml)) * (gr[i] * gc);
+                                mx = fmaxf(mx, fabsf(x[cb][i]));
+                            } else {
+                                x[cb][i] = 0.f;
+                            }
+                        }
+                    } else {
+#pragma unroll
+                        for (int i = 0; i < N8; ++i) x[cb][i] = 0.f;
+                    }
+                }
+#pragma unroll
+                for (int o = C::LW / 2; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+                const float sc = pow2_scale(__float_as_uint(mx));
+                if (sval) {
+#pragma unroll
+                    for (int cb = 0; cb < C::CB; ++cb) {
+                        const int j = cb * 32 + jl;
+                        if (j < K1) {
+#pragma unroll
+                            for (int g = 0; g < N8 / 8; ++g) {
+                                const int row = s * N8 + 8 * g;
+                                const int off = (row >> 7) * (128 * K1 * 2) + ((row & 127) >> 3) * 128 + (j & 7) * 16 +
+                                                (j >> 3) * 2048;
+                                tc_put8<T>(Ahi, A1lo, off, &x[cb][8 * g], sc);
+                            }
+                        }
                     }
                 }
             }
@@ -335,11 +400,11 @@ __global__ void __launch_bounds__(128) k_window_tc32(TcArgs a) {
         if (t == 0) {
             // consecutive MMAs go to different accumulators (tiles) so that
             // the tensor pipe can overlap them
-            for (int s = 0; s < 2; ++s)
-                for (int tile = 0; tile < 4; ++tile)
-                    mma3(tmem + 32 * tile, tc::desc(ahi + tile * 8192 + s * 256, 128, 512),
-                         tc::desc(alo + tile * 8192 + s * 256, 128, 512), tc::desc(b1hi + s * 256, 128, 512),
-                         tc::desc(b1lo + s * 256, 128, 512), id1, s > 0);
+            for (int s = 0; s < K1 / 16; ++s)
+                for (int tl = 0; tl < C::T1; ++tl)
+                    mma3(tmem + tl * K1, tc::desc(ahi + tl * (128 * K1 * 2) + s * 4096, 2048, 128),
+                         tc::desc(ahi + C::A1B + tl * (128 * K1 * 2) + s * 4096, 2048, 128),
+                         tc::desc(b1hi + s * 256, 128, K1 * 16), tc::desc(b1lo + s * 256, 128, K1 * 16), id1, s > 0);
             tc::commit(s_mbar);
         }
         if (!wait_stage()) {
@@ -347,37 +412,50 @@ __global__ void __launch_bounds__(128) k_window_tc32(TcArgs a) {
             break;
         }
 
-        // ---- phase 1: D1 rows -> A2 (MN-major, 2 tiles) ---------------------
+        // ---- stage 1: T rows -> A2 (MN-major rows (ky group, window, ky lo)) --
         {
-            const int wl = t >> 6, img = (t >> 5) & 1, i = t & 31;
+            unsigned char* A2lo = Ahi + 2 * C::A2B;
 #pragma unroll 1
-            for (int tile = 0; tile < 4; ++tile) {
-                float d[32];
-                tc::tmem_ld32(tmem + lane_base + 32 * tile, d);
-                const int w = 2 * tile + wl;
-                // rows m = w*16 + kc (two m-cores), K block of this image
-                const int base2 = img * 16384 + (2 * w) * 128 + (i % 8) * 16;
-#pragma unroll
-                for (int part = 0; part < 2; ++part) {
-                    const int off = base2 + (part * 4 + i / 8) * 2048;
-                    uint4 hi, lo;
-                    SP::run(d + 16 * part, hi, lo);
-                    *reinterpret_cast<uint4*>(Ahi + off) = hi;
-                    *reinterpret_cast<uint4*>(Alo + off) = lo;
-                    SP::run(d + 16 * part + 8, hi, lo);
-                    *reinterpret_cast<uint4*>(Ahi + off + 128) = hi;
-                    *reinterpret_cast<uint4*>(Alo + off + 128) = lo;
+            for (int tl = 0; tl < C::T1; ++tl) {
+                const int g = tl * 128 + qd * 32 + lane;  // S1 row
+                const int s = g / N8, i = g - s * N8;
+                float v[K1];
+                tc::tmem_ld<K1>(tmem + lane_base + tl * K1, v);
+                if (s < C::SUBS) {
+                    const int w = s >> 1, img = s & 1;
+                    sfor<0, 2 * C::G2>([&](auto chc) {
+                        constexpr int ch = decltype(chc)::value;
+                        constexpr int p = ch / C::G2, g2 = ch % C::G2;
+                        if ((ch & 1) == hf) {
+                            float c8[8];
+                            sfor<0, 8>([&](auto kc) {
+                                constexpr int kk = decltype(kc)::value;
+                                constexpr int ky = 8 * g2 + kk;
+                                if constexpr (p == 0) {
+                                    c8[kk] = (ky <= H) ? v[ky <= H ? ky : 0] : 0.f;
+                                } else if constexpr (C::PACK) {
+                                    c8[kk] = v[ky == 0 ? H : H + ky];
+                                } else {
+                                    c8[kk] = (ky > 0 && ky < H) ? v[(ky > 0 && ky < H) ? H + ky : 0] : 0.f;
+                                }
+                            });
+                            const int mn = (g2 * WIT + w) * 8;
+                            const int k = p * N8 + i;
+                            const int off = img * C::A2B + (mn >> 3) * 128 + (k & 7) * 16 + (k >> 3) * 2048;
+                            tc_put8<T>(Ahi, A2lo, off, c8, 1.0f);
+                        }
+                    });
                 }
             }
         }
         tc::fence_before();
         to_mma();
         if (t == 0) {
-            for (int s = 0; s < 4; ++s)
+            for (int s = 0; s < K2 / 16; ++s)
                 for (int img = 0; img < 2; ++img)
-                    mma3(tmem + 128 + 64 * img, tc::desc(ahi + img * 16384 + s * 4096, 2048, 128),
-                         tc::desc(alo + img * 16384 + s * 4096, 2048, 128), tc::desc(b2hi + s * 256, 128, 1024),
-                         tc::desc(b2lo + s * 256, 128, 1024), id2, s > 0);
+                    mma3(tmem + img * K2, tc::desc(ahi + img * C::A2B + s * 4096, 2048, 128),
+                         tc::desc(ahi + 2 * C::A2B + img * C::A2B + s * 4096, 2048, 128),
+                         tc::desc(b2hi + s * 256, 128, K2 * 16), tc::desc(b2lo + s * 256, 128, K2 * 16), id2, s > 0);
             tc::commit(s_mbar);
         }
         if (!wait_stage()) {
@@ -385,177 +463,256 @@ __global__ void __launch_bounds__(128) k_window_tc32(TcArgs a) {
             break;
         }
 
-        // ---- phase 2: spectra -> conj(A) B filt^2 -> A3 (K-major) --------
+        // ---- stage 2: spectra -> conj(A) B filt^2 -> A3 (K-major) ----------
         {
-            // row t = (window w, packed column kc); both images in one lane
-            const int kc = t & 15;
-            const float h0 = kc ? 1.0f : 0.5f, z6 = kc ? 0.0f : 0.5f;
-            const float fk0 = kc ? s_f[kc] : s_f[0], fk6 = s_f[H];
-            float ur[32], ui[32];
-            float mx = 0.f;
-            sfor<0, 2>([&](auto hc) {
-                constexpr int half = decltype(hc)::value;
-                // columns q in [16 half, 16 half + 16): complete (kx, -kx) pairs
-                float ar[16], ai[16], br[16], bi[16];
-                tc::tmem_ld16(tmem + lane_base + 128 + 16 * half, ar);
-                tc::tmem_ld16(tmem + lane_base + 160 + 16 * half, ai);
-                tc::tmem_ld16(tmem + lane_base + 192 + 16 * half, br);
-                tc::tmem_ld16(tmem + lane_base + 224 + 16 * half, bi);
-                sfor<0, 16>([&](auto qc) {
-                    constexpr int qq = decltype(qc)::value;
-                    constexpr int q = 16 * half + qq;
-                    constexpr int mq = tc_mirror(q) - 16 * half;  // mirror within this half
-                    const float Ar = ar[qq], Ai = ai[qq], Br = br[qq], Bi = bi[qq];
-                    const float sr = kc ? 0.0f : ar[mq], si = kc ? 0.0f : ai[mq];
-                    const float tr = kc ? 0.0f : br[mq], ti = kc ? 0.0f : bi[mq];
-                    const float a0r = h0 * (Ar + sr), a0i = h0 * (Ai - si);
-                    const float a6r = z6 * (Ai + si), a6i = z6 * (sr - Ar);
-                    const float b0r = h0 * (Br + tr), b0i = h0 * (Bi - ti);
-                    const float b6r = z6 * (Bi + ti), b6i = z6 * (tr - Br);
-                    const float fx = s_f[tc_kx(q)];
-                    const float f0 = fx * fk0, f6 = fx * fk6;
-                    const float c0r = f0 * (a0r * b0r + a0i * b0i), c0i = f0 * (a0r * b0i - a0i * b0r);
-                    const float c6r = f6 * (a6r * b6r + a6i * b6i), c6i = f6 * (a6r * b6i - a6i * b6r);
-                    ur[q] = c0r - c6i;  // u = C0 + i C16 (C16 = 0 for kc > 0)
-                    ui[q] = c0i + c6r;
-                    mx = fmaxf(mx, fmaxf(fabsf(ur[q]), fabsf(ui[q])));
-                });
-            });
-#pragma unroll
-            for (int o = 8; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-            const float sc = pow2_scale(__float_as_uint(mx));
-#pragma unroll
-            for (int q = 0; q < 32; ++q) {
-                ur[q] *= sc;
-                ui[q] *= sc;
-            }
-            const int rowoff = (t % 8) * 16 + (t / 8) * 1024;
-#pragma unroll
-            for (int part = 0; part < 2; ++part) {
-                const float* src = part ? ui : ur;
-#pragma unroll
-                for (int c = 0; c < 4; ++c) {
-                    uint4 hi, lo;
-                    SP::run(src + 8 * c, hi, lo);
-                    const int kcore = part * 4 + c;
-                    *reinterpret_cast<uint4*>(Ahi + rowoff + kcore * 128) = hi;
-                    *reinterpret_cast<uint4*>(Alo + rowoff + kcore * 128) = lo;
-                }
-            }
-        }
-        tc::fence_before();
-        to_mma();
-        if (t == 0) {
-            for (int s = 0; s < 4; ++s)
-                mma3(tmem, tc::desc(ahi + s * 256, 128, 1024), tc::desc(alo + s * 256, 128, 1024),
-                     tc::desc(b2hi + s * 2048, 1024, 128), tc::desc(b2lo + s * 2048, 1024, 128), id3, s > 0);
-            tc::commit(s_mbar);
-        }
-        if (!wait_stage()) {
-            ok = false;
-            break;
-        }
-
-        // ---- phase 3: D3 rows -> A4 (MN-major, 2 tiles) ---------------------
-        {
-            const int wg = t >> 4, kc = t & 15;
-            float ur[32], ui[32];
-            tc::tmem_ld32(tmem + lane_base, ur);
-            tc::tmem_ld32(tmem + lane_base + 32, ui);
-            const float wgt = kc ? 2.0f : 1.0f;  // c2r weights of ky = 1..15
-#pragma unroll
-            for (int q = 0; q < 32; ++q) {
-                ur[q] *= wgt;
-                ui[q] *= wgt;
-            }
-            const int t4 = wg >> 2, wl4 = wg & 3;
-#pragma unroll
-            for (int part = 0; part < 2; ++part) {
-                const int k = part * 16 + kc;
-                const float* src = part ? ui : ur;
-#pragma unroll
-                for (int c = 0; c < 4; ++c) {
-                    const int off = t4 * 8192 + (wl4 * 4 + c) * 128 + (k % 8) * 16 + (k / 8) * 2048;
-                    uint4 hi, lo;
-                    SP::run(src + 8 * c, hi, lo);
-                    *reinterpret_cast<uint4*>(Ahi + off) = hi;
-                    *reinterpret_cast<uint4*>(Alo + off) = lo;
-                }
-            }
-        }
-        tc::fence_before();
-        to_mma();
-        if (t == 0) {
-            for (int s = 0; s < 2; ++s)
-                for (int t4 = 0; t4 < 2; ++t4)
-                    mma3(tmem + 128 + 32 * t4, tc::desc(ahi + t4 * 8192 + s * 4096, 2048, 128),
-                         tc::desc(alo + t4 * 8192 + s * 4096, 2048, 128), tc::desc(b1hi + s * 1024, 512, 128),
-                         tc::desc(b1lo + s * 1024, 512, 128), id4, s > 0);
-            tc::commit(s_mbar);
-        }
-        if (!wait_stage()) {
-            ok = false;
-            break;
-        }
-
-        // ---- phase 4: |c|, first strict maximum, peak record -----------------
-        {
-            float* stage = reinterpret_cast<float*>(Ahi) + warp * 32 * 33;  // 32 x 32 per warp, row stride 33
+            unsigned char* A3lo = Ahi + C::A3B;
+            const int mn = qd * 32 + lane;  // S2 row
+            const int grp = mn >> 3, g2 = grp / WIT, w = grp - g2 * WIT;
+            const int ky = g2 * 8 + (mn & 7);
+            const bool valid = g2 < C::G2 && ky < C::KYN;
+            const bool special = C::PACK && ky == 0;  // packed ky = 0 / H row
+            const float cs = __uint_as_float((uint32_t)(127 - C::CSH1) << 23) * (special ? 0.25f : 1.0f);
+            const float fk = s_f[valid ? ky : 0];
+            const float f0 = s_f[0], fH = s_f[H];
 #pragma unroll 1
-            for (int t4 = 0; t4 < 2; ++t4) {
-                float c[32];
-                tc::tmem_ld32(tmem + lane_base + 128 + 32 * t4, c);
-                const int i = lane;
-                const int I = (i + H) & 31;
-                unsigned long long best = 0ull;
+            for (int qc = hf; qc < C::QC; qc += 2) {
+                float yr1[8], yi1[8], yr2[8], yi2[8];
+                {
+                    uint32_t r0[8], r1[8], r2[8], r3[8];
+                    const uint32_t tb = tmem + lane_base + 8 * qc;
+                    tc::tmem_ld8_nw(tb, r0);
+                    tc::tmem_ld8_nw(tb + N8, r1);
+                    tc::tmem_ld8_nw(tb + K2, r2);
+                    tc::tmem_ld8_nw(tb + K2 + N8, r3);
+                    tc::tmem_wait_ld();
 #pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    const int J = (j + H) & 31;
-                    const float v = fabsf(c[j]);
-                    stage[I * 33 + J] = v;
-                    if (!(v != v)) {
-                        const unsigned long long key = ((unsigned long long)__float_as_uint(v) << 32) |
-                                                       (unsigned long long)(0xffffffffu - (unsigned)(I * 32 + J));
-                        best = key > best ? key : best;
+                    for (int k = 0; k < 8; ++k) {
+                        yr1[k] = __uint_as_float(r0[k]);
+                        yi1[k] = __uint_as_float(r1[k]);
+                        yr2[k] = __uint_as_float(r2[k]);
+                        yi2[k] = __uint_as_float(r3[k]);
                     }
                 }
-                best = warp_max_key(best);
-                __syncwarp();
-                const int wg = 4 * t4 + warp;
-                const bool valid = base + wg < nwork;
+                if (!valid) continue;
+                float ur[8], ui[8];
+                if (!special) {
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) {
+                        ur[k] = yr1[k] * yr2[k] + yi1[k] * yi2[k];
+                        ui[k] = yr1[k] * yi2[k] - yi1[k] * yr2[k];
+                    }
+                    if (a.use_filter) {
+                        sfor<0, 8>([&](auto kc) {
+                            constexpr int k = decltype(kc)::value;
+                            // wavenumber of column 8 qc + k (qc is the loop's
+                            // runtime index; the table is read by column)
+                            const int q = 8 * qc + k;
+                            const int kx = C::PACK ? tc_kx(q, N) : q;
+                            const float f = s_f[kx < N ? kx : 0] * fk;
+                            ur[k] *= f;
+                            ui[k] *= f;
+                        });
+                    }
+                } else {
+                    // packed row: Y = A0 + i AH and Z = B0 + i BH with A0, AH,
+                    // B0, BH the (Hermitian) spectra of the real columns ky = 0
+                    // and ky = H: 2 A0 = Y + Ym, 2i AH = Y - Ym (Ym = conj Y(-kx));
+                    // u = f0 conj(A0) B0 + i fH conj(AH) BH (the 1/4 is in cs)
+                    sfor<0, 8>([&](auto kc) {
+                        constexpr int k = decltype(kc)::value;
+                        // chunks hold whole mirror pairs: columns 0 and 1 of
+                        // the first chunk are their own mirrors (kx = 0, H),
+                        // every other column pairs with its neighbour
+                        const bool self = qc == 0 && k < 2;
+                        const float mr1 = self ? yr1[k] : yr1[k ^ 1], mi1 = self ? yi1[k] : yi1[k ^ 1];
+                        const float mr2 = self ? yr2[k] : yr2[k ^ 1], mi2 = self ? yi2[k] : yi2[k ^ 1];
+                        const float syr = yr1[k] + mr1, syi = yi1[k] - mi1;
+                        const float dyr = yr1[k] - mr1, dyi = yi1[k] + mi1;
+                        const float szr = yr2[k] + mr2, szi = yi2[k] - mi2;
+                        const float dzr = yr2[k] - mr2, dzi = yi2[k] + mi2;
+                        const float c0r = syr * szr + syi * szi, c0i = syr * szi - syi * szr;
+                        const float chr = dyr * dzr + dyi * dzi, chi = dyr * dzi - dyi * dzr;
+                        float fx = 1.0f, a0 = 1.0f, aH = 1.0f;
+                        if (a.use_filter) {
+                            const int q = 8 * qc + k;
+                            fx = s_f[tc_kx(q, N)];
+                            a0 = f0;
+                            aH = fH;
+                        }
+                        ur[k] = fx * (a0 * c0r - aH * chi);
+                        ui[k] = fx * (a0 * c0i + aH * chr);
+                    });
+                }
+                const int k0 = 8 * qc;
+                const int rowoff = (mn & 7) * 16 + (mn >> 3) * (K2 * 16);
+                tc_put8<T>(Ahi, A3lo, rowoff + (k0 >> 3) * 128, ur, cs);
+                tc_put8<T>(Ahi, A3lo, rowoff + ((N8 + k0) >> 3) * 128, ui, cs);
+            }
+        }
+        tc::fence_before();
+        to_mma();
+        if (t == 0) {
+            for (int s = 0; s < K2 / 16; ++s)
+                mma3(tmem, tc::desc(ahi + s * 256, 128, K2 * 16), tc::desc(ahi + C::A3B + s * 256, 128, K2 * 16),
+                     tc::desc(b2hi + s * 2 * (K2 * 16), K2 * 16, 128), tc::desc(b2lo + s * 2 * (K2 * 16), K2 * 16, 128),
+                     id3, s > 0);
+            tc::commit(s_mbar);
+        }
+        if (!wait_stage()) {
+            ok = false;
+            break;
+        }
+
+        // ---- stage 3: U rows -> A4 (MN-major rows (window, i)) -------------
+        {
+            unsigned char* A4lo = Ahi + C::A4B;
+            const int mn = qd * 32 + lane;
+            const int grp = mn >> 3, g2 = grp / WIT, w = grp - g2 * WIT;
+            const int ky = g2 * 8 + (mn & 7);
+            const bool valid = g2 < C::G2 && ky < C::KYN;
+            // spectral term rows k4 of S4 (ky = 0 -> 0, ky = H -> H, else
+            // ky and H + ky) and the c2r weights
+            int kre, kim;
+            float wgt;
+            constexpr float s2 = 1.0f / (float)(1 << C::CSH2);
+            if (C::PACK) {
+                kre = ky;
+                kim = ky == 0 ? H : H + ky;
+                wgt = ky == 0 ? s2 : 2.0f * s2;
+            } else {
+                kre = ky;
+                kim = (ky > 0 && ky < H) ? H + ky : -1;
+                wgt = (ky > 0 && ky < H) ? 2.0f * s2 : s2;
+            }
+            // zero the spectral-term columns k4 in [N, K1) (no row writes them)
+            if constexpr (K1 > N) {
+                for (int e = t; e < C::T4 * 16 * (K1 - N); e += 256) {
+                    const int k4 = N + e % (K1 - N), rg = e / (K1 - N);  // rg: tile * 16 + row group
+                    const int off = (rg >> 4) * (128 * K1 * 2) + (rg & 15) * 128 + (k4 & 7) * 16 + (k4 >> 3) * 2048;
+                    *reinterpret_cast<uint4*>(Ahi + off) = make_uint4(0u, 0u, 0u, 0u);
+                    *reinterpret_cast<uint4*>(A4lo + off) = make_uint4(0u, 0u, 0u, 0u);
+                }
+            }
+            sfor<0, 2>([&](auto pc) {
+                constexpr int p = decltype(pc)::value;
+                float u[N8];
+                tc::tmem_ld<N8>(tmem + lane_base + p * N8, u);
+                const int k4 = p ? kim : kre;
+                if (valid && k4 >= 0) {
+#pragma unroll
+                    for (int ic = 0; ic < N8 / 8; ++ic) {
+                        if ((ic & 1) != hf) continue;
+                        const int row = w * N8 + 8 * ic;
+                        const int off = (row >> 7) * (128 * K1 * 2) + ((row & 127) >> 3) * 128 + (k4 & 7) * 16 +
+                                        (k4 >> 3) * 2048;
+                        tc_put8<T>(Ahi, A4lo, off, &u[8 * ic], wgt);
+                    }
+                }
+            });
+        }
+        tc::fence_before();
+        to_mma();
+        if (t == 0) {
+            for (int s = 0; s < K1 / 16; ++s)
+                for (int tl = 0; tl < C::T4; ++tl)
+                    mma3(tmem + tl * K1, tc::desc(ahi + tl * (128 * K1 * 2) + s * 4096, 2048, 128),
+                         tc::desc(ahi + C::A4B + tl * (128 * K1 * 2) + s * 4096, 2048, 128),
+                         tc::desc(b1hi + s * 2 * (K1 * 16), K1 * 16, 128),
+                         tc::desc(b1lo + s * 2 * (K1 * 16), K1 * 16, 128), id4, s > 0);
+            tc::commit(s_mbar);
+        }
+        if (!wait_stage()) {
+            ok = false;
+            break;
+        }
+
+        // ---- stage 4: |c|, first strict maximum, peak record ---------------
+        {
+            float* stg = reinterpret_cast<float*>(Ahi);
+            // rows of both halves: J in [0, H) <- j in [H, N); J in [H, N) <- j in [0, H)
+            auto row_pass = [&](auto jbc) {
+                constexpr int jb = decltype(jbc)::value;  // first j of this half
+                constexpr int Jb = jb ? 0 : H;             // its first J
+#pragma unroll 1
+                for (int tl = 0; tl < C::T4; ++tl) {
+                    const int r4 = tl * 128 + qd * 32 + lane;
+                    const int w = r4 / N8, i = r4 - w * N8;
+                    float c[K1];
+                    tc::tmem_ld<K1>(tmem + lane_base + tl * K1, c);
+                    if (w < WIT && i < N) {
+                        const int I = (i + H) % N;
+                        float m = 0.f;
+                        float* dst = stg + (w * N + I) * C::SROW + Jb;
+#pragma unroll
+                        for (int jj = 0; jj < H; ++jj) {
+                            m = fmaxf(m, fabsf(c[jb + jj]));
+                            dst[jj] = c[jb + jj];
+                        }
+                        if (jb == H && I == 0 && c[H] != c[H]) s_wnan[w] = 1;
+                        atomicMax(s_wmax + w, __float_as_uint(m));
+                    }
+                }
+            };
+            if (hf == 0) row_pass(std::integral_constant<int, H>{});
+            else row_pass(std::integral_constant<int, 0>{});
+            __syncthreads();
+            // candidates: rows whose half holds the window maximum
+#pragma unroll 1
+            for (int tl = 0; tl < C::T4; ++tl) {
+                const int r4 = tl * 128 + qd * 32 + lane;
+                const int w = r4 / N8, i = r4 - w * N8;
+                if (w < WIT && i < N) {
+                    const unsigned wm = s_wmax[w];
+                    const int I = (i + H) % N;
+                    const int Jb = hf ? H : 0;
+                    const float* row = stg + (w * N + I) * C::SROW + Jb;
+                    if (wm != 0u) {
+                        const float fm = __uint_as_float(wm);
+                        for (int jj = 0; jj < H; ++jj) {
+                            if (fabsf(row[jj]) == fm) {
+                                atomicMin(s_widx + w, I * N + Jb + jj);
+                                break;
+                            }
+                        }
+                    }
+                }
+            }
+            __syncthreads();
+            // peak records: one window per group of 64 threads
+            for (int e = t; e < WIT * 64; e += 256) {
+                const int w = e >> 6, k = e & 63;
+                if (!s_valid[w]) continue;
                 int Ip, Jp;
                 bool have;
-                const float v0 = stage[0];
-                if (v0 != v0) {
+                if (s_wnan[w]) {
                     Ip = 0;
                     Jp = 0;
                     have = true;
                 } else {
-                    const unsigned L = 0xffffffffu - (unsigned)(best & 0xffffffffull);
-                    have = __uint_as_float((unsigned)(best >> 32)) != 0.0f;
-                    Ip = have ? (int)(L / 32) : H;
-                    Jp = have ? (int)(L % 32) : H;
+                    have = s_wmax[w] != 0u;
+                    const int idx = s_widx[w];
+                    Ip = have ? idx / N : H;
+                    Jp = have ? idx - (idx / N) * N : H;
                 }
-                const bool dofit = have && Ip > 0 && Ip < N - 1 && Jp > 0 && Jp < N - 1;
-                if (valid && a.peaks_h) {
-                    // -h: the 6x6 patch around the peak, 37 words
-                    float* rec = reinterpret_cast<float*>(a.peaks_h + s_gi[wg]);
-                    for (int k = lane; k < kHiresPatch * kHiresPatch + 1; k += 32) {
+                const float* sw = stg + w * N * C::SROW;
+                if (a.peaks_h) {
+                    if (k < kHiresPatch * kHiresPatch + 1) {
+                        float* rec = reinterpret_cast<float*>(a.peaks_h + s_gi[w]);
                         if (k < kHiresPatch * kHiresPatch) {
                             const int r = Ip - 2 + k / kHiresPatch, cc = Jp - 2 + k % kHiresPatch;
-                            rec[k] = (r >= 0 && r < N && cc >= 0 && cc < N) ? stage[r * 33 + cc] : 0.f;
+                            rec[k] = (r >= 0 && r < N && cc >= 0 && cc < N) ? fabsf(sw[r * C::SROW + cc]) : 0.f;
                         } else {
                             rec[k] = __uint_as_float(peak_meta(Ip, Jp, have));
                         }
                     }
-                } else if (valid && lane < 10) {
-                    float* rec = reinterpret_cast<float*>(a.peaks + s_gi[wg]);
-                    if (lane < 9)
-                        rec[lane] = dofit ? stage[(Ip - 1 + lane / 3) * 33 + (Jp - 1 + lane % 3)] : 0.f;
+                } else if (k < 10) {
+                    const bool dofit = have && Ip > 0 && Ip < N - 1 && Jp > 0 && Jp < N - 1;
+                    float* rec = reinterpret_cast<float*>(a.peaks + s_gi[w]);
+                    if (k < 9)
+                        rec[k] = dofit ? fabsf(sw[(Ip - 1 + k / 3) * C::SROW + (Jp - 1 + k % 3)]) : 0.f;
                     else
                         rec[9] = __uint_as_float(peak_meta(Ip, Jp, dofit));
                 }
-                __syncwarp();
             }
         }
         tc::fence_before();
@@ -571,12 +728,17 @@ __global__ void __launch_bounds__(128) k_window_tc32(TcArgs a) {
     tc::fence_before();
     __syncthreads();
     tc::fence_after();
-    if (warp == 0) tc::tmem_dealloc(tmem, 256);
+    if (wp == 0) tc::tmem_dealloc(tmem, C::TCOLS);
 }
 
-template <typename T>
-cudaError_t launch_window_tc32(const TcArgs& a, int grid, cudaStream_t st);
-template <typename T>
-int window_tc32_blocks_per_sm();
+template <int N, typename T>
+cudaError_t launch_window_tc(const TcArgs& a, int grid, cudaStream_t st, bool pdl);
+template <int N, typename T>
+int window_tc_blocks_per_sm();
+
+// Host-side construction of the split DFT matrices in their shared-memory
+// layouts (TcArgs::bmat, TcCfg<n>::BB bytes): fmt 0 = FP16, 1 = BF16.
+void tc_build_bmat(int n, int fmt, std::vector<uint16_t>* out);
+int tc_bmat_bytes(int n);
 
 }  // namespace flct

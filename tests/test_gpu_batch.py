@@ -105,7 +105,7 @@ def test_batch_equals_single_pairs(form):
 
 
 def test_batch_tensor_core_form_equals_single():
-    specs = [s for s in SPECS if s[1]["sigma"] == 8]
+    specs = list(SPECS)
     frames = frames_for(specs, 12)
     b = run_batch(specs, frames, "tc_fp16")
     for k, ((f1, f2), (_, kw, _)) in enumerate(zip(frames, specs)):
@@ -158,9 +158,10 @@ def test_batch_errors_and_empty():
         b.run()
     assert e.value.code == _lib.ERR_SKIP_NONPOSITIVE
     assert "pair 1" in e.value.message
-    tc = FlctBatch([(40, 40)], [make_params(1.0, 1.0, 4, form="tc_fp16")])
+    # a box above 64 (sigma 16) has no window kernel of either form
+    big = FlctBatch([(220, 220)], [make_params(1.0, 1.0, 16, form="tc_fp16")])
     with pytest.raises(FlctError) as e:
-        tc.run()
+        big.run()
     assert e.value.code == _lib.ERR_UNSUPPORTED
     empty = FlctBatch([], [])
     empty.run()
