@@ -56,9 +56,13 @@ def build(force: bool = False, jobs: int | None = None, verbose: bool = False) -
         if force or _stale(o, s, headers):
             todo.append((s, o))
 
+    # extra nvcc flags, e.g. -DFLCT_TC_PROFILE for the tensor-core kernel's
+    # per-stage clock counters (objects then rebuild: pass --force)
+    extra = os.environ.get("FLCT_NVCC_EXTRA", "").split()
+
     def run(so):
         s, o = so
-        cmd = [cc] + ARCH + NVFLAGS + ["-c", s, "-o", o]
+        cmd = [cc] + ARCH + NVFLAGS + extra + ["-c", s, "-o", o]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed on {os.path.basename(s)}:\n{r.stderr}")

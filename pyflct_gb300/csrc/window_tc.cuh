@@ -118,7 +118,11 @@ struct TcCfg {
     static constexpr int A2B = 128 * K2 * 2;                  // per image
     static constexpr int A3B = 128 * K2 * 2;
     static constexpr int A4B = T4 * 128 * K1 * 2;
-    static constexpr int SROW = N + 1;                        // staged c row, floats (odd: no bank conflicts)
+    // staged correlation rows: vectors of SV floats, row stride SROW floats
+    // (16 bytes past a multiple of 128: 16-byte stores of 8 rows hit
+    // distinct banks)
+    static constexpr int SV = (H % 4 == 0) ? 4 : 2;
+    static constexpr int SROW = N + SV;
     static constexpr int STGB = WIT * N * SROW * 4;
     static constexpr int AREG =
         (tc_max(tc_max(2 * A1B, 4 * A2B), tc_max(tc_max(2 * A3B, 2 * A4B), STGB)) + 1023) / 1024 * 1024;
@@ -163,8 +167,8 @@ struct Split16<__half> {
 #pragma unroll
         for (int p = 0; p < 4; ++p) {
             const __half2 a = __floats2half2_rn(v[2 * p], v[2 * p + 1]);
-            const float2 b = __half22float2(a);
-            const __half2 c = __floats2half2_rn(v[2 * p] - b.x, v[2 * p + 1] - b.y);
+            const float2 d = csub(make_float2(v[2 * p], v[2 * p + 1]), __half22float2(a));
+            const __half2 c = __floats2half2_rn(d.x, d.y);
             h[p] = *reinterpret_cast<const uint32_t*>(&a);
             l[p] = *reinterpret_cast<const uint32_t*>(&c);
         }
@@ -180,8 +184,8 @@ struct Split16<__nv_bfloat16> {
 #pragma unroll
         for (int p = 0; p < 4; ++p) {
             const __nv_bfloat162 a = __floats2bfloat162_rn(v[2 * p], v[2 * p + 1]);
-            const float2 b = __bfloat1622float2(a);
-            const __nv_bfloat162 c = __floats2bfloat162_rn(v[2 * p] - b.x, v[2 * p + 1] - b.y);
+            const float2 d = csub(make_float2(v[2 * p], v[2 * p + 1]), __bfloat1622float2(a));
+            const __nv_bfloat162 c = __floats2bfloat162_rn(d.x, d.y);
             h[p] = *reinterpret_cast<const uint32_t*>(&a);
             l[p] = *reinterpret_cast<const uint32_t*>(&c);
         }
@@ -197,17 +201,38 @@ __device__ __forceinline__ void tc_put8(unsigned char* hi_plane, unsigned char* 
                                         float s) {
     float w[8];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) w[k] = v[k] * s;
+    for (int k = 0; k < 8; k += 2) {
+        const float2 m = emul(make_float2(v[k], v[k + 1]), make_float2(s, s));
+        w[k] = m.x;
+        w[k + 1] = m.y;
+    }
     uint4 hi, lo;
     Split16<T>::run(w, hi, lo);
     *reinterpret_cast<uint4*>(hi_plane + off) = hi;
     *reinterpret_cast<uint4*>(lo_plane + off) = lo;
 }
 
+#ifdef FLCT_TC_PROFILE
+// Per-stage clock sums of thread 0 of every CTA (profiling builds only).
+static __device__ unsigned long long g_tc_stage_clk[12];
+#define FLCT_TC_STAMP(k)                                                     \
+    do {                                                                     \
+        if (t == 0) {                                                        \
+            const long long c_ = clock64();                                  \
+            atomicAdd(&g_tc_stage_clk[k], (unsigned long long)(c_ - clk0_)); \
+            clk0_ = c_;                                                      \
+        }                                                                    \
+    } while (0)
+#else
+#define FLCT_TC_STAMP(k) \
+    do {                 \
+    } while (0)
+#endif
+
 template <int N, typename T>
 __global__ void __launch_bounds__(256, TcCfg<N>::MINB) k_window_tc(TcArgs a) {
     using C = TcCfg<N>;
-    constexpr int H = C::H, N8 = C::N8, K1 = C::K1, K2 = C::K2, WIT = C::WIT, R2 = C::R2;
+    constexpr int H = C::H, N8 = C::N8, K1 = C::K1, K2 = C::K2, WIT = C::WIT;
     constexpr uint64_t kLimit = 2000000000ull;  // 2 s per wait
     extern __shared__ unsigned char sm_raw[];
     unsigned char* sm = reinterpret_cast<unsigned char*>(
@@ -268,8 +293,18 @@ __global__ void __launch_bounds__(256, TcCfg<N>::MINB) k_window_tc(TcArgs a) {
     constexpr uint32_t id3 = tc::idesc(Split16<T>::fmt, 128, K2, false, true);
     constexpr uint32_t id4 = tc::idesc(Split16<T>::fmt, 128, K1, true, true);
     const uint32_t ahi = tc::smem_u32(Ahi);
-    const uint32_t b1hi = tc::smem_u32(B1hi), b1lo = tc::smem_u32(B1lo);
-    const uint32_t b2hi = tc::smem_u32(B2hi), b2lo = tc::smem_u32(B2lo);
+    const uint32_t b1hi = tc::smem_u32(B1hi);
+    const uint32_t b2hi = tc::smem_u32(B2hi);
+    // base descriptors of every operand layout; a tile or K step adds its
+    // byte offset / 16 to the start-address field (all offsets stay inside
+    // the 256 KB shared window, so the field never carries)
+    const uint64_t dA_mn = tc::desc(ahi, 2048, 128);     // A1, A2, A4 (MN-major, 128 rows)
+    const uint64_t dA3 = tc::desc(ahi, 128, K2 * 16);    // A3 (K-major)
+    const uint64_t dB1k = tc::desc(b1hi, 128, K1 * 16);  // B1 K-major (S1)
+    const uint64_t dB1m = tc::desc(b1hi, K1 * 16, 128);  // B1 MN-major (S4)
+    const uint64_t dB2k = tc::desc(b2hi, 128, K2 * 16);  // B2 K-major (S2)
+    const uint64_t dB2m = tc::desc(b2hi, K2 * 16, 128);  // B2 MN-major (S3)
+    constexpr uint64_t oB1lo = (uint64_t)(C::B1B >> 4), oB2lo = (uint64_t)(C::B2B >> 4);
 
     grid_dep_wait();  // work list, means and counters come from earlier kernels
     const int nwork = *a.nwork;
@@ -281,12 +316,16 @@ __global__ void __launch_bounds__(256, TcCfg<N>::MINB) k_window_tc(TcArgs a) {
         tc::mma(d, ah, bl, id, 1u);
         tc::mma(d, al, bh, id, 1u);
     };
+    // one thread polls the MMA barrier, the others wait at the CTA barrier
+    // (a barrier wait takes no issue slots from the other CTA on the SM)
     auto wait_stage = [&]() -> bool {
-        const bool done =
-            a.stall_ns ? tc::mbar_wait(s_never, 0u, a.stall_ns) : tc::mbar_wait(s_mbar, phase, kLimit);
+        bool done = true;
+        if (t == 0)
+            done = a.stall_ns ? tc::mbar_wait(s_never, 0u, a.stall_ns) : tc::mbar_wait(s_mbar, phase, kLimit);
         phase ^= 1u;
+        const bool all = __syncthreads_and(done ? 1 : 0) != 0;
         tc::fence_after();
-        return __syncthreads_and(done ? 1 : 0) != 0;
+        return all;
     };
     auto to_mma = [&]() {
         tc::fence_async_smem();
@@ -295,101 +334,145 @@ __global__ void __launch_bounds__(256, TcCfg<N>::MINB) k_window_tc(TcArgs a) {
         tc::fence_after();
     };
 
+    // The work items of an iteration, fetched one iteration ahead by the
+    // threads t < WIT (their global-load latency then overlaps the previous
+    // iteration's tensor-core stages).
+    struct Fetch {
+        const float2* f1;
+        const float2* f2;
+        float4 mean;
+        int gi, pix, nx, ny, valid;
+    };
+    auto fetch = [&](int b) {
+        Fetch f;
+        f.valid = b + t < nwork;
+        int w = f.valid ? b + t : nwork - 1;
+        f.f1 = a.s1;
+        f.f2 = a.s2;
+        f.nx = a.nx;
+        f.ny = a.ny;
+        if (a.nseg > 0) {
+            const int k = seg_find(a.seg_start, a.nseg, w);
+            const WinSeg sg = a.segs[k];
+            f.f1 = sg.s1;
+            f.f2 = sg.s2;
+            f.nx = sg.nx;
+            f.ny = sg.ny;
+            w = sg.base + (w - __ldg(a.seg_start + k));
+        }
+        f.gi = w;
+        f.pix = a.work[w];
+        f.mean = a.means ? a.means[w] : make_float4(0.f, 0.f, 0.f, 0.f);
+        return f;
+    };
+    Fetch nxt{};
+    if (t < WIT && blockIdx.x * WIT < nwork) nxt = fetch(blockIdx.x * WIT);
+#ifdef FLCT_TC_PROFILE
+    long long clk0_ = clock64();
+#endif
     for (int base = blockIdx.x * WIT; base < nwork && ok; base += gridDim.x * WIT) {
-        // ---- window table --------------------------------------------------
+        // ---- window table (from the prefetched items) ------------------------
         if (t < WIT) {
-            const bool valid = base + t < nwork;
-            int w = valid ? base + t : nwork - 1;
-            const float2* f1s = a.s1;
-            const float2* f2s = a.s2;
-            int nx = a.nx, ny = a.ny;
-            if (a.nseg > 0) {
-                const int k = seg_find(a.seg_start, a.nseg, w);
-                const WinSeg sg = a.segs[k];
-                f1s = sg.s1;
-                f2s = sg.s2;
-                nx = sg.nx;
-                ny = sg.ny;
-                w = sg.base + (w - __ldg(a.seg_start + k));
-            }
-            const int pix = a.work[w];
             int ic, jc, imin, jmin;
             if (a.direct) {
-                imin = pix / ny;
+                imin = nxt.pix / nxt.ny;
                 jmin = 0;
                 ic = imin;
                 jc = 0;
             } else {
-                ic = pix / ny;
-                jc = pix - ic * ny;
-                imin = box_start(ic, nx, a.nsize);
-                jmin = box_start(jc, ny, a.nsize);
+                ic = nxt.pix / nxt.ny;
+                jc = nxt.pix - ic * nxt.ny;
+                imin = box_start(ic, nxt.nx, a.nsize);
+                jmin = box_start(jc, nxt.ny, a.nsize);
             }
-            s_gi[t] = w;
-            s_valid[t] = valid ? 1 : 0;
+            s_gi[t] = nxt.gi;
+            s_valid[t] = nxt.valid;
             s_geo[t] = make_int4(imin, jmin, imin - ic + N, jmin - jc + N);
-            s_src[2 * t] = f1s + (size_t)imin * ny + jmin;
-            s_src[2 * t + 1] = f2s + (size_t)imin * ny + jmin;
-            s_ny[t] = ny;
-            s_mean[t] = a.means ? a.means[w] : make_float4(0.f, 0.f, 0.f, 0.f);
+            s_src[2 * t] = nxt.f1 + (size_t)imin * nxt.ny + jmin;
+            s_src[2 * t + 1] = nxt.f2 + (size_t)imin * nxt.ny + jmin;
+            s_ny[t] = nxt.ny;
+            s_mean[t] = nxt.mean;
             s_wmax[t] = 0u;
             s_widx[t] = 0x7fffffff;
             s_wnan[t] = 0;
         }
         __syncthreads();
+        FLCT_TC_STAMP(0);
 
         // ---- stage 0: boxes -> A1 (MN-major; lane = box column) ------------
         {
             unsigned char* A1lo = Ahi + C::A1B;
+            // a warp's passes over sub-images, PJ of them at once when their
+            // values fit in registers (more loads in flight per lane)
+            constexpr int NPASS = (C::SUBS + 8 * C::SPW - 1) / (8 * C::SPW);
+            constexpr int PJ = (C::CB * N8 <= 32 && NPASS >= 2) ? 2 : 1;
 #pragma unroll 1
-            for (int sp = wp * C::SPW; sp < C::SUBS; sp += 8 * C::SPW) {
-                const int s = sp + lane / C::LW;
+            for (int p0 = 0; p0 < NPASS; p0 += PJ) {
+                float x[PJ][C::CB][N8];
+                float gcol[PJ][C::CB];
+                float mx[PJ];
+                int sub[PJ];
                 const int jl = lane % C::LW;
-                const bool sval = s < C::SUBS;
-                const int w = sval ? (s >> 1) : 0, img = s & 1;
-                const int4 geo = s_geo[w];
-                const int ny = s_ny[w];
-                const float4 mm = s_mean[w];
-                const float mh = img ? mm.z : mm.x, ml = img ? mm.w : mm.y;
-                const float2* src = s_src[2 * w + img];
-                const float* gr = s_g + geo.z;
-                float x[C::CB][N8];
-                float mx = 0.f;
 #pragma unroll
-                for (int cb = 0; cb < C::CB; ++cb) {
-                    const int j = cb * 32 + jl;
-                    const bool jv = sval && j < N;
-                    const float gc = jv ? s_g[geo.w + j] : 0.f;
-                    if (jv) {
-#pragma unroll
-                        for (int i = 0; i < N8; ++i) {
-                            if (i < N) {
-                                const float2 u = __ldg(src + (size_t)i * ny + j);
-                                x[cb][i] = ((u.x - mh) + (u.y - ml)) * (gr[i] * gc);
-                                mx = fmaxf(mx, fabsf(x[cb][i]));
-                            } else {
-                                x[cb][i] = 0.f;
-                            }
-                        }
-                    } else {
-#pragma unroll
-                        for (int i = 0; i < N8; ++i) x[cb][i] = 0.f;
-                    }
-                }
-#pragma unroll
-                for (int o = C::LW / 2; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-                const float sc = pow2_scale(__float_as_uint(mx));
-                if (sval) {
+                for (int pj = 0; pj < PJ; ++pj) {
+                    const int s = (p0 + pj) * 8 * C::SPW + wp * C::SPW + lane / C::LW;
+                    const bool sval = p0 + pj < NPASS && s < C::SUBS;
+                    sub[pj] = sval ? s : -1;
+                    const int w = sval ? (s >> 1) : 0, img = s & 1;
+                    const int4 geo = s_geo[w];
+                    const int ny = s_ny[w];
+                    const float4 mm = s_mean[w];
+                    // x = (f - mean) g_r(i): the column weight g_c(j) >= 0 is
+                    // folded into the lane's final scale
+                    const float2 mhl = img ? make_float2(mm.z, mm.w) : make_float2(mm.x, mm.y);
+                    const float2* src = s_src[2 * w + img];
+                    const float* gr = s_g + geo.z;
+                    mx[pj] = 0.f;
 #pragma unroll
                     for (int cb = 0; cb < C::CB; ++cb) {
                         const int j = cb * 32 + jl;
-                        if (j < K1) {
+                        const bool jv = sval && j < N;
+                        gcol[pj][cb] = jv ? s_g[geo.w + j] : 0.f;
+                        float mc = 0.f;
+                        if (jv) {
+                            const float2* col = src + j;
 #pragma unroll
-                            for (int g = 0; g < N8 / 8; ++g) {
-                                const int row = s * N8 + 8 * g;
-                                const int off = (row >> 7) * (128 * K1 * 2) + ((row & 127) >> 3) * 128 + (j & 7) * 16 +
-                                                (j >> 3) * 2048;
-                                tc_put8<T>(Ahi, A1lo, off, &x[cb][8 * g], sc);
+                            for (int i = 0; i < N8; ++i) {
+                                if (i < N) {
+                                    const float2 d = csub(__ldg(col + (size_t)i * ny), mhl);
+                                    x[pj][cb][i] = (d.x + d.y) * gr[i];
+                                    mc = fmaxf(mc, fabsf(x[pj][cb][i]));
+                                } else {
+                                    x[pj][cb][i] = 0.f;
+                                }
+                            }
+                        } else {
+#pragma unroll
+                            for (int i = 0; i < N8; ++i) x[pj][cb][i] = 0.f;
+                        }
+                        mx[pj] = fmaxf(mx[pj], mc * gcol[pj][cb]);
+                    }
+                }
+#pragma unroll
+                for (int pj = 0; pj < PJ; ++pj) {
+#pragma unroll
+                    for (int o = C::LW / 2; o > 0; o >>= 1)
+                        mx[pj] = fmaxf(mx[pj], __shfl_xor_sync(0xffffffffu, mx[pj], o));
+                    const float sc = pow2_scale(__float_as_uint(mx[pj]));
+                    const int s = sub[pj];
+                    if (s >= 0) {
+#pragma unroll
+                        for (int cb = 0; cb < C::CB; ++cb) {
+                            const int j = cb * 32 + jl;
+                            if (j < K1) {
+                                const float sj = sc * gcol[pj][cb];
+#pragma unroll
+                                for (int g = 0; g < N8 / 8; ++g) {
+                                    const int row = s * N8 + 8 * g;
+                                    const int off = (row >> 7) * (128 * K1 * 2) + ((row & 127) >> 3) * 128 +
+                                                    (j & 7) * 16 + (j >> 3) * 2048;
+                                    tc_put8<T>(Ahi, A1lo, off, &x[pj][cb][8 * g], sj);
+                                }
                             }
                         }
                     }
@@ -397,20 +480,25 @@ __global__ void __launch_bounds__(256, TcCfg<N>::MINB) k_window_tc(TcArgs a) {
             }
         }
         to_mma();
+        FLCT_TC_STAMP(1);
         if (t == 0) {
             // consecutive MMAs go to different accumulators (tiles) so that
             // the tensor pipe can overlap them
+#pragma unroll
             for (int s = 0; s < K1 / 16; ++s)
+#pragma unroll
                 for (int tl = 0; tl < C::T1; ++tl)
-                    mma3(tmem + tl * K1, tc::desc(ahi + tl * (128 * K1 * 2) + s * 4096, 2048, 128),
-                         tc::desc(ahi + C::A1B + tl * (128 * K1 * 2) + s * 4096, 2048, 128),
-                         tc::desc(b1hi + s * 256, 128, K1 * 16), tc::desc(b1lo + s * 256, 128, K1 * 16), id1, s > 0);
+                    mma3(tmem + tl * K1, dA_mn + ((tl * (128 * K1 * 2) + s * 4096) >> 4),
+                         dA_mn + ((C::A1B + tl * (128 * K1 * 2) + s * 4096) >> 4), dB1k + (s * 256 >> 4),
+                         dB1k + oB1lo + (s * 256 >> 4), id1, s > 0);
             tc::commit(s_mbar);
         }
+        if (t < WIT && base + (int)gridDim.x * WIT < nwork) nxt = fetch(base + gridDim.x * WIT);
         if (!wait_stage()) {
             ok = false;
             break;
         }
+        FLCT_TC_STAMP(2);
 
         // ---- stage 1: T rows -> A2 (MN-major rows (ky group, window, ky lo)) --
         {
@@ -450,24 +538,28 @@ __global__ void __launch_bounds__(256, TcCfg<N>::MINB) k_window_tc(TcArgs a) {
         }
         tc::fence_before();
         to_mma();
+        FLCT_TC_STAMP(3);
         if (t == 0) {
+#pragma unroll
             for (int s = 0; s < K2 / 16; ++s)
+#pragma unroll
                 for (int img = 0; img < 2; ++img)
-                    mma3(tmem + img * K2, tc::desc(ahi + img * C::A2B + s * 4096, 2048, 128),
-                         tc::desc(ahi + 2 * C::A2B + img * C::A2B + s * 4096, 2048, 128),
-                         tc::desc(b2hi + s * 256, 128, K2 * 16), tc::desc(b2lo + s * 256, 128, K2 * 16), id2, s > 0);
+                    mma3(tmem + img * K2, dA_mn + ((img * C::A2B + s * 4096) >> 4),
+                         dA_mn + ((2 * C::A2B + img * C::A2B + s * 4096) >> 4), dB2k + (s * 256 >> 4),
+                         dB2k + oB2lo + (s * 256 >> 4), id2, s > 0);
             tc::commit(s_mbar);
         }
         if (!wait_stage()) {
             ok = false;
             break;
         }
+        FLCT_TC_STAMP(4);
 
         // ---- stage 2: spectra -> conj(A) B filt^2 -> A3 (K-major) ----------
         {
             unsigned char* A3lo = Ahi + C::A3B;
             const int mn = qd * 32 + lane;  // S2 row
-            const int grp = mn >> 3, g2 = grp / WIT, w = grp - g2 * WIT;
+            const int g2 = (mn >> 3) / WIT;
             const int ky = g2 * 8 + (mn & 7);
             const bool valid = g2 < C::G2 && ky < C::KYN;
             const bool special = C::PACK && ky == 0;  // packed ky = 0 / H row
@@ -551,17 +643,19 @@ __global__ void __launch_bounds__(256, TcCfg<N>::MINB) k_window_tc(TcArgs a) {
         }
         tc::fence_before();
         to_mma();
+        FLCT_TC_STAMP(5);
         if (t == 0) {
+#pragma unroll
             for (int s = 0; s < K2 / 16; ++s)
-                mma3(tmem, tc::desc(ahi + s * 256, 128, K2 * 16), tc::desc(ahi + C::A3B + s * 256, 128, K2 * 16),
-                     tc::desc(b2hi + s * 2 * (K2 * 16), K2 * 16, 128), tc::desc(b2lo + s * 2 * (K2 * 16), K2 * 16, 128),
-                     id3, s > 0);
+                mma3(tmem, dA3 + (s * 256 >> 4), dA3 + ((C::A3B + s * 256) >> 4),
+                     dB2m + (s * 2 * (K2 * 16) >> 4), dB2m + oB2lo + (s * 2 * (K2 * 16) >> 4), id3, s > 0);
             tc::commit(s_mbar);
         }
         if (!wait_stage()) {
             ok = false;
             break;
         }
+        FLCT_TC_STAMP(6);
 
         // ---- stage 3: U rows -> A4 (MN-major rows (window, i)) -------------
         {
@@ -612,22 +706,126 @@ __global__ void __launch_bounds__(256, TcCfg<N>::MINB) k_window_tc(TcArgs a) {
         }
         tc::fence_before();
         to_mma();
+        FLCT_TC_STAMP(7);
         if (t == 0) {
+#pragma unroll
             for (int s = 0; s < K1 / 16; ++s)
+#pragma unroll
                 for (int tl = 0; tl < C::T4; ++tl)
-                    mma3(tmem + tl * K1, tc::desc(ahi + tl * (128 * K1 * 2) + s * 4096, 2048, 128),
-                         tc::desc(ahi + C::A4B + tl * (128 * K1 * 2) + s * 4096, 2048, 128),
-                         tc::desc(b1hi + s * 2 * (K1 * 16), K1 * 16, 128),
-                         tc::desc(b1lo + s * 2 * (K1 * 16), K1 * 16, 128), id4, s > 0);
+                    mma3(tmem + tl * K1, dA_mn + ((tl * (128 * K1 * 2) + s * 4096) >> 4),
+                         dA_mn + ((C::A4B + tl * (128 * K1 * 2) + s * 4096) >> 4),
+                         dB1m + (s * 2 * (K1 * 16) >> 4), dB1m + oB1lo + (s * 2 * (K1 * 16) >> 4), id4, s > 0);
             tc::commit(s_mbar);
         }
         if (!wait_stage()) {
             ok = false;
             break;
         }
+        FLCT_TC_STAMP(8);
 
         // ---- stage 4: |c|, first strict maximum, peak record ---------------
-        {
+        if constexpr (32 % N8 == 0) {
+            // every window's rows lie in one warp: maximum, first maximum and
+            // record without CTA barriers (warp h of a quadrant takes tile h)
+            float* stg = reinterpret_cast<float*>(Ahi);
+            constexpr int G = N8;  // lanes per window
+            const int gbase = lane & ~(G - 1);
+            const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << gbase);
+#pragma unroll 1
+            for (int tl = hf; tl < C::T4; tl += 2) {
+                const int r4 = tl * 128 + qd * 32 + lane;
+                const int w = r4 / N8, i = r4 - w * N8;
+                float c[K1];
+                tc::tmem_ld<K1>(tmem + lane_base + tl * K1, c);
+                const bool rv = w < WIT && i < N;
+                const int I = (i + H) % N;
+                float m = 0.f;
+                if (rv) {
+                    float* dst = stg + (w * N + I) * C::SROW;
+#pragma unroll
+                    for (int j = 0; j < N; ++j) m = fmaxf(m, fabsf(c[j]));
+                    // J = j - H (mod N): the row's two halves, swapped
+                    if constexpr (C::SV == 4) {
+#pragma unroll
+                        for (int jj = 0; jj < H; jj += 4) {
+                            *reinterpret_cast<float4*>(dst + jj) =
+                                make_float4(c[H + jj], c[H + jj + 1], c[H + jj + 2], c[H + jj + 3]);
+                            *reinterpret_cast<float4*>(dst + H + jj) =
+                                make_float4(c[jj], c[jj + 1], c[jj + 2], c[jj + 3]);
+                        }
+                    } else {
+#pragma unroll
+                        for (int jj = 0; jj < H; jj += 2) {
+                            *reinterpret_cast<float2*>(dst + jj) = make_float2(c[H + jj], c[H + jj + 1]);
+                            *reinterpret_cast<float2*>(dst + H + jj) = make_float2(c[jj], c[jj + 1]);
+                        }
+                    }
+                }
+                // window maximum over its lanes (pad rows and absent
+                // windows add 0)
+                float wm = m;
+#pragma unroll
+                for (int o = G / 2; o > 0; o >>= 1) wm = fmaxf(wm, __shfl_xor_sync(0xffffffffu, wm, o));
+                const bool nan0 = rv && I == 0 && c[H] != c[H];
+                const bool wnan = (__ballot_sync(0xffffffffu, nan0) & gmask) != 0u;
+                // the first row (in I order) holding the maximum, then its
+                // first column (in J order)
+                int key = (rv && wm != 0.f && m == wm) ? I : 0x7fffffff;
+#pragma unroll
+                for (int o = G / 2; o > 0; o >>= 1) key = min(key, __shfl_xor_sync(0xffffffffu, key, o));
+                int Jl = 0;
+                if (rv && key == I) {
+                    bool found = false;
+#pragma unroll
+                    for (int J = 0; J < N; ++J) {
+                        const int j = (J + H) % N;
+                        if (!found && fabsf(c[j]) == wm) {
+                            Jl = J;
+                            found = true;
+                        }
+                    }
+                }
+                const int win_lane = gbase + ((key == 0x7fffffff ? 0 : key) + H) % N;
+                const int Jw = __shfl_sync(0xffffffffu, Jl, win_lane);
+                __syncwarp();
+                if (w < WIT && s_valid[w]) {
+                    int Ip, Jp;
+                    bool have;
+                    if (wnan) {
+                        Ip = 0;
+                        Jp = 0;
+                        have = true;
+                    } else {
+                        have = wm != 0.f;
+                        Ip = have ? key : H;
+                        Jp = have ? Jw : H;
+                    }
+                    const float* sw = stg + w * N * C::SROW;
+                    const int kl = lane - gbase;
+                    if (a.peaks_h) {
+                        float* rec = reinterpret_cast<float*>(a.peaks_h + s_gi[w]);
+                        for (int k = kl; k < kHiresPatch * kHiresPatch + 1; k += G) {
+                            if (k < kHiresPatch * kHiresPatch) {
+                                const int r = Ip - 2 + k / kHiresPatch, cc = Jp - 2 + k % kHiresPatch;
+                                rec[k] = (r >= 0 && r < N && cc >= 0 && cc < N) ? fabsf(sw[r * C::SROW + cc]) : 0.f;
+                            } else {
+                                rec[k] = __uint_as_float(peak_meta(Ip, Jp, have));
+                            }
+                        }
+                    } else {
+                        const bool dofit = have && Ip > 0 && Ip < N - 1 && Jp > 0 && Jp < N - 1;
+                        float* rec = reinterpret_cast<float*>(a.peaks + s_gi[w]);
+                        for (int k = kl; k < 10; k += G) {
+                            if (k < 9)
+                                rec[k] = dofit ? fabsf(sw[(Ip - 1 + k / 3) * C::SROW + (Jp - 1 + k % 3)]) : 0.f;
+                            else
+                                rec[9] = __uint_as_float(peak_meta(Ip, Jp, dofit));
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+        } else {
             float* stg = reinterpret_cast<float*>(Ahi);
             // rows of both halves: J in [0, H) <- j in [H, N); J in [H, N) <- j in [0, H)
             auto row_pass = [&](auto jbc) {
@@ -639,17 +837,31 @@ __global__ void __launch_bounds__(256, TcCfg<N>::MINB) k_window_tc(TcArgs a) {
                     const int w = r4 / N8, i = r4 - w * N8;
                     float c[K1];
                     tc::tmem_ld<K1>(tmem + lane_base + tl * K1, c);
+                    float m_row = 0.f;
                     if (w < WIT && i < N) {
                         const int I = (i + H) % N;
-                        float m = 0.f;
                         float* dst = stg + (w * N + I) * C::SROW + Jb;
 #pragma unroll
-                        for (int jj = 0; jj < H; ++jj) {
-                            m = fmaxf(m, fabsf(c[jb + jj]));
-                            dst[jj] = c[jb + jj];
+                        for (int jj = 0; jj < H; ++jj) m_row = fmaxf(m_row, fabsf(c[jb + jj]));
+                        if constexpr (C::SV == 4) {
+#pragma unroll
+                            for (int jj = 0; jj < H; jj += 4)
+                                *reinterpret_cast<float4*>(dst + jj) =
+                                    make_float4(c[jb + jj], c[jb + jj + 1], c[jb + jj + 2], c[jb + jj + 3]);
+                        } else {
+#pragma unroll
+                            for (int jj = 0; jj < H; jj += 2)
+                                *reinterpret_cast<float2*>(dst + jj) = make_float2(c[jb + jj], c[jb + jj + 1]);
                         }
                         if (jb == H && I == 0 && c[H] != c[H]) s_wnan[w] = 1;
-                        atomicMax(s_wmax + w, __float_as_uint(m));
+                    }
+                    // window maximum: lanes of one window reduce, one of them
+                    // updates the shared slot
+                    const bool rv = w < WIT && i < N;
+                    const unsigned same = __match_any_sync(0xffffffffu, rv ? w : -1);
+                    if (rv) {
+                        const unsigned mb = __reduce_max_sync(same, __float_as_uint(m_row));
+                        if ((int)(__ffs(same) - 1) == lane) atomicMax(s_wmax + w, mb);
                     }
                 }
             };
@@ -714,10 +926,11 @@ __global__ void __launch_bounds__(256, TcCfg<N>::MINB) k_window_tc(TcArgs a) {
                         rec[9] = __uint_as_float(peak_meta(Ip, Jp, dofit));
                 }
             }
-        }
+                }
         tc::fence_before();
         __syncthreads();
         tc::fence_after();
+        FLCT_TC_STAMP(9);
     }
 
     if (!ok) {

@@ -176,7 +176,7 @@ def test_config3_full_size(form):
     from pyflct_gb300 import synth
     rng = np.random.default_rng(20263)
     f1 = synth.kfield((1024, 1024), rng)
-    f2 = synth.spline_warp(f1, *synth.vortex_shift(f1.shape, rng))
+    f2 = synth.spectral_warp(f1, *synth.vortex_shift(f1.shape, rng))
     kw = dict(sigma=8, skip=4, interpolate=True)
     got = run(f1, f2, form, sigma=8.0, skip="4i")
     rep = compare(f1, f2, got, po.velocity(f1, f2, **kw), kw, tol=TOL[form])
@@ -189,7 +189,7 @@ def test_precision_study_config2():
     from pyflct_gb300 import synth
     rng = np.random.default_rng(20262)
     f1 = synth.config2_image1(rng)
-    f2 = synth.spline_warp(f1, *synth.rotation_shift(f1.shape, 0.01))
+    f2 = synth.spectral_warp(f1, *synth.rotation_shift(f1.shape, 0.01))
     kw = dict(sigma=8, thresh=0.1, thresh_abs=True, kr=0.5)
     ref = po.velocity(f1, f2, **kw)
     for form, tol in (("fp32", 1e-3), ("tc_fp16", 1e-3), ("tc_bf16", 1e-2)):
