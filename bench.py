@@ -1,11 +1,13 @@
 #!/usr/bin/env python
-"""FLCT velocity vectors/s on one GB300: the headline workload.
+"""FLCT velocity vectors/s on one GB300: the headline workload and the
+other benchmark configurations.
 
-Workload (one "step" = the whole flct computation on one frame pair):
+Headline (one "step" = the whole flct computation on one frame pair):
 1024 x 1024 float64 k^-2 random field, image2 = image1 advected by five
-Gaussian vortices, sigma = 8 (box 32), -s 4i (every 4th pixel correlated,
-the rest cubic-convolution interpolated), thresh = 0.  That is 65,536
-correlation windows and 1,048,576 output pixels per step.
+Gaussian vortices through the spectral warp (warp_frac2d semantics, run on
+the GPU by this library), sigma = 8 (box 32), -s 4i (every 4th pixel
+correlated, the rest cubic-convolution interpolated), thresh = 0.  That is
+65,536 correlation windows and 1,048,576 output pixels per step.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--form auto|fp32|tc_fp16|tc_bf16]
     python bench.py --impl reference ...   # the CPU implementation arm
@@ -16,9 +18,13 @@ value  = correlation windows per second with inputs resident in HBM
 e2e    = the same metric through flct_gpu_velocity with pinned host
          buffers: both input frames copied in and vx, vy, vm copied out
          every step.
-Beside the headline line's keys: the 64-pair heterogeneous batch
-(batch_64_pairs) and the warp entry points' Mpixel/s at 512^2 (warp_512);
---no-batch skips both.
+Beside the headline line's keys: measured peaks (FP32 pipe, pinned copies),
+`configs` with one record per other benchmark configuration (128^2 blobs,
+the 512^2 precision study, the 64-pair heterogeneous batch, the 4096^2
+sigma-15 stress case with its GPU warp), each with every window form, the
+accuracy against the FP64 oracle and the oracle on one host core, and the
+warp entry points at 512^2.  --no-batch skips the batch, the 4096^2 case
+and the warp timing; --no-cpu skips the oracle runs.
 """
 from __future__ import annotations
 
@@ -37,9 +43,14 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-WORKLOAD = "1024x1024 k^-2 field, 5-vortex warp, sigma=8 (box 32), -s 4i, thresh 0"
+WORKLOAD = "1024x1024 k^-2 field, 5-vortex spectral warp, sigma=8 (box 32), -s 4i, thresh 0"
 METRIC = "FLCT velocity vectors/s (correlation windows/s) at 1024^2 sigma=8"
 NSIDE, SIGMA, SKIP = 1024, 8.0, "4i"
+FORMS = ("fp32", "tc_fp16", "tc_bf16")
+CPU_SAMPLE = ("the oracle (C restatement of flct.c over the project double FFT; FFTW unavailable), "
+              "1 thread")
+
+
 # algorithmic flops of one n x n window: 3 real transforms at 2.5 M log2 M,
 # M = n^2, plus means (2n^2), windowing (4n^2), conj product (4n^2), |c| and
 # argmax (2n^2); 4 n (n/2+1) more with -k.
@@ -49,12 +60,35 @@ def window_flops(n: int, kr: bool = False) -> float:
     return f + (4 * n * (n // 2 + 1) if kr else 0)
 
 
-def workload():
+def tc_flops_per_window(n: int) -> float:
+    """Tensor flops the split tensor-core form executes per n x n window:
+    four M = 128 GEMM stages per CTA iteration (the geometry of TcCfg<n> in
+    window_tc.cuh), each product as hi*hi + hi*lo + lo*hi."""
+    r8 = lambda x: (x + 7) // 8 * 8  # noqa: E731
+    r16 = lambda x: (x + 15) // 16 * 16  # noqa: E731
+    h = n // 2
+    pack = h % 8 == 0
+    r2 = h if pack else r8(h + 1)
+    wit = 128 // r2
+    n8, k1 = r8(n), r16(n)
+    k2 = 2 * n8
+    t1 = (2 * wit * n8 + 127) // 128
+    t4 = (wit * n8 + 127) // 128
+    macs = 3 * (t1 * 128 * k1 * k1 + 2 * 128 * k2 * k2 + 128 * k2 * k2 + t4 * 128 * k1 * k1)
+    return 2.0 * macs / wit
+
+
+def box_of(sigma: float) -> int:
+    """n = 2 nsize, nsize = even part of (int)((int)sigma sqrt(ln 100))."""
+    return 2 * (int(int(sigma) * np.sqrt(np.log(100.0))) // 2 * 2)
+
+
+def workload(device=0):
     from pyflct_gb300 import synth
     rng = np.random.default_rng(20263)
     f1 = synth.kfield((NSIDE, NSIDE), rng)
     dfast, dslow = synth.vortex_shift(f1.shape, rng)
-    f2 = synth.spline_warp(f1, dfast, dslow)
+    f2 = synth.spectral_warp(f1, dfast, dslow, device)
     return np.ascontiguousarray(f1), np.ascontiguousarray(f2)
 
 
@@ -148,7 +182,10 @@ def oracle():
 def run_reference(a):
     """The reference arm: the CPU implementation of the path (the oracle's
     C restatement of flct.c; the reference itself cannot be compiled on the
-    GPU host because its sources do not travel there) on all host threads."""
+    GPU host because its sources do not travel there) on all host threads,
+    with the same run on one thread reported beside it.  image2 is made by
+    the same GPU spectral warp as in the GPU arm (input generation, outside
+    the timed region)."""
     ws, rank, _ = dist_init()
     if rank != 0:
         return
@@ -164,6 +201,9 @@ def run_reference(a):
     dt = time.perf_counter() - t0
     windows = 256 * 256
     v = windows * a.steps / dt
+    t1 = time.perf_counter()
+    po.velocity(f1, f2, nthreads=1, **kw)
+    one = windows / (time.perf_counter() - t1)
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "windows/s", "n_gpus": ws,
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * dt / a.steps,
@@ -173,52 +213,305 @@ def run_reference(a):
                          "sample": "full frame per step (65,536 windows + interpolation), "
                                    f"{threads} threads, C restatement of flct.c over the "
                                    "project double FFT (FFTW unavailable)"},
+        "cpu_1core": {"value": one, "unit": "windows/s", "cores": 1, "kind": "port",
+                      "sample": "one full frame, 1 thread (the reference program is single-threaded)"},
         "e2e": {"value": v, "unit": "windows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
-# MMA work the tensor-core form executes per 32x32 window: four M=128 GEMM
-# stages over 8 windows, each product as hi*hi + hi*lo + lo*hi.
-TC_MACS_PER_8 = 3 * (4 * 128 * 32 * 32 + 2 * 128 * 64 * 64 + 128 * 64 * 64 + 2 * 128 * 32 * 32)
-TC_FLOPS_PER_WINDOW = 2 * TC_MACS_PER_8 / 8
+# ------------------------------------------------------------------ GPU side
 
 
-def run_batch(a, dev, flush):
+def measured_fp32_peak():
+    """FP32-pipe throughput measured here (libflctprobe.so: independent FMA
+    chains, scalar and packed, CUDA events); TFLOP/s, or None."""
+    from pyflct_gb300 import build
+    try:
+        lib = C.CDLL(build.build_probe())
+        s, p = C.c_double(), C.c_double()
+        if lib.flct_probe_fp32_peak(5, C.byref(s), C.byref(p)) != 0:
+            return None
+        return {"scalar_tflops": s.value, "packed_tflops": p.value, "tflops": max(s.value, p.value)}
+    except Exception:
+        return None
+
+
+def measured_copy_peaks(dev):
+    """Pinned host <-> device copy bandwidth: one 256 MiB cudaMemcpyAsync
+    each way (torch copy_), best of 5, CUDA events."""
+    import torch
+    nbytes = 256 << 20
+    h = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    d = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    out = {}
+    for name, fn in (("h2d_gbs", lambda: d.copy_(h, non_blocking=True)),
+                     ("d2h_gbs", lambda: h.copy_(d, non_blocking=True))):
+        best = 0.0
+        for _ in range(6):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            best = max(best, nbytes / (e0.elapsed_time(e1) / 1e3) / 1e9)
+        out[name] = best
+    return out
+
+
+class DeviceRunner:
+    """Timed device-buffer calls (flct_gpu_velocity_device) of one frame
+    pair with one parameter set, L2 flushed between steps."""
+
+    def __init__(self, ctx, dev, flush, f1, f2):
+        import torch
+        self.ctx, self.dev, self.flush = ctx, dev, flush
+        self.nx, self.ny = f1.shape
+        self.d1 = torch.from_numpy(np.ascontiguousarray(f1)).to(dev)
+        self.d2 = torch.from_numpy(np.ascontiguousarray(f2)).to(dev)
+        self.stream = torch.cuda.current_stream(dev)
+
+    def run(self, p, steps, warmup, clocks=None):
+        import torch
+        from pyflct_gb300 import _lib
+        lib, ctx = self.ctx.lib, self.ctx
+        out = [torch.empty(self.nx, self.ny, dtype=torch.float64, device=self.dev) for _ in range(3)]
+        sh = C.c_void_p(self.stream.cuda_stream)
+
+        def step():
+            ctx.check(lib.flct_gpu_velocity_device(
+                ctx.h, C.byref(p), C.c_void_p(self.d1.data_ptr()), C.c_void_p(self.d2.data_ptr()),
+                self.nx, self.ny, *[C.c_void_p(o.data_ptr()) for o in out], sh))
+
+        for _ in range(max(3, warmup)):
+            step()
+        torch.cuda.synchronize()
+        t = ctx.timing()
+        names = {v: k for k, v in _lib.FORMS.items()}
+        res = dict(windows=int(t.windows), launches=int(t.launches), box=int(t.box), used=names[int(t.form)])
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        win_ms = []
+        torch.cuda.synchronize()
+        wall0 = time.perf_counter()
+        if clocks:
+            clocks.__enter__()
+        for k in range(steps):
+            self.flush.zero_()
+            evs[k][0].record(self.stream)
+            step()
+            evs[k][1].record(self.stream)
+            win_ms.append(ctx.timing().ms_window)
+        torch.cuda.synchronize()
+        if clocks:
+            clocks.__exit__()
+        res["wall_s"] = time.perf_counter() - wall0
+        res["total_ms"] = sum(e0.elapsed_time(e1) for e0, e1 in evs)
+        res["ms_per_step"] = res["total_ms"] / steps
+        res["window_ms"] = statistics.mean(win_ms)
+        res["value"] = res["windows"] * steps / (res["total_ms"] / 1e3)
+        res["out"] = out
+        return res
+
+
+def accuracy(got, ref, tol=1e-3):
+    """max / rms |dv| on computed (vm = 1) and interpolated (vm = 0.5)
+    pixels against the oracle, and mask equality."""
+    vx, vy, vm = got
+    ox, oy, om = ref
+    comp = om == 1.0
+    finite = np.isfinite(ox) & np.isfinite(oy)
+    dv = np.where(finite, np.maximum(np.abs(vx - ox), np.abs(vy - oy)), 0.0)
+    r = {"mask_equal": bool(np.array_equal(vm, om)),
+         "max_dv_computed": float(dv[comp].max(initial=0.0)),
+         "rms_dv_computed": float(np.sqrt(np.mean(dv[comp] ** 2))) if comp.any() else 0.0,
+         "n_over_tol": int((dv[comp] > tol).sum())}
+    if (om == 0.5).any():
+        r["max_dv_interp"] = float(dv[om == 0.5].max())
+    return r
+
+
+def config_record(name, desc, f1, f2, kw_gpu, kw_oracle, a, runner_args, po):
+    """Every window form on one frame pair: windows/s with inputs resident,
+    accuracy against the FP64 oracle, and the oracle on one core."""
+    from pyflct_gb300.flct import make_params
+    ctx, dev, flush = runner_args
+    r = DeviceRunner(ctx, dev, flush, f1, f2)
+    steps = max(3, min(a.steps, 10))
+    rec = {"workload": desc, "shape": list(f1.shape), "forms": {}}
+    ref = po.velocity(f1, f2, nthreads=os.cpu_count(), **kw_oracle) if po else None
+    for form in FORMS:
+        p = make_params(1.0, 1.0, form=form, **kw_gpu)
+        x = r.run(p, steps, 3)
+        rec["windows_per_step"] = x["windows"]
+        rec["box"] = x["box"]
+        f = {"windows_s": x["value"], "ms_per_step": x["ms_per_step"], "window_ms": x["window_ms"]}
+        if ref is not None:
+            f["accuracy_vs_fp64_oracle"] = accuracy([o.cpu().numpy() for o in x["out"]], ref)
+        rec["forms"][form] = f
+    if po:
+        t0 = time.perf_counter()
+        po.velocity(f1, f2, nthreads=1, **kw_oracle)
+        dt = time.perf_counter() - t0
+        rec["cpu_1core"] = {"windows_s": rec["windows_per_step"] / dt, "cores": 1, "kind": "port",
+                            "sample": "one full frame, " + CPU_SAMPLE}
+    rec["tc_fp16_speedup_over_fp32_form"] = rec["forms"]["tc_fp16"]["windows_s"] / rec["forms"]["fp32"]["windows_s"]
+    return rec
+
+
+def run_config1(a, runner_args, po):
+    from pyflct_gb300 import synth
+    f1, f2, kw = synth.config1()
+    return config_record("config1", "128x128 Gaussian blobs + noise, exact shift (0.3, -0.2), sigma=4 (box 16)",
+                         f1, f2, dict(sigma=4.0), dict(sigma=4.0), a, runner_args, po)
+
+
+def run_config2(a, runner_args, po):
+    from pyflct_gb300 import synth
+    rng = np.random.default_rng(20262)
+    f1 = synth.config2_image1(rng)
+    f2 = synth.spectral_warp(f1, *synth.rotation_shift(f1.shape, 0.01), runner_args[1].index or 0)
+    return config_record("config2", "512x512 k^-2 field with 20% near-zero pixels, 0.01 deg rotation by the "
+                         "spectral warp, sigma=8 (box 32), -t 0.1a -k 0.5", f1, f2,
+                         dict(sigma=8.0, thresh="0.1a", kr=0.5),
+                         dict(sigma=8.0, thresh=0.1, thresh_abs=True, kr=0.5), a, runner_args, po)
+
+
+def run_batch(a, dev, flush, po):
     """The 64-pair heterogeneous workload (sides from {128..768}, sigma from
-    {3, 5, 8, 12}, uniform sub-pixel shifts) as one batched call: windows/s
-    with the inputs resident in HBM, one captured CUDA graph per step."""
+    {3, 5, 8, 12}, uniform sub-pixel shifts) as one batched call per step
+    (a captured CUDA graph): windows/s with the inputs resident in HBM per
+    window form, accuracy of 8 pairs against the oracle, and the oracle on
+    one core and on every host core over a sample of pairs."""
     import torch
     from pyflct_gb300 import synth
     from pyflct_gb300.flct import FlctBatch, make_params
     pairs = synth.config4_pairs()
-    params = [make_params(1.0, 1.0, kw["sigma"], form="auto") for _, _, kw, _ in pairs]
-    b = FlctBatch([f1.shape for f1, _, _, _ in pairs], params, device=dev.index or 0)
-    b.load([(f1, f2) for f1, f2, _, _ in pairs])
     stream = torch.cuda.current_stream(dev)
-    for _ in range(3):
-        b.run(stream)
-    torch.cuda.synchronize()
-    t = b.timing()
-    windows, launches = int(t.windows), int(t.launches)
-    steps = max(3, min(a.steps, 10))
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
-    for k in range(steps):
-        flush.zero_()
-        evs[k][0].record(stream)
-        b.run(stream)
-        evs[k][1].record(stream)
-    torch.cuda.synchronize()
-    ms = sum(e0.elapsed_time(e1) for e0, e1 in evs) / steps
-    def box(sigma):  # n = 2 nsize, nsize = even part of (int)((int)sigma sqrt(ln 100))
-        return 2 * (int(int(sigma) * np.sqrt(np.log(100.0))) // 2 * 2)
+    boxes = sorted({box_of(kw["sigma"]) for _, _, kw, _ in pairs})
+    flops = sum(window_flops(box_of(kw["sigma"])) * f1.size for f1, _, kw, _ in pairs)
+    res = {"pairs": len(pairs), "boxes": boxes, "forms": {},
+           "note": "inputs resident in HBM (179 MB > L2), L2 flushed between steps"}
+    check = list(range(0, len(pairs), 8))
+    refs = {k: po.velocity(pairs[k][0], pairs[k][1], nthreads=os.cpu_count(), sigma=pairs[k][2]["sigma"])
+            for k in check} if po else {}
+    for form in ("auto",) + FORMS:
+        params = [make_params(1.0, 1.0, kw["sigma"], form=form) for _, _, kw, _ in pairs]
+        b = FlctBatch([f1.shape for f1, _, _, _ in pairs], params, device=dev.index or 0)
+        b.load([(f1, f2) for f1, f2, _, _ in pairs])
+        for _ in range(3):
+            b.run(stream)
+        torch.cuda.synchronize()
+        t = b.timing()
+        windows, launches = int(t.windows), int(t.launches)
+        steps = max(3, min(a.steps, 10))
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for k in range(steps):
+            flush.zero_()
+            evs[k][0].record(stream)
+            b.run(stream)
+            evs[k][1].record(stream)
+        torch.cuda.synchronize()
+        ms = sum(e0.elapsed_time(e1) for e0, e1 in evs) / steps
+        f = {"windows_s": windows / (ms / 1e3), "ms_per_step": ms, "kernels_per_graph": launches,
+             "algorithmic_tflops": flops / (ms / 1e3) / 1e12}
+        if refs:
+            worst = {"max_dv_computed": 0.0, "mask_equal": True}
+            for k in check:
+                got = (b.vx[k].cpu().numpy(), b.vy[k].cpu().numpy(), b.vm[k].cpu().numpy())
+                acc = accuracy(got, refs[k])
+                worst["max_dv_computed"] = max(worst["max_dv_computed"], acc["max_dv_computed"])
+                worst["mask_equal"] &= acc["mask_equal"]
+            worst["pairs_checked"] = len(check)
+            f["accuracy_vs_fp64_oracle"] = worst
+        res["forms"][form] = f
+        res["windows_per_step"] = windows
+        del b
+        torch.cuda.empty_cache()
+    # headline keys of this record: the autotuned form
+    res.update({"value": res["forms"]["auto"]["windows_s"], "unit": "windows/s",
+                "ms_per_step": res["forms"]["auto"]["ms_per_step"],
+                "kernels_per_graph": res["forms"]["auto"]["kernels_per_graph"],
+                "algorithmic_tflops": res["forms"]["auto"]["algorithmic_tflops"]})
+    if po:
+        sample = list(range(0, len(pairs), 4))
+        nwin = 0
+        t0 = time.perf_counter()
+        for k in sample[:4]:
+            o = po.velocity(pairs[k][0], pairs[k][1], nthreads=1, sigma=pairs[k][2]["sigma"])
+            nwin += int((o[2] == 1).sum())
+        one = nwin / (time.perf_counter() - t0)
+        nwin = 0
+        t0 = time.perf_counter()
+        for k in sample:
+            o = po.velocity(pairs[k][0], pairs[k][1], nthreads=os.cpu_count(), sigma=pairs[k][2]["sigma"])
+            nwin += int((o[2] == 1).sum())
+        allc = nwin / (time.perf_counter() - t0)
+        res["cpu_1core"] = {"windows_s": one, "cores": 1, "kind": "port",
+                            "sample": f"pairs {sample[:4]}, " + CPU_SAMPLE}
+        res["cpu_nproc"] = {"windows_s": allc, "cores": os.cpu_count(), "kind": "port",
+                            "sample": f"{len(sample)} of the 64 pairs, the oracle's windows on every host thread"}
+    return res
 
-    boxes = sorted({box(kw["sigma"]) for _, _, kw, _ in pairs})
-    flops = sum(window_flops(box(kw["sigma"])) * f1.size for f1, _, kw, _ in pairs)
-    return {"pairs": len(pairs), "windows_per_step": windows, "value": windows / (ms / 1e3),
-            "unit": "windows/s", "ms_per_step": ms, "steps": steps, "kernels_per_graph": launches,
-            "boxes": boxes, "algorithmic_tflops": flops / (ms / 1e3) / 1e12,
-            "note": "inputs resident in HBM (179 MB > L2), L2 flushed between steps, form auto"}
+
+def run_config5(a, runner_args, po):
+    """4096^2 float32 k^-2 field, image2 by the GPU spectral warp along a
+    k^-3 displacement field of RMS 0.3 px (its time is the warp's Mpixel/s),
+    sigma 15 (box 64), every pixel a window (16.7M): windows/s per form,
+    accuracy against the FP64 oracle's per-window correlation on a random
+    1% of the pixels, the oracle's windows/s on one core over a sample."""
+    import torch
+    from pyflct_gb300 import synth
+    from pyflct_gb300.flct import make_params
+    ctx, dev, flush = runner_args
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    f1, f2, kw, _ = synth.config5(device=dev.index or 0)
+    warp_s = time.perf_counter() - t0  # dominated by warp_frac2d (field synthesis on the host is ~2 s)
+    rec = {"workload": "4096x4096 float32 k^-2 field, k^-3 displacement RMS 0.3 px by the GPU spectral "
+                       "warp, sigma=15 (box 64), every pixel", "shape": list(f1.shape), "forms": {}}
+    rec["warp_4096"] = {"seconds": warp_s, "mpix_s": f1.size / warp_s / 1e6,
+                        "note": "synth.config5 wall time: warp_frac2d through the host-buffer C ABI plus "
+                                "the field synthesis"}
+    r = DeviceRunner(ctx, dev, flush, f1, f2)
+    steps = max(2, min(a.steps, 3))
+    pts = None
+    if po:
+        rng = np.random.default_rng(5)
+        flat = rng.choice(f1.size, size=f1.size // 100, replace=False)
+        pts = np.stack([flat // f1.shape[1], flat % f1.shape[1]], axis=1)
+        sx, sy = np.empty(len(pts)), np.empty(len(pts))
+        for b0 in range(0, len(pts), 4096):
+            part = pts[b0:b0 + 4096]
+            w = [po.extract_window(f1, f2, i, j, sigma=15.0) for i, j in part]
+            sx[b0:b0 + len(part)], sy[b0:b0 + len(part)] = po.cross_cor_batch(
+                np.stack([x for x, _ in w]), np.stack([y for _, y in w]))
+        t0 = time.perf_counter()
+        w = [po.extract_window(f1, f2, i, j, sigma=15.0) for i, j in pts[:400]]
+        po.cross_cor_batch(np.stack([x for x, _ in w]), np.stack([y for _, y in w]), nthreads=1)
+        rec["cpu_1core"] = {"windows_s": 400 / (time.perf_counter() - t0), "cores": 1, "kind": "port",
+                            "sample": "400 of the sampled windows (extraction + cross_cor), " + CPU_SAMPLE}
+    for form in ("fp32", "tc_fp16"):
+        p = make_params(1.0, 1.0, 15.0, form=form)
+        x = r.run(p, steps, 1)
+        rec["windows_per_step"] = x["windows"]
+        f = {"windows_s": x["value"], "ms_per_step": x["ms_per_step"], "window_ms": x["window_ms"]}
+        if form == "tc_fp16":
+            tf = tc_flops_per_window(64) * x["windows"] / (x["window_ms"] / 1e3) / 1e12
+            pk, src = peaks()
+            f["tensor_tflops_executed"] = tf
+            f["tensor_pipe_frac_of_bf16_peak"] = tf / pk["bf16_tflops"]
+        if pts is not None:
+            vx, vy = x["out"][0].cpu().numpy(), x["out"][1].cpu().numpy()
+            dv = np.maximum(np.abs(vx[pts[:, 0], pts[:, 1]] - sy), np.abs(vy[pts[:, 0], pts[:, 1]] - sx))
+            f["accuracy_vs_fp64_oracle_1pct"] = {"pixels": int(len(pts)), "max_dv": float(dv.max()),
+                                                 "rms_dv": float(np.sqrt(np.mean(dv ** 2))),
+                                                 "n_over_1e-3": int((dv > 1e-3).sum())}
+        rec["forms"][form] = f
+        del x
+    rec["tc_fp16_speedup_over_fp32_form"] = rec["forms"]["tc_fp16"]["windows_s"] / rec["forms"]["fp32"]["windows_s"]
+    del r
+    torch.cuda.empty_cache()
+    return rec
 
 
 def run_warp(a, dev):
@@ -259,66 +552,31 @@ def run_ours(a):
         dist.init_process_group("nccl")
     ctx = _lib.context(local)
     lib = ctx.lib
-    f1, f2 = workload()
-    npx = f1.size
     dev = torch.device("cuda", local)
-    d_f1 = torch.from_numpy(f1).to(dev)
-    d_f2 = torch.from_numpy(f2).to(dev)
-    outs = {}
+    f1, f2 = workload(local)
+    npx = f1.size
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
-    stream = torch.cuda.current_stream(dev)
-    sh = C.c_void_p(stream.cuda_stream)
 
     def barrier():
         if ws > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
-    forms = [a.form] + [f for f in ("fp32", "tc_fp16", "tc_bf16") if f != a.form and not a.only]
-    names = {v: k for k, v in _lib.FORMS.items()}
+    runner = DeviceRunner(ctx, dev, flush, f1, f2)
+    forms = [a.form] + [f for f in FORMS if f != a.form and not a.only]
     res = {}
     clk = None
     for form in forms:
         p = make_params(1.0, 1.0, SIGMA, skip=SKIP, form=form)
-        d_out = [torch.empty(NSIDE, NSIDE, dtype=torch.float64, device=dev) for _ in range(3)]
-        outs[form] = d_out
-
-        def step():
-            ctx.check(lib.flct_gpu_velocity_device(
-                ctx.h, C.byref(p), C.c_void_p(d_f1.data_ptr()), C.c_void_p(d_f2.data_ptr()), NSIDE, NSIDE,
-                C.c_void_p(d_out[0].data_ptr()), C.c_void_p(d_out[1].data_ptr()),
-                C.c_void_p(d_out[2].data_ptr()), sh))
-
-        for _ in range(max(3, a.warmup)):
-            step()
-        torch.cuda.synchronize()
-        t = ctx.timing()
-        windows, launches, box = int(t.windows), int(t.launches), int(t.box)
-        used = names[int(t.form)]  # the autotuner's choice for "auto"
-        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-               for _ in range(a.steps)]
-        win_ms = []
         barrier()
-        wall0 = time.perf_counter()
         clocks = Clocks(local) if form == a.form else None
+        r = runner.run(p, a.steps, a.warmup, clocks)
         if clocks:
-            clocks.__enter__()
-        for k in range(a.steps):
-            flush.zero_()  # L2 flush between steps (outside the step's events)
-            evs[k][0].record(stream)
-            step()
-            evs[k][1].record(stream)
-            win_ms.append(ctx.timing().ms_window)
-        barrier()
-        if clocks:
-            clocks.__exit__()
             clk = clocks
-        wall = time.perf_counter() - wall0
-        total_ms = sum(e0.elapsed_time(e1) for e0, e1 in evs)
-        total_ms = reduce_max(total_ms, dev)
-        res[form] = dict(value=windows * a.steps * ws / (total_ms / 1e3), ms_per_step=total_ms / a.steps,
-                         window_ms=statistics.mean(win_ms), windows=windows, launches=launches, box=box,
-                         wall_s=wall, used=used)
+        r["total_ms"] = reduce_max(r["total_ms"], dev)
+        r["value"] = r["windows"] * a.steps * ws / (r["total_ms"] / 1e3)
+        r["ms_per_step"] = r["total_ms"] / a.steps
+        res[form] = r
 
     head = res[a.form]
     windows, launches, box = head["windows"], head["launches"], head["box"]
@@ -351,66 +609,81 @@ def run_ours(a):
     flush_s = time.perf_counter() - t1
     e2e_val = windows * a.steps * ws / max(1e-9, reduce_max(e2e_s - flush_s, dev))
 
-    batch = None if a.no_batch else run_batch(a, dev, flush)
-    warp = None if (a.no_batch or rank != 0) else run_warp(a, dev)
-
     if rank != 0:
         if ws > 1:
             torch.distributed.destroy_process_group()
         return
 
+    po = None if a.no_cpu else oracle()
+    runner_args = (ctx, dev, flush)
+    configs = {}
+    if not a.no_configs:
+        configs["config1"] = run_config1(a, runner_args, po)
+        configs["config2"] = run_config2(a, runner_args, po)
+    batch = None if a.no_batch else run_batch(a, dev, flush, po)
+    if batch is not None:
+        configs["config4"] = batch
+    if not (a.no_batch or a.no_configs):
+        configs["config5"] = run_config5(a, runner_args, po)
+    warp = None if a.no_batch else run_warp(a, dev)
+
     pk, src = peaks()
     fl = window_flops(box)
     nsm = torch.cuda.get_device_properties(dev).multi_processor_count
+    fp32pk = measured_fp32_peak()
+    copies = measured_copy_peaks(dev)
 
     def roofline(form):
         r = res[form]
         form = r["used"]
         achieved = r["windows"] * fl / (r["window_ms"] / 1e3) / 1e12
         if form == "fp32":
-            peak = nsm * 128 * 2 * pk.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
+            if fp32pk:
+                peak = fp32pk["tflops"]
+                psrc = ("measured here: libflctprobe.so FMA chains (best of scalar and packed f32x2), "
+                        "CUDA events")
+            else:
+                peak = nsm * 128 * 2 * pk.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
+                psrc = f"derived: {nsm} SMs x 128 FP32 lanes x 2 x {pk.get('sm_max_mhz')} MHz"
             return {"bound": "fp32", "kernel": f"k_window_fp32<{box}>", "achieved": achieved, "peak": peak,
                     "unit": "TFLOP/s", "frac": achieved / peak, "flops_per_window": fl,
-                    "window_ms": r["window_ms"],
-                    "peak_source": f"derived: {nsm} SMs x 128 FP32 lanes x 2 x {pk.get('sm_max_mhz')} MHz "
-                                   f"({src} max clock); no FP32 figure in MEASURED_PEAKS.json"}
+                    "window_ms": r["window_ms"], "peak_source": psrc}
         peak = pk["bf16_tflops"]
-        tensor = r["windows"] * TC_FLOPS_PER_WINDOW / (r["window_ms"] / 1e3) / 1e12
-        return {"bound": "tensor", "kernel": f"k_window_tc32<{'half' if form == 'tc_fp16' else 'bf16'}>",
+        tfl = tc_flops_per_window(box)
+        tensor = r["windows"] * tfl / (r["window_ms"] / 1e3) / 1e12
+        return {"bound": "tensor", "kernel": f"k_window_tc<{box}, {'half' if form == 'tc_fp16' else 'bf16'}>",
                 "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                 "flops_per_window": fl, "window_ms": r["window_ms"],
-                "tensor_flops_per_window": TC_FLOPS_PER_WINDOW, "tensor_achieved": tensor,
+                "tensor_flops_per_window": tfl, "tensor_achieved": tensor,
                 "tensor_frac": tensor / peak, "peak_source": f"{src} bf16_tflops (dense 16-bit rate)"}
 
     rl = roofline(a.form)
     tp = os.path.join(ROOT, "profiles", "traffic.json")
+    rl["traffic"] = None
     if os.path.exists(tp):
         with open(tp) as fh:
             rl["traffic"] = json.load(fh).get(f"window_{head['used']}_n{box}")
-    else:
-        rl["traffic"] = None
 
     # accuracy against the FP64 oracle on the same frame, and the CPU baseline
     acc, cpu = {}, None
-    if not a.no_cpu:
-        po = oracle()
+    if po:
         kw = dict(sigma=SIGMA, skip=4, interpolate=True)
         ref = po.velocity(f1, f2, nthreads=os.cpu_count(), **kw)
-        comp = ref[2] == 1.0
-        for form, d_out in outs.items():
-            got = [x.cpu().numpy() for x in d_out]
-            dv = np.maximum(np.abs(got[0] - ref[0]), np.abs(got[1] - ref[1]))
-            acc[form] = {"mask_equal": bool(np.array_equal(got[2], ref[2])),
-                         "max_dv_computed": float(dv[comp].max()),
-                         "rms_dv_computed": float(np.sqrt(np.mean(dv[comp] ** 2))),
-                         "n_over_1e-3": int((dv[comp] > 1e-3).sum()),
-                         "max_dv_interp": float(dv[ref[2] == 0.5].max())}
+        for form, r in res.items():
+            acc[form] = accuracy([x.cpu().numpy() for x in r["out"]], ref)
         t0 = time.perf_counter()
         po.velocity(f1, f2, nthreads=1, **kw)
         cdt = time.perf_counter() - t0
         cpu = {"value": windows / cdt, "unit": "windows/s", "cores": 1, "kind": "port",
                "sample": "one full frame (65,536 windows + interpolation), 1 thread, C restatement "
                          "of flct.c over the project double FFT (FFTW unavailable)"}
+
+    # e2e against its bound: the step's copies at the measured pinned rates
+    # (each direction its own engine) or the device step, whichever is longer
+    h2d, d2h = 2 * npx * 8, 3 * npx * 8
+    copy_ms = max(h2d / (copies["h2d_gbs"] * 1e9), d2h / (copies["d2h_gbs"] * 1e9)) * 1e3
+    bound_ms = max(copy_ms, head["ms_per_step"])
+    e2e_ms = windows / e2e_val * 1e3
 
     line = {
         "metric": METRIC, "value": head["value"], "unit": "windows/s", "n_gpus": ws, "steps": a.steps,
@@ -423,11 +696,14 @@ def run_ours(a):
                    "windows_per_step": windows,
                    "output_pixels_per_step": npx, "l2": "flushed (256 MiB write) between steps",
                    "parallelism": f"replicas x{ws}"},
-        "e2e": {"value": e2e_val, "unit": "windows/s", "h2d_bytes_per_step": 2 * npx * 8,
-                "d2h_bytes_per_step": 3 * npx * 8},
+        "e2e": {"value": e2e_val, "unit": "windows/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": e2e_ms, "bound_ms": bound_ms, "copy_bound_ms": copy_ms,
+                "frac_of_bound": bound_ms / e2e_ms},
         "roofline": rl,
+        "measured_peaks": {"fp32": fp32pk, "pinned_copies": copies},
         "forms": {f: {"value": r["value"], "ms_per_step": r["ms_per_step"], "window_ms": r["window_ms"],
                       "used": r["used"]} for f, r in res.items()},
+        "configs": configs,
         "batch_64_pairs": batch,
         "warp_512": warp,
         "cpu_baseline": cpu,
@@ -452,9 +728,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--form", default="auto", choices=["auto", "fp32", "tc_fp16", "tc_bf16"])
-    ap.add_argument("--no-batch", action="store_true", help="skip the 64-pair batched workload and the warp timing")
+    ap.add_argument("--no-batch", action="store_true",
+                    help="skip the 64-pair batch, the 4096^2 configuration and the warp timing")
+    ap.add_argument("--no-configs", action="store_true", help="skip configurations 1, 2 and 5")
     ap.add_argument("--only", action="store_true", help="time only --form (skip the other forms)")
-    ap.add_argument("--no-cpu", action="store_true", help="skip the oracle accuracy and CPU baseline")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the oracle accuracy and CPU baselines")
     a = ap.parse_args()
     if a.impl == "reference":
         run_reference(a)
