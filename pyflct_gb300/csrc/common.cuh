@@ -87,6 +87,40 @@ inline cudaError_t launch_kernel(void (*kern)(KArgs...), dim3 grid, dim3 block, 
     return cudaLaunchKernelEx(&cfg, kern, static_cast<Args&&>(args)...);
 }
 
+// Per-pair launches of one kernel merged into one grid (batched calls):
+// pair p owns blocks [start[p], start[p + 1]) and runs with args[p], its
+// block index and grid size relative to its own blocks.
+template <class A>
+struct MultiArgs {
+    const A* args;
+    const int* start;  // npairs + 1 block prefix sums
+    int npairs;
+};
+
+// The pair that owns this block (pairs without blocks are skipped).
+template <class A>
+__device__ __forceinline__ int multi_owner(const MultiArgs<A>& m) {
+    int lo = 0, hi = m.npairs - 1;
+    const int b = (int)blockIdx.x;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(m.start + mid) <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// The kernel NAME(ARGS a) over one pair, and NAME_multi over many: the body
+// NAME_body(a, vb, vg) sees its block index and grid size as vb and vg.
+#define FLCT_MULTI_KERNEL(BOUNDS, NAME, ARGS)                                                    \
+    __global__ void BOUNDS NAME(ARGS a) { NAME##_body(a, (int)blockIdx.x, (int)gridDim.x); }    \
+    __global__ void BOUNDS NAME##_multi(MultiArgs<ARGS> m) {                                     \
+        const int p_ = multi_owner(m);                                                           \
+        const ARGS a_ = m.args[p_];                                                              \
+        const int s_ = __ldg(m.start + p_);                                                      \
+        NAME##_body(a_, (int)blockIdx.x - s_, __ldg(m.start + p_ + 1) - s_);                     \
+    }
+
 // A kernel launched as a programmatic dependent (its launch overlaps the
 // tail of the kernel before it on the stream) waits here until that kernel
 // has finished and its writes are visible; launched normally, this returns

@@ -18,12 +18,14 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "global.cuh"
 #include "prepass.cuh"
 #include "warp.cuh"
 #include "window_fp32.cuh"
+#include "window_big.cuh"
 #include "window_tc.cuh"
 
 using namespace flct;
@@ -118,10 +120,12 @@ struct flct_ctx {
         return {&b_s1,   &b_s2,   &b_work,   &b_ctr,    &b_r1,     &b_r2,     &b_b1,     &b_b2,
                 &b_gvx,  &b_gvy,  &b_ix,     &b_iy,     &b_f1,     &b_f2,     &b_vx,     &b_vy,
                 &b_vm,   &b_aux1, &b_aux2,   &b_means,  &b_peaks,  &b_grid,   &b_tc,     &bb_arena,
-                &bb_work, &bb_means, &bb_peaks, &bb_ctr, &bb_meta, &b_peaks_h, &bb_peaks_h, &b_re1, &b_re2};
+                &bb_work, &bb_means, &bb_peaks, &bb_ctr, &bb_meta, &b_peaks_h, &bb_peaks_h, &b_re1, &b_re2,
+                &bb_multi};
     }
     int bps[sizeof(kWin) / sizeof(kWin[0])] = {0};
     int bps_tc[kNumTc][2] = {};
+    int bps_big = 0;
     Buf b_tc;              // tensor-core DFT matrices of every box size and split type
     size_t tc_off[kNumTc][2] = {};
     bool tc_ready = false;
@@ -140,7 +144,7 @@ struct flct_ctx {
     // at it), branch streams of the captured graph, the instantiated graph
     // of the last batch and the pairs it was built for
     static constexpr int kBranches = 8;
-    Buf bb_arena, bb_work, bb_means, bb_peaks, bb_peaks_h, bb_ctr, bb_meta;
+    Buf bb_arena, bb_work, bb_means, bb_peaks, bb_peaks_h, bb_ctr, bb_meta, bb_multi;
     cudaStream_t bstream[kBranches] = {};
     cudaEvent_t bev[kBranches + 1] = {};
     cudaEvent_t bdone = nullptr;  // recorded after each batch launch
@@ -261,6 +265,7 @@ flct_status derive(flct_ctx* ctx, const flct_params* p, int nx, int ny, Derived*
 }
 
 void fill_tables(const flct_params* p, int n, float* gauss, float* filt2) {
+    if (n > kMaxBox) return;  // the big-box kernel builds its own (launch_windows)
     // Gaussian weight by offset d in [-n, n] (flct.c:652-665), separable
     const double sigminv = 1. / p->sigma;
     for (int d = -n; d <= n; ++d) {
@@ -351,6 +356,49 @@ flct_status pick_form(flct_ctx* ctx, int requested, int n, int* form) {
 flct_status launch_windows(flct_ctx* ctx, int form, const WinEntry* we, int n, const WinArgs& wa, unsigned* status,
                            cudaStream_t st, int grid_div = 1, long max_items = -1, bool pdl = false) {
     if (grid_div < 1) grid_div = 1;
+    if (n > kMaxBox) {
+        // boxes above 64: the big-box FP32 kernel, one window per CTA
+        if (form != FLCT_FORM_FP32 || n > kMaxBigBox)
+            return fail(ctx, FLCT_ERR_UNSUPPORTED, "box %d has no kernel of this form", n);
+        BigArgs ba{};
+        ba.s1 = wa.s1;
+        ba.s2 = wa.s2;
+        ba.means = wa.means;
+        ba.work = wa.work;
+        ba.nwork = wa.nwork;
+        ba.nx = wa.nx;
+        ba.ny = wa.ny;
+        ba.nsize = wa.nsize;
+        ba.n = n;
+        ba.use_filter = wa.use_filter;
+        ba.direct = wa.direct;
+        ba.peaks = wa.peaks;
+        ba.peaks_h = wa.peaks_h;
+        ba.segs = wa.segs;
+        ba.seg_start = wa.seg_start;
+        ba.nseg = wa.nseg;
+        const double tw = 2.0 * 3.14159265358979323846 / n;
+        for (int m = 0; m < n; ++m) ba.tw[m] = make_float2((float)std::cos(tw * m), (float)-std::sin(tw * m));
+        // the same tables as fill_tables: Gaussian by offset (unit weights
+        // for direct windows) and the squared filter by frequency index
+        for (int d = -n; d <= n; ++d) {
+            const double ax = (double)d / wa.sigma;
+            ba.gauss[d + n] = wa.direct ? 1.0f : (float)std::exp(-ax * ax);
+        }
+        if (wa.use_filter) {
+            const double kroll = wa.kr * (double)(n / 2);
+            for (int k = 0; k < n; ++k) {
+                const int kk = (k <= n / 2) ? k : k - n;
+                const double ax = (double)kk / kroll;
+                ba.filt2[k] = (float)std::exp(-2.0 * ax * ax);
+            }
+        }
+        if (ctx->bps_big == 0) ctx->bps_big = std::max(1, window_big_blocks_per_sm(kMaxBigBox));
+        int grid = std::max(ctx->nsm, ctx->nsm * ctx->bps_big / grid_div);
+        if (max_items >= 0) grid = (int)std::max<long>(1, max_items);
+        CK(launch_window_big(ba, grid, st, pdl));
+        return FLCT_OK;
+    }
     if (form == FLCT_FORM_FP32) {
         int grid = std::max(ctx->nsm, win_grid(ctx, n) / grid_div);
         if (max_items >= 0) grid = (int)std::max<long>(1, (max_items + we->teams - 1) / we->teams);
@@ -524,7 +572,7 @@ flct_status plan_job(flct_ctx* ctx, const flct_params* p, const double* f1, cons
         return fail(ctx, FLCT_ERR_UNSUPPORTED, "-k with kr <= 0 is not available on the GPU path");
     j->n = j->d.n;
     j->we = j->d.global ? nullptr : find_win(j->n);
-    if (!j->d.global && !j->we)
+    if (!j->d.global && !j->we && j->n > kMaxBigBox)
         return fail(ctx, FLCT_ERR_UNSUPPORTED, "box size %d (sigma %g) has no GPU kernel", j->n, p->sigma);
     j->p = p;
     j->f1 = f1;
@@ -592,15 +640,8 @@ JobSizes job_sizes(const Job& j) {
 // Classification of frame rows [r0, r1): threshold test, skip grid, the
 // float split, the work list (b.work / b.ctr: the windows of those rows)
 // and the final values of pixels without a window (flct.c:684-755).
-flct_status enqueue_classify(flct_ctx* ctx, const Job& j, const JobBufs& b, int r0, int r1, const double* d_thr,
-                             cudaStream_t st, int* launches, int blocks_per_sm = 8, const JobBufs* b2 = nullptr,
-                             int rsplit = 0) {
+ClassifyArgs classify_args(const Job& j, const JobBufs& b, int r0, int r1, const double* d_thr) {
     ClassifyArgs ca{};
-    if (b2) {  // windows of rows >= rsplit to b2's list
-        ca.work2 = b2->work;
-        ca.nwork2 = (int*)b2->ctr;
-        ca.rsplit = rsplit;
-    }
     ca.f1 = j.f1;
     ca.f2 = j.f2;
     ca.nx = j.nx;
@@ -623,6 +664,18 @@ flct_status enqueue_classify(flct_ctx* ctx, const Job& j, const JobBufs& b, int 
     ca.status = (unsigned*)(b.ctr + 4);
     ca.r0 = r0;
     ca.r1 = r1;
+    return ca;
+}
+
+flct_status enqueue_classify(flct_ctx* ctx, const Job& j, const JobBufs& b, int r0, int r1, const double* d_thr,
+                             cudaStream_t st, int* launches, int blocks_per_sm = 8, const JobBufs* b2 = nullptr,
+                             int rsplit = 0) {
+    ClassifyArgs ca = classify_args(j, b, r0, r1, d_thr);
+    if (b2) {  // windows of rows >= rsplit to b2's list
+        ca.work2 = b2->work;
+        ca.nwork2 = (int*)b2->ctr;
+        ca.rsplit = rsplit;
+    }
     const long tiles = (long)(r1 - r0) * ((j.ny + 255) / 256);
     k_classify<<<(int)std::max(1l, std::min<long>(tiles, (long)ctx->nsm * blocks_per_sm)), 256, 0, st>>>(ca);
     ++*launches;
@@ -652,19 +705,38 @@ BoxArgs box_args(const Job& j, const JobBufs& b) {
     return ba;
 }
 
-// Exact row sums of frame rows [r0, r1) at the grid's box columns.
-flct_status enqueue_box_rows(flct_ctx* ctx, const Job& j, const JobBufs& b, int r0, int r1, cudaStream_t st,
-                             int* launches, int blocks_per_sm = 4) {
-    if (r1 <= r0) return FLCT_OK;
+// Row pass arguments for frame rows [r0, r1), and its warp tasks.
+BoxArgs box_rows_args(const Job& j, const JobBufs& b, int r0, int r1, long* tasks) {
     BoxArgs ba = box_args(j, b);
     ba.r0 = r0;
     ba.r1 = r1;
     // a warp pass covers P grid columns whose input span fits kRowSpan
     ba.pass_r = std::max(1, std::min(j.gj, (kRowSpan - j.n) / j.gs + 1));
-    const long tasks = 2l * (r1 - r0) * ((j.gj + ba.pass_r - 1) / ba.pass_r);
-    const size_t smem = (size_t)kBoxWarps * (5 * (kRowSpan + 64) + 5 * 32) * sizeof(unsigned);
+    *tasks = 2l * (r1 - r0) * ((j.gj + ba.pass_r - 1) / ba.pass_r);
+    return ba;
+}
+
+constexpr size_t kBoxRowsSmem = (size_t)kBoxWarps * (5 * (kRowSpan + 64) + 5 * 32) * sizeof(unsigned);
+
+// Column pass arguments for grid rows [q0, q1), and its threads.
+BoxArgs box_cols_args(const Job& j, const JobBufs& b, int q0, int q1, long* threads) {
+    BoxArgs ba = box_args(j, b);
+    ba.q0 = q0;
+    ba.q1 = q1;
+    *threads = 2l * j.gj * ((q1 - q0 + kColRun - 1) / kColRun) * kColLanes;
+    return ba;
+}
+
+// Exact row sums of frame rows [r0, r1) at the grid's box columns.
+flct_status enqueue_box_rows(flct_ctx* ctx, const Job& j, const JobBufs& b, int r0, int r1, cudaStream_t st,
+                             int* launches, int blocks_per_sm = 4) {
+    if (r1 <= r0) return FLCT_OK;
+    long tasks = 0;
+    BoxArgs ba = box_rows_args(j, b, r0, r1, &tasks);
+    const size_t smem = kBoxRowsSmem;
     if (!ctx->box_attr) {
         CK(cudaFuncSetAttribute(k_box_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        CK(cudaFuncSetAttribute(k_box_rows_multi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         ctx->box_attr = true;
     }
     const long blocks = std::min<long>((tasks + kBoxWarps - 1) / kBoxWarps, (long)ctx->nsm * blocks_per_sm);
@@ -679,10 +751,8 @@ flct_status enqueue_box_rows(flct_ctx* ctx, const Job& j, const JobBufs& b, int 
 flct_status enqueue_box_cols(flct_ctx* ctx, const Job& j, const JobBufs& b, int q0, int q1, cudaStream_t st,
                              int* launches) {
     if (q1 <= q0) return FLCT_OK;
-    BoxArgs ba = box_args(j, b);
-    ba.q0 = q0;
-    ba.q1 = q1;
-    const long t = 2l * j.gj * ((q1 - q0 + kColRun - 1) / kColRun) * kColLanes;
+    long t = 0;
+    BoxArgs ba = box_cols_args(j, b, q0, q1, &t);
     k_box_cols<<<(int)((t + 127) / 128), 128, 0, st>>>(ba);
     ++*launches;
     CK(cudaGetLastError());
@@ -691,8 +761,7 @@ flct_status enqueue_box_cols(flct_ctx* ctx, const Job& j, const JobBufs& b, int 
 
 // FP64 local means of the work list b.work / b.ctr (flct.c:815-827), one
 // window per lane.
-flct_status enqueue_means(flct_ctx* ctx, const Job& j, const JobBufs& b, long max_items, cudaStream_t st,
-                          int* launches, bool pdl = false) {
+MeansArgs means_args(const Job& j, const JobBufs& b) {
     MeansArgs ma{};
     ma.work = b.work;
     ma.nwork = (const int*)b.ctr;
@@ -705,6 +774,12 @@ flct_status enqueue_means(flct_ctx* ctx, const Job& j, const JobBufs& b, long ma
     ma.bs2 = b.b2;
     ma.inv_n2 = 1. / ((double)j.n * j.n);
     ma.means = b.means;
+    return ma;
+}
+
+flct_status enqueue_means(flct_ctx* ctx, const Job& j, const JobBufs& b, long max_items, cudaStream_t st,
+                          int* launches, bool pdl = false) {
+    const MeansArgs ma = means_args(j, b);
     long blocks = std::min<long>((max_items + 255) / 256, (long)ctx->nsm * 8);
     CK(launch_kernel(k_means, dim3((unsigned)std::max(1l, blocks)), dim3(256), 0, st, pdl, ma));
     ++*launches;
@@ -723,8 +798,8 @@ flct_status enqueue_prepass(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaS
     double* d_thr = (double*)(b.ctr + 24);
     CK(cudaMemsetAsync(b.ctr, 0, 64, st));
     if (j.d.rel_thresh) {
-        k_absmax<<<ctx->nsm * 4, 256, 0, st>>>(j.f1, j.f2, (long)npx, d_absmax);
-        k_thresh_final<<<1, 1, 0, st>>>(j.f1, j.f2, d_absmax, j.p->thresh, d_thr);
+        k_absmax<<<ctx->nsm * 4, 256, 0, st>>>(AbsmaxArgs{j.f1, j.f2, (long)npx, d_absmax});
+        k_thresh_final<<<1, 1, 0, st>>>(ThreshArgs{j.f1, j.f2, d_absmax, j.p->thresh, d_thr});
         *launches += 2;
     }
     const double* thr = j.d.rel_thresh ? d_thr : nullptr;
@@ -755,6 +830,8 @@ flct_status enqueue_prepass(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaS
 void make_wargs(const Job& j, const JobBufs& b, WinArgs* wa) {
     *wa = WinArgs{};
     fill_tables(j.p, j.n, wa->gauss, wa->filt2);
+    wa->sigma = j.p->sigma;
+    wa->kr = j.p->kr;
     wa->use_filter = j.p->filter;
     wa->s1 = b.s1;
     wa->s2 = b.s2;
@@ -775,8 +852,7 @@ struct Pub {
     unsigned* dst = nullptr;
 };
 
-flct_status enqueue_fit(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaStream_t st, int* launches,
-                        long max_items = -1, Pub pub = Pub{}, bool pdl = false) {
+FitArgs fit_args(const Job& j, const JobBufs& b, Pub pub) {
     FitArgs fa{};
     fa.pub_src = pub.src;
     fa.pub_dst = pub.dst;
@@ -794,9 +870,15 @@ flct_status enqueue_fit(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaStrea
     fa.vy = j.vy;
     fa.vm = j.vm;
     fa.grid = j.interp ? b.grid : nullptr;
+    if (j.p->hires) fa.peaks_h = b.peaks_h;
+    return fa;
+}
+
+flct_status enqueue_fit(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaStream_t st, int* launches,
+                        long max_items = -1, Pub pub = Pub{}, bool pdl = false) {
+    const FitArgs fa = fit_args(j, b, pub);
     const size_t npx = max_items >= 0 ? (size_t)max_items : (size_t)j.nx * j.ny;
     if (j.p->hires) {
-        fa.peaks_h = b.peaks_h;
         long blocks = std::min<long>((long)(npx + 3) / 4, (long)ctx->nsm * 16);
         CK(launch_kernel(k_fit_hires, dim3((unsigned)std::max(1l, blocks)), dim3(128), 0, st, pdl, fa));
     } else {
@@ -810,10 +892,7 @@ flct_status enqueue_fit(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaStrea
 
 // Cubic-convolution interpolation of the skip grid onto the skipped pixels,
 // mask and xmiss reset (flct.c:958-1133).
-flct_status enqueue_interp(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaStream_t st, int* launches,
-                           int i0 = 0, int i1 = -1, Pub pub = Pub{}, bool pdl = false) {
-    if (i1 < 0) i1 = j.nx;
-    if (i1 <= i0) return FLCT_OK;
+InterpArgs interp_args(const Job& j, const JobBufs& b, int i0, int i1, Pub pub) {
     InterpArgs ia{};
     ia.pub_src = pub.src;
     ia.pub_dst = pub.dst;
@@ -832,6 +911,14 @@ flct_status enqueue_interp(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaSt
     ia.i1 = i1;
     // pixel pairs (j even) start on 16-byte boundaries when ny is even
     ia.pairs = (j.ny % 2 == 0) && ((((uintptr_t)j.vx) | ((uintptr_t)j.vy) | ((uintptr_t)j.vm)) & 15u) == 0u;
+    return ia;
+}
+
+flct_status enqueue_interp(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaStream_t st, int* launches,
+                           int i0 = 0, int i1 = -1, Pub pub = Pub{}, bool pdl = false) {
+    if (i1 < 0) i1 = j.nx;
+    if (i1 <= i0) return FLCT_OK;
+    const InterpArgs ia = interp_args(j, b, i0, i1, pub);
     const long tiles = (long)((i1 - i0 + kTileR - 1) / kTileR) * ((j.ny + kTileC - 1) / kTileC);
     CK(launch_kernel(k_interp_grid, dim3((unsigned)std::max(1l, std::min<long>(tiles, (long)ctx->nsm * 8))),
                      dim3(kInterpThreads), 0, st, pdl, ia));
@@ -843,6 +930,10 @@ flct_status enqueue_interp(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaSt
 // Occupancy queries and the tensor-core tables need the host; done before
 // a stream capture so the captured launches make none of these calls.
 flct_status prime_form(flct_ctx* ctx, int form, int n) {
+    if (form == FLCT_FORM_FP32 && n > kMaxBox) {
+        if (ctx->bps_big == 0) ctx->bps_big = std::max(1, window_big_blocks_per_sm(kMaxBigBox));
+        return FLCT_OK;
+    }
     if (form == FLCT_FORM_FP32) {
         if (win_grid(ctx, n) <= 0) return fail(ctx, FLCT_ERR_CUDA, "no occupancy for the box-%d window kernel", n);
         return FLCT_OK;
@@ -1020,15 +1111,24 @@ struct BatchGroup {
     int hires = 0;
     float gauss[2 * kMaxBox + 1] = {};
     float filt2[kMaxBox] = {};
+    double sigma = 0., kr = 0.;
     std::vector<int> pairs;
     int form = FLCT_FORM_FP32;
     int grid_div = 1;
+};
+
+// One kernel's launches for many pairs merged into one grid: the per-pair
+// argument structs and block prefix sums in the batch's device tables.
+struct MultiSet {
+    size_t args = 0, start = 0;  // byte offsets in bb_multi
+    int npairs = 0, blocks = 0;
 };
 
 struct BatchPlan {
     std::vector<Job> jobs;
     std::vector<JobBufs> bufs;
     std::vector<BatchGroup> groups;
+    MultiSet m_abs, m_thr, m_cls, m_rows, m_cols, m_means, m_fit, m_fith, m_interp;
     WinSeg* segs = nullptr;  // device, group-major
     int* starts = nullptr;   // device, per group nseg + 1 entries
     int* seg_pair = nullptr; // device
@@ -1069,6 +1169,102 @@ flct_status pair_fail(flct_ctx* ctx, flct_status s, int k) {
     return s;
 }
 
+// The merged launches of a batch's per-pair kernels: every pair's prepass
+// kernels, fit and interpolation as one grid each, with the same argument
+// structs the single-pair calls use and as many blocks per pair as the
+// pair's work (the kernels' loops are strided over the pair's own blocks).
+flct_status plan_multi(flct_ctx* ctx, BatchPlan* bp) {
+    const int np = (int)bp->jobs.size();
+    std::vector<unsigned char> host;
+    auto add = [&host](const void* p, size_t bytes) {
+        const size_t o = host.size();
+        host.resize(align256(o + bytes));
+        memcpy(host.data() + o, p, bytes);
+        return o;
+    };
+    // args and per-pair blocks -> a MultiSet (pairs with 0 blocks left out)
+    auto pack = [&](auto& args, const std::vector<long>& blocks, MultiSet* m) {
+        using A = typename std::decay_t<decltype(args)>::value_type;
+        std::vector<A> used;
+        std::vector<int> start(1, 0);
+        for (size_t k = 0; k < args.size(); ++k) {
+            if (blocks[k] <= 0) continue;
+            used.push_back(args[k]);
+            start.push_back(start.back() + (int)blocks[k]);
+        }
+        m->npairs = (int)used.size();
+        m->blocks = start.back();
+        if (!used.empty()) {
+            m->args = add(used.data(), used.size() * sizeof(A));
+            m->start = add(start.data(), start.size() * sizeof(int));
+        }
+    };
+    std::vector<AbsmaxArgs> abs;
+    std::vector<ThreshArgs> thr;
+    std::vector<ClassifyArgs> cls;
+    std::vector<BoxArgs> rows, cols;
+    std::vector<MeansArgs> means;
+    std::vector<FitArgs> fit, fith;
+    std::vector<InterpArgs> ia;
+    std::vector<long> babs, bthr, bcls, brows, bcols, bmeans, bfit, bfith, bia;
+    for (int k = 0; k < np; ++k) {
+        const Job& j = bp->jobs[k];
+        const JobBufs& b = bp->bufs[k];
+        const long npx = (long)j.nx * j.ny;
+        unsigned long long* d_absmax = (unsigned long long*)(b.ctr + 8);
+        double* d_thr = (double*)(b.ctr + 24);
+        abs.push_back(AbsmaxArgs{j.f1, j.f2, npx, d_absmax});
+        babs.push_back(j.d.rel_thresh ? std::max(1l, std::min<long>((npx + 1023) / 1024, ctx->nsm)) : 0);
+        thr.push_back(ThreshArgs{j.f1, j.f2, d_absmax, j.p->thresh, d_thr});
+        bthr.push_back(j.d.rel_thresh ? 1 : 0);
+        cls.push_back(classify_args(j, b, 0, j.nx, j.d.rel_thresh ? d_thr : nullptr));
+        bcls.push_back((long)j.nx * ((j.ny + 255) / 256));
+        long tasks = 0, threads = 0;
+        rows.push_back(box_rows_args(j, b, 0, j.nx, &tasks));
+        brows.push_back((tasks + kBoxWarps - 1) / kBoxWarps);
+        cols.push_back(box_cols_args(j, b, 0, j.gi, &threads));
+        bcols.push_back((threads + 127) / 128);
+        means.push_back(means_args(j, b));
+        bmeans.push_back(std::max(1l, (npx + 255) / 256));
+        const FitArgs fa = fit_args(j, b, Pub{});
+        fit.push_back(fa);
+        fith.push_back(fa);
+        bfit.push_back(j.p->hires ? 0 : std::max(1l, (npx + 127) / 128));
+        bfith.push_back(j.p->hires ? std::max(1l, (npx + 3) / 4) : 0);
+        ia.push_back(interp_args(j, b, 0, j.nx, Pub{}));
+        bia.push_back(j.interp ? (long)((j.nx + kTileR - 1) / kTileR) * ((j.ny + kTileC - 1) / kTileC) : 0);
+    }
+    for (const auto* v : {&babs, &bthr, &bcls, &brows, &bcols, &bmeans, &bfit, &bfith, &bia}) {
+        long tot = 0;
+        for (long x : *v) tot += x;
+        if (tot >= (1l << 31)) return fail(ctx, FLCT_ERR_UNSUPPORTED, "batch needs more than 2^31 blocks");
+    }
+    pack(abs, babs, &bp->m_abs);
+    pack(thr, bthr, &bp->m_thr);
+    pack(cls, bcls, &bp->m_cls);
+    pack(rows, brows, &bp->m_rows);
+    pack(cols, bcols, &bp->m_cols);
+    pack(means, bmeans, &bp->m_means);
+    pack(fit, bfit, &bp->m_fit);
+    pack(fith, bfith, &bp->m_fith);
+    pack(ia, bia, &bp->m_interp);
+    ENSURE(ctx->bb_multi, std::max<size_t>(host.size(), 256));
+    CK(cudaMemcpy(ctx->bb_multi.p, host.data(), host.size(), cudaMemcpyHostToDevice));
+    return FLCT_OK;
+}
+
+// Launch a merged kernel of the batch (nothing when no pair has blocks).
+template <class A>
+cudaError_t launch_multi(flct_ctx* ctx, void (*kern)(MultiArgs<A>), const MultiSet& m, int threads, size_t smem,
+                         cudaStream_t st, int* launches) {
+    if (m.npairs == 0) return cudaSuccess;
+    const unsigned char* M = (const unsigned char*)ctx->bb_multi.p;
+    MultiArgs<A> ma{(const A*)(M + m.args), (const int*)(M + m.start), m.npairs};
+    kern<<<m.blocks, threads, smem, st>>>(ma);
+    ++*launches;
+    return cudaGetLastError();
+}
+
 // Checks every pair, groups the pairs, lays out and allocates the batch
 // workspace and uploads the segment tables.
 flct_status plan_batch(flct_ctx* ctx, int npairs, const flct_pair* pairs, BatchPlan* bp) {
@@ -1092,9 +1288,12 @@ flct_status plan_batch(flct_ctx* ctx, int npairs, const flct_pair* pairs, BatchP
         g.use_filter = j.p->filter ? 1 : 0;
         g.hires = j.p->hires ? 1 : 0;
         fill_tables(j.p, j.n, g.gauss, g.filt2);
+        g.sigma = j.p->sigma;
+        g.kr = j.p->filter ? j.p->kr : 0.;
         bool found = false;
         for (auto& G : bp->groups)
             if (G.n == g.n && G.req_form == g.req_form && G.use_filter == g.use_filter && G.hires == g.hires &&
+                (g.n <= kMaxBox || (G.sigma == g.sigma && G.kr == g.kr)) &&
                 !memcmp(G.gauss, g.gauss, sizeof(g.gauss)) && !memcmp(G.filt2, g.filt2, sizeof(g.filt2))) {
                 G.pairs.push_back(k);
                 found = true;
@@ -1196,7 +1395,7 @@ flct_status plan_batch(flct_ctx* ctx, int npairs, const flct_pair* pairs, BatchP
     bp->starts = (int*)(M + seg_bytes);
     bp->seg_pair = (int*)(M + seg_bytes + start_bytes);
     bp->first = (int*)(M + seg_bytes + start_bytes + pair_bytes);
-    return FLCT_OK;
+    return plan_multi(ctx, bp);
 }
 
 // Window-kernel arguments of group g (all its pairs in one launch).
@@ -1205,6 +1404,8 @@ void group_wargs(flct_ctx* ctx, const BatchPlan& bp, int g, WinArgs* wa) {
     *wa = WinArgs{};
     memcpy(wa->gauss, G.gauss, sizeof(G.gauss));
     memcpy(wa->filt2, G.filt2, sizeof(G.filt2));
+    wa->sigma = G.sigma;
+    wa->kr = G.kr;
     wa->use_filter = G.use_filter;
     wa->means = (const float4*)ctx->bb_means.p;
     wa->work = (const int*)ctx->bb_work.p;
@@ -1217,38 +1418,57 @@ void group_wargs(flct_ctx* ctx, const BatchPlan& bp, int g, WinArgs* wa) {
     wa->nwork = wa->seg_start + wa->nseg;
 }
 
-// Enqueues a planned batch on `bs`: every pair's prepass, the per-group
-// prefix sums, one persistent window launch per group, every pair's fit and
-// interpolation.  With `branches` the per-pair and per-group work spreads
-// over the context's branch streams (fork / join through events), which a
-// stream capture turns into parallel graph branches.
-flct_status enqueue_batch(flct_ctx* ctx, BatchPlan& bp, cudaStream_t bs, bool branches, int* launches) {
+// The prepass of every pair of a batch as merged launches: one counter
+// memset, the relative thresholds, the classification (on a side stream,
+// beside the box sums: all three only read the frames), row and column box
+// sums, means, then the per-group prefix sums of the work counts.  With
+// `side` null everything runs on bs.
+flct_status enqueue_batch_prepass(flct_ctx* ctx, BatchPlan& bp, cudaStream_t bs, cudaStream_t side, int* launches) {
     const int np = (int)bp.jobs.size();
     const int ng = (int)bp.groups.size();
-    const int nb = branches ? std::min(np, flct_ctx::kBranches) : 0;
-    auto fork = [&]() -> flct_status {
-        if (!nb) return FLCT_OK;
+    CK(cudaMemsetAsync(ctx->bb_ctr.p, 0, (size_t)np * 64, bs));
+    CK(launch_multi(ctx, k_absmax_multi, bp.m_abs, 256, 0, bs, launches));
+    CK(launch_multi(ctx, k_thresh_final_multi, bp.m_thr, 32, 0, bs, launches));
+    cudaStream_t cs = side ? side : bs;
+    if (side) {
         CK(cudaEventRecord(ctx->bev[0], bs));
-        for (int k = 0; k < nb; ++k) CK(cudaStreamWaitEvent(ctx->bstream[k], ctx->bev[0], 0));
-        return FLCT_OK;
-    };
-    auto join = [&]() -> flct_status {
-        for (int k = 0; k < nb; ++k) {
-            CK(cudaEventRecord(ctx->bev[1 + k], ctx->bstream[k]));
-            CK(cudaStreamWaitEvent(bs, ctx->bev[1 + k], 0));
-        }
-        return FLCT_OK;
-    };
-    auto lane = [&](int i) { return nb ? ctx->bstream[i % nb] : bs; };
-    flct_status s = fork();
-    for (int k = 0; k < np && s == FLCT_OK; ++k) s = enqueue_prepass(ctx, bp.jobs[k], bp.bufs[k], lane(k), launches);
-    if (s == FLCT_OK) s = join();
-    if (s != FLCT_OK) return s;
+        CK(cudaStreamWaitEvent(side, ctx->bev[0], 0));
+    }
+    if (!ctx->box_attr) {
+        CK(cudaFuncSetAttribute(k_box_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBoxRowsSmem));
+        CK(cudaFuncSetAttribute(k_box_rows_multi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBoxRowsSmem));
+        ctx->box_attr = true;
+    }
+    CK(launch_multi(ctx, k_box_rows_multi, bp.m_rows, kBoxWarps * 32, kBoxRowsSmem, bs, launches));
+    CK(launch_multi(ctx, k_classify_multi, bp.m_cls, 256, 0, cs, launches));
+    CK(launch_multi(ctx, k_box_cols_multi, bp.m_cols, 128, 0, bs, launches));
+    if (side) {
+        CK(cudaEventRecord(ctx->bev[1], side));
+        CK(cudaStreamWaitEvent(bs, ctx->bev[1], 0));
+    }
+    CK(launch_multi(ctx, k_means_multi, bp.m_means, 256, 0, bs, launches));
     k_batch_starts<<<(ng + 31) / 32, 32, 0, bs>>>((const unsigned char*)ctx->bb_ctr.p, bp.seg_pair, bp.first, ng,
                                                    bp.starts);
     ++*launches;
     CK(cudaGetLastError());
-    s = fork();
+    return FLCT_OK;
+}
+
+// Enqueues a planned batch on `bs`: the merged prepass, one persistent
+// window launch per group (groups on the context's branch streams, so that
+// a stream capture makes them parallel graph branches), then the merged
+// fit and interpolation of every pair.
+flct_status enqueue_batch(flct_ctx* ctx, BatchPlan& bp, cudaStream_t bs, bool branches, int* launches) {
+    const int np = (int)bp.jobs.size();
+    const int ng = (int)bp.groups.size();
+    const int nb = branches ? std::min(std::max(ng, 1), flct_ctx::kBranches) : 0;
+    flct_status s = enqueue_batch_prepass(ctx, bp, bs, branches ? ctx->bstream[0] : nullptr, launches);
+    if (s != FLCT_OK) return s;
+    if (nb) {
+        CK(cudaEventRecord(ctx->bev[0], bs));
+        for (int k = 0; k < nb; ++k) CK(cudaStreamWaitEvent(ctx->bstream[k], ctx->bev[0], 0));
+    }
+    auto lane = [&](int i) { return nb ? ctx->bstream[i % nb] : bs; };
     for (int g = 0; g < ng && s == FLCT_OK; ++g) {
         const BatchGroup& G = bp.groups[g];
         WinArgs wa;
@@ -1257,15 +1477,16 @@ flct_status enqueue_batch(flct_ctx* ctx, BatchPlan& bp, cudaStream_t bs, bool br
         s = launch_windows(ctx, G.form, find_win(G.n), G.n, wa, status, lane(g), G.grid_div);
         ++*launches;
     }
-    if (s == FLCT_OK) s = join();
     if (s != FLCT_OK) return s;
-    s = fork();
-    for (int k = 0; k < np && s == FLCT_OK; ++k) {
-        s = enqueue_fit(ctx, bp.jobs[k], bp.bufs[k], lane(k), launches);
-        if (s == FLCT_OK && bp.jobs[k].interp) s = enqueue_interp(ctx, bp.jobs[k], bp.bufs[k], lane(k), launches);
+    for (int k = 0; k < nb; ++k) {
+        CK(cudaEventRecord(ctx->bev[1 + k], ctx->bstream[k]));
+        CK(cudaStreamWaitEvent(bs, ctx->bev[1 + k], 0));
     }
-    if (s == FLCT_OK) s = join();
-    return s;
+    CK(launch_multi(ctx, k_fit_multi, bp.m_fit, 128, 0, bs, launches));
+    CK(launch_multi(ctx, k_fit_hires_multi, bp.m_fith, 128, 0, bs, launches));
+    CK(launch_multi(ctx, k_interp_grid_multi, bp.m_interp, kInterpThreads, 0, bs, launches));
+    (void)np;
+    return FLCT_OK;
 }
 
 // Autotunes every FLCT_FORM_AUTO group whose box size has no measurement
@@ -1275,14 +1496,9 @@ flct_status tune_batch(flct_ctx* ctx, BatchPlan& bp, cudaStream_t bs) {
     for (const auto& G : bp.groups) any |= G.req_form == FLCT_FORM_AUTO && !ctx->tune.count(G.n);
     if (!any) return FLCT_OK;
     int launches = 0;
-    for (size_t k = 0; k < bp.jobs.size(); ++k) {
-        flct_status s = enqueue_prepass(ctx, bp.jobs[k], bp.bufs[k], bs, &launches);
-        if (s != FLCT_OK) return s;
-    }
+    flct_status ps = enqueue_batch_prepass(ctx, bp, bs, nullptr, &launches);
+    if (ps != FLCT_OK) return ps;
     const int ng = (int)bp.groups.size();
-    k_batch_starts<<<(ng + 31) / 32, 32, 0, bs>>>((const unsigned char*)ctx->bb_ctr.p, bp.seg_pair, bp.first, ng,
-                                                   bp.starts);
-    CK(cudaGetLastError());
     for (int g = 0; g < ng; ++g) {
         const BatchGroup& G = bp.groups[g];
         if (G.req_form != FLCT_FORM_AUTO || ctx->tune.count(G.n)) continue;
@@ -2141,7 +2357,8 @@ flct_status flct_gpu_cross_cor_batch(flct_ctx* ctx, const double* g1, const doub
         return fail(ctx, FLCT_ERR_ARG, "null pointer or bad window size");
     if (nwin == 0) return FLCT_OK;
     const WinEntry* we = find_win(n);
-    if (!we) return fail(ctx, FLCT_ERR_UNSUPPORTED, "window size %d has no GPU kernel", n);
+    if (!we && (n > kMaxBigBox || n % 4 != 0))
+        return fail(ctx, FLCT_ERR_UNSUPPORTED, "window size %d has no GPU kernel", n);
     int fsel = FLCT_FORM_FP32;
     {
         flct_status fs = pick_form(ctx, form, n, &fsel);
@@ -2199,7 +2416,9 @@ flct_status flct_gpu_cross_cor_batch(flct_ctx* ctx, const double* g1, const doub
         fp.sigma = 1.0;
         fill_tables(&fp, n, wa.gauss, wa.filt2);
     }
-    for (int k = 0; k <= 2 * n; ++k) wa.gauss[k] = 1.0f;
+    for (int k = 0; k <= 2 * n && k <= 2 * kMaxBox; ++k) wa.gauss[k] = 1.0f;
+    wa.sigma = 1.0;
+    wa.kr = kr;
     wa.use_filter = filter;
     wa.s1 = (const float2*)ctx->b_s1.p;
     wa.s2 = (const float2*)ctx->b_s2.p;

@@ -30,35 +30,35 @@ __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v)
 
 // max(|f|) over non-NaN elements of both frames, as IEEE bit patterns
 // (for non-negative doubles the bit order is the numeric order).
-__global__ void k_absmax(const double* __restrict__ f1, const double* __restrict__ f2, long n,
-                         unsigned long long* __restrict__ out) {
+__device__ __forceinline__ void k_absmax_body(const AbsmaxArgs& a, const int vb, const int vg) {
     unsigned long long m1 = 0ull, m2 = 0ull;
     const unsigned long long kAbs = 0x7fffffffffffffffull, kInf = 0x7ff0000000000000ull;
-    for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
-        unsigned long long a = (unsigned long long)__double_as_longlong(f1[k]) & kAbs;
-        unsigned long long b = (unsigned long long)__double_as_longlong(f2[k]) & kAbs;
-        if (a <= kInf && a > m1) m1 = a;
-        if (b <= kInf && b > m2) m2 = b;
+    for (long k = vb * (long)blockDim.x + threadIdx.x; k < a.n; k += (long)vg * blockDim.x) {
+        unsigned long long x = (unsigned long long)__double_as_longlong(a.f1[k]) & kAbs;
+        unsigned long long y = (unsigned long long)__double_as_longlong(a.f2[k]) & kAbs;
+        if (x <= kInf && x > m1) m1 = x;
+        if (y <= kInf && y > m2) m2 = y;
     }
     m1 = warp_max_u64(m1);
     m2 = warp_max_u64(m2);
     if ((threadIdx.x & 31) == 0) {
-        atomicMax(out, m1);
-        atomicMax(out + 1, m2);
+        atomicMax(a.out, m1);
+        atomicMax(a.out + 1, m2);
     }
 }
+FLCT_MULTI_KERNEL(, k_absmax, AbsmaxArgs)
 
 // thresh *= max(f1max, f2max), where fNmax follows maxloc's sequential scan:
 // a NaN first element is never replaced (flct.c:608-621, 2142-2161).
-__global__ void k_thresh_final(const double* __restrict__ f1, const double* __restrict__ f2,
-                               const unsigned long long* __restrict__ mx, double thresh,
-                               double* __restrict__ thr) {
-    double a1 = fabs(f1[0]), a2 = fabs(f2[0]);
-    double m1 = (a1 != a1) ? a1 : __longlong_as_double((long long)mx[0]);
-    double m2 = (a2 != a2) ? a2 : __longlong_as_double((long long)mx[1]);
+__device__ __forceinline__ void k_thresh_final_body(const ThreshArgs& a, const int, const int) {
+    if (threadIdx.x != 0) return;
+    double a1 = fabs(a.f1[0]), a2 = fabs(a.f2[0]);
+    double m1 = (a1 != a1) ? a1 : __longlong_as_double((long long)a.mx[0]);
+    double m2 = (a2 != a2) ? a2 : __longlong_as_double((long long)a.mx[1]);
     double fmax = (m1 > m2) ? m1 : m2;
-    *thr = __dmul_rn(thresh, fmax);
+    *a.thr = __dmul_rn(a.thresh, fmax);
 }
+FLCT_MULTI_KERNEL(, k_thresh_final, ThreshArgs)
 
 // ------------------------------------------------------- classify ----
 
@@ -73,7 +73,7 @@ __device__ __forceinline__ bool finite_bits(double x) {
 // split of both frames uses integer operations, and the threshold test
 // 0.5*|f1+f2| < thresh (flct.c:721-722) needs one FP64 add only when the
 // threshold is positive (otherwise no pixel is below it).
-__global__ void __launch_bounds__(256) k_classify(ClassifyArgs a) {
+__device__ __forceinline__ void k_classify_body(const ClassifyArgs& a, const int vb, const int vg) {
     __shared__ int s_cnt[8];
     __shared__ int s_base;
     const double thr = a.thr_ptr ? *a.thr_ptr : a.thr_val;
@@ -93,22 +93,22 @@ __global__ void __launch_bounds__(256) k_classify(ClassifyArgs a) {
         j0 = (t - ti * tpr) * 256;
     };
     double fa = 0., fb = 0.;
-    if (blockIdx.x < ntile) {
+    if (vb < ntile) {
         int i, j0;
-        pixel(blockIdx.x, i, j0);
+        pixel(vb, i, j0);
         if (j0 + (int)threadIdx.x < a.ny) {
             fa = a.f1[(size_t)i * a.ny + j0 + threadIdx.x];
             fb = a.f2[(size_t)i * a.ny + j0 + threadIdx.x];
         }
     }
-    for (int t = blockIdx.x; t < ntile; t += gridDim.x) {
+    for (int t = vb; t < ntile; t += vg) {
         int i, j0;
         pixel(t, i, j0);
         const int j = j0 + threadIdx.x;
         double na = 0., nb = 0.;
-        if (t + (int)gridDim.x < ntile) {
+        if (t + (int)vg < ntile) {
             int i2, j2;
-            pixel(t + gridDim.x, i2, j2);
+            pixel(t + vg, i2, j2);
             if (j2 + (int)threadIdx.x < a.ny) {
                 na = a.f1[(size_t)i2 * a.ny + j2 + threadIdx.x];
                 nb = a.f2[(size_t)i2 * a.ny + j2 + threadIdx.x];
@@ -183,6 +183,7 @@ __global__ void __launch_bounds__(256) k_classify(ClassifyArgs a) {
         fb = nb;
     }
 }
+FLCT_MULTI_KERNEL(__launch_bounds__(256), k_classify, ClassifyArgs)
 
 // ------------------------------------------------------- box sums ----
 
@@ -195,7 +196,7 @@ __global__ void __launch_bounds__(256) k_classify(ClassifyArgs a) {
 // exclusive warp scan of the lane totals gives each chunk's offset, and
 // lane L then takes grid columns M + L, M + L + 32, ...: a box sum is the
 // difference of two prefix sums, stored coalesced.
-__global__ void __launch_bounds__(kBoxWarps * 32) k_box_rows(BoxArgs a) {
+__device__ __forceinline__ void k_box_rows_body(const BoxArgs& a, const int vb, const int vg) {
     extern __shared__ unsigned s_rw[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     constexpr int SW = kRowSpan + 64;  // staged words per array (chunks of up to C <= kRowSpan / 32 + 2)
@@ -204,8 +205,8 @@ __global__ void __launch_bounds__(kBoxWarps * 32) k_box_rows(BoxArgs a) {
     const int rows = a.r1 - a.r0, lines = 2 * rows;
     const int P = a.pass_r;
     const int passes = (a.gj + P - 1) / P;
-    for (long task = (long)blockIdx.x * kBoxWarps + warp; task < (long)lines * passes;
-         task += (long)gridDim.x * kBoxWarps) {
+    for (long task = (long)vb * kBoxWarps + warp; task < (long)lines * passes;
+         task += (long)vg * kBoxWarps) {
         const int lam = (int)(task / passes), pass = (int)(task - (long)lam * passes);
         const int img = lam >= rows, i = a.r0 + lam - img * rows;
         const double* __restrict__ v = (img ? a.f2 : a.f1) + (size_t)i * a.ny;
@@ -294,6 +295,7 @@ __global__ void __launch_bounds__(kBoxWarps * 32) k_box_rows(BoxArgs a) {
         __syncwarp();  // the next pass overwrites the stage
     }
 }
+FLCT_MULTI_KERNEL(__launch_bounds__(kBoxWarps * 32), k_box_rows, BoxArgs)
 
 // Box sums B[q][m] = sum_{ii<n} RT[t_q + ii][m] at the grid's box rows
 // t_q = box_start(xo + q gs), exact.  kColLanes consecutive lanes take one
@@ -314,10 +316,10 @@ __device__ __forceinline__ void col_reduce(unsigned long long& lo, unsigned long
     }
 }
 
-__global__ void __launch_bounds__(128) k_box_cols(BoxArgs a) {
+__device__ __forceinline__ void k_box_cols_body(const BoxArgs& a, const int vb, const int vg) {
     const int lines = 2 * a.gj;
     const int runs = (a.q1 - a.q0 + kColRun - 1) / kColRun;
-    const long gid = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    const long gid = vb * (long)blockDim.x + threadIdx.x;
     const int p = (int)(gid & (kColLanes - 1));
     long idx = gid / kColLanes;
     // a group past the end repeats the last line (every lane of the warp
@@ -372,6 +374,7 @@ __global__ void __launch_bounds__(128) k_box_cols(BoxArgs a) {
         t = tn;
     }
 }
+FLCT_MULTI_KERNEL(__launch_bounds__(128), k_box_cols, BoxArgs)
 
 // --------------------------------------------------- interpolation ----
 
@@ -516,7 +519,7 @@ constexpr int kPatchR = kTileR + 4, kPatchC = kTileC + 4;  // cdata rows / colum
 constexpr int kPairCols = kTileC / 2;                       // threads per tile row in the output step
 constexpr int kPairRows = kInterpThreads / kPairCols;       // tile rows per output pass
 
-__global__ void __launch_bounds__(kInterpThreads) k_interp_grid(InterpArgs a) {
+__device__ __forceinline__ void k_interp_grid_body(const InterpArgs& a, const int vb, const int vg) {
     __shared__ float2 s_p[kPatchR * kPatchC];
     __shared__ unsigned char s_pb[kPatchR * kPatchC];
     __shared__ float2 s_v[kTileR * kPatchC];
@@ -534,7 +537,7 @@ __global__ void __launch_bounds__(kInterpThreads) k_interp_grid(InterpArgs a) {
     const int tc = (threadIdx.x % kPairCols) * 2, tr = threadIdx.x / kPairCols;
     grid_dep_wait();
     publish_counters(a.pub_src, a.pub_dst);
-    for (int tile = blockIdx.x; tile < ntr * ntc; tile += gridDim.x) {
+    for (int tile = vb; tile < ntr * ntc; tile += vg) {
         const int i0 = a.i0 + (tile / ntc) * kTileR, j0 = (tile - (tile / ntc) * ntc) * kTileC;
         // cdata rows / columns the tile's in-range pixels use
         const int dlo = max(i0 - a.xoff, 0), dhi = min(min(i0 + kTileR, a.i1) - 1 - a.xoff, imax);
@@ -661,6 +664,7 @@ __global__ void __launch_bounds__(kInterpThreads) k_interp_grid(InterpArgs a) {
         }
     }
 }
+FLCT_MULTI_KERNEL(__launch_bounds__(kInterpThreads), k_interp_grid, InterpArgs)
 
 // interpcc2d on caller arrays (the standalone entry point).
 __global__ void k_interp_general(const double* __restrict__ f, int gx, int gy, double xmiss,

@@ -66,12 +66,34 @@ struct InterpArgs {
     unsigned* pub_dst;
 };
 
-__global__ void k_absmax(const double* f1, const double* f2, long n, unsigned long long* out);
-__global__ void k_thresh_final(const double* f1, const double* f2, const unsigned long long* mx,
-                               double thresh, double* thr);
+// max |f| of both frames (IEEE bit patterns, NaN skipped) into out[0..1]
+struct AbsmaxArgs {
+    const double* f1;
+    const double* f2;
+    long n;
+    unsigned long long* out;
+};
+// the relative threshold thresh * max(f1max, f2max) into *thr
+struct ThreshArgs {
+    const double* f1;
+    const double* f2;
+    const unsigned long long* mx;
+    double thresh;
+    double* thr;
+};
+
+__global__ void k_absmax(AbsmaxArgs a);
+__global__ void k_thresh_final(ThreshArgs a);
 __global__ void k_classify(ClassifyArgs a);
 __global__ void k_box_rows(BoxArgs a);
 __global__ void k_box_cols(BoxArgs a);
+// the same kernels over many frame pairs at once (MultiArgs, common.cuh)
+__global__ void k_absmax_multi(MultiArgs<AbsmaxArgs> m);
+__global__ void k_thresh_final_multi(MultiArgs<ThreshArgs> m);
+__global__ void k_classify_multi(MultiArgs<ClassifyArgs> m);
+__global__ void k_box_rows_multi(MultiArgs<BoxArgs> m);
+__global__ void k_box_cols_multi(MultiArgs<BoxArgs> m);
+__global__ void k_interp_grid_multi(MultiArgs<InterpArgs> m);
 __global__ void k_interp_axis(int n, int gcount, int off, int skip, const double* want, int* zero,
                               double* wts, unsigned char* ok);
 __global__ void k_interp_grid(InterpArgs a);

@@ -7,10 +7,10 @@ __device__ __forceinline__ double dm(double a, double b) { return __dmul_rn(a, b
 __device__ __forceinline__ double da(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double ds(double a, double b) { return __dsub_rn(a, b); }
 
-__global__ void k_means(MeansArgs a) {
+__device__ __forceinline__ void k_means_body(const MeansArgs& a, const int vb, const int vg) {
     grid_dep_wait();
     const int nw = *a.nwork;
-    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < nw; w += gridDim.x * blockDim.x) {
+    for (int w = vb * blockDim.x + threadIdx.x; w < nw; w += vg * blockDim.x) {
         const int pix = a.work[w];
         const int i = pix / a.ny, j = pix - (pix / a.ny) * a.ny;
         const size_t b = (size_t)((i - a.xo) / a.gs) * a.gj + (j - a.yo) / a.gs;
@@ -20,6 +20,7 @@ __global__ void k_means(MeansArgs a) {
         a.means[w] = make_float4(m1.x, m1.y, m2.x, m2.y);
     }
 }
+FLCT_MULTI_KERNEL(, k_means, MeansArgs)
 
 // Shifts of work item w to velocity, mask and the skip-grid copy
 // (flct.c:901-942, 1125-1133), or to the raw-shift outputs.
@@ -73,13 +74,13 @@ __device__ __forceinline__ void fit3x3(const double* v, double* sx, double* sy) 
 // to block c mod gridDim), so every SM gets about the same number of fits:
 // the kernel is bound by each SM's FP64 pipe, and a plain grid-stride
 // mapping leaves the low blocks (and the SMs holding them) with the most.
-__global__ void k_fit(FitArgs a) {
+__device__ __forceinline__ void k_fit_body(const FitArgs& a, const int vb, const int vg) {
     grid_dep_wait();
     publish_counters(a.pub_src, a.pub_dst);
     const int nw = *a.nwork;
     const int half = a.n / 2, half1 = (a.n1 ? a.n1 : a.n) / 2;
     const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
-    for (long c = blockIdx.x + (long)gridDim.x * (threadIdx.x >> 5); c * 32 < nw; c += (long)gridDim.x * wpb) {
+    for (long c = vb + (long)vg * (threadIdx.x >> 5); c * 32 < nw; c += (long)vg * wpb) {
         const int w = (int)(c * 32) + lane;
         if (w >= nw) continue;
         const PeakRec r = a.peaks[w];
@@ -94,6 +95,7 @@ __global__ void k_fit(FitArgs a) {
         store_shift(a, w, da((double)(I - half), sx), da((double)(J - half1), sy));
     }
 }
+FLCT_MULTI_KERNEL(, k_fit, FitArgs)
 
 // ------------------------------------------------------------- -h ------
 
@@ -138,7 +140,7 @@ __device__ __forceinline__ unsigned ordered_bits(float v) {
 // maximum, and the 3x3 fit there scaled by 0.1.  One warp per work item;
 // lane j < 21 owns zoom column j.  The interpolation runs in FP32 on the
 // FP32 |c| patch, the fit and the shift in FP64.
-__global__ void __launch_bounds__(128) k_fit_hires(FitArgs a) {
+__device__ __forceinline__ void k_fit_hires_body(const FitArgs& a, const int vb, const int vg) {
     constexpr int NI = 21, P = kHiresPatch;
     __shared__ float s_p[4][P * P];
     __shared__ float s_h[4][P][NI];
@@ -151,7 +153,7 @@ __global__ void __launch_bounds__(128) k_fit_hires(FitArgs a) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nw = *a.nwork;
     const int n = a.n, m = a.n1 ? a.n1 : a.n;
-    for (int w = blockIdx.x * 4 + warp; w < nw; w += gridDim.x * 4) {
+    for (int w = vb * 4 + warp; w < nw; w += vg * 4) {
         const PeakRecH& r = a.peaks_h[w];
         s_p[warp][lane] = r.v[lane];
         if (lane < P * P - 32) s_p[warp][32 + lane] = r.v[32 + lane];
@@ -247,6 +249,7 @@ __global__ void __launch_bounds__(128) k_fit_hires(FitArgs a) {
         __syncwarp();
     }
 }
+FLCT_MULTI_KERNEL(__launch_bounds__(128), k_fit_hires, FitArgs)
 
 __global__ void k_batch_starts(const unsigned char* ctr, const int* seg_pair, const int* first, int ngroups,
                                int* start) {

@@ -100,6 +100,10 @@ __device__ __forceinline__ int seg_find(const int* __restrict__ start, int nseg,
 __global__ void k_means(MeansArgs a);
 __global__ void k_fit(FitArgs a);
 __global__ void k_fit_hires(FitArgs a);
+// the same kernels over many frame pairs at once (MultiArgs, common.cuh)
+__global__ void k_means_multi(MultiArgs<MeansArgs> m);
+__global__ void k_fit_multi(MultiArgs<FitArgs> m);
+__global__ void k_fit_hires_multi(MultiArgs<FitArgs> m);
 
 // Batched launches: for every group g, start[first[g] + g + k] (k = 0..nseg)
 // = prefix sums of the work counts (int at ctr + 64 * pair) of the group's

@@ -48,6 +48,8 @@ struct WinArgs {
     int nseg;
     float gauss[2 * kMaxBox + 1];  // weight of offset d at d + n (separable Gaussian)
     float filt2[kMaxBox];          // squared k-space filter factor by frequency index
+    // boxes above kMaxBox: the big-box kernel builds its own tables from these
+    double sigma, kr;
 };
 
 template <int N>

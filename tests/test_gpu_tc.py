@@ -208,7 +208,7 @@ def test_auto_form_and_unsupported_box():
     # chose one of the FP32-accurate forms
     assert _lib.context(0).timing().form in (_lib.FORMS["fp32"], _lib.FORMS["tc_fp16"])
     assert np.all(got[2] == 1)
-    # boxes above 64 have no window kernel of either form
+    # boxes above 64 have no tensor-core kernel (the FP32 big-box kernel serves them)
     big = rng.standard_normal((220, 220))
     with pytest.raises(FlctError) as e:
         run(big, big, "tc_fp16", sigma=16.0)
