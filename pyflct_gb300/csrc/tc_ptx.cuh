@@ -73,6 +73,24 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, uint6
     }
 }
 
+// mbar_wait for a single polling thread: it naps `nap_ns` between tries,
+// so its warp leaves the scheduler's issue slots to the other warps.
+__device__ __forceinline__ bool mbar_wait_nap(uint64_t* mbar, uint32_t parity, uint64_t limit_ns, unsigned nap_ns) {
+    const uint32_t a = smem_u32(mbar);
+    uint32_t done = 0;
+    const uint64_t t0 = globaltimer();
+    while (true) {
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            "selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(a), "r"(parity));
+        if (done) return true;
+        if (globaltimer() - t0 > limit_ns) return false;
+        __nanosleep(nap_ns);
+    }
+}
+
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;"); }
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;"); }

@@ -321,7 +321,7 @@ __global__ void __launch_bounds__(256, TcCfg<N>::MINB) k_window_tc(TcArgs a) {
     auto wait_stage = [&]() -> bool {
         bool done = true;
         if (t == 0)
-            done = a.stall_ns ? tc::mbar_wait(s_never, 0u, a.stall_ns) : tc::mbar_wait(s_mbar, phase, kLimit);
+            done = a.stall_ns ? tc::mbar_wait(s_never, 0u, a.stall_ns) : tc::mbar_wait_nap(s_mbar, phase, kLimit, 64);
         phase ^= 1u;
         const bool all = __syncthreads_and(done ? 1 : 0) != 0;
         tc::fence_after();
