@@ -364,6 +364,7 @@ flct_status launch_windows(flct_ctx* ctx, int form, const WinEntry* we, int n, c
         ba.s1 = wa.s1;
         ba.s2 = wa.s2;
         ba.means = wa.means;
+        ba.mg = wa.mg;
         ba.work = wa.work;
         ba.nwork = wa.nwork;
         ba.nx = wa.nx;
@@ -413,6 +414,7 @@ flct_status launch_windows(flct_ctx* ctx, int form, const WinEntry* we, int n, c
     ta.s1 = wa.s1;
     ta.s2 = wa.s2;
     ta.means = wa.means;
+    ta.mg = wa.mg;
     ta.work = wa.work;
     ta.nwork = wa.nwork;
     ta.nx = wa.nx;
@@ -602,13 +604,11 @@ struct JobBufs {
     float2* s1 = nullptr;
     float2* s2 = nullptr;
     int* work = nullptr;
-    float4* means = nullptr;
+    float4* means = nullptr;  // local means [gi][gj] (MeanGrid)
     PeakRec* peaks = nullptr;
     PeakRecH* peaks_h = nullptr;  // -h only
     BoxSum* r1 = nullptr;  // exact row sums [nx][gj]
     BoxSum* r2 = nullptr;
-    BoxSum* b1 = nullptr;  // exact box sums [gi][gj]
-    BoxSum* b2 = nullptr;
     int* re1 = nullptr;    // the row sums' exponents [nx][gj]
     int* re2 = nullptr;
     // 64 bytes: [0] work count (int), [4] status bits, [8..23] |f1|,|f2|
@@ -619,7 +619,7 @@ struct JobBufs {
 
 // Bytes of each workspace region of a job.
 struct JobSizes {
-    size_t s = 0, work = 0, means = 0, peaks = 0, peaks_h = 0, r = 0, re = 0, b = 0, grid = 0;
+    size_t s = 0, work = 0, means = 0, peaks = 0, peaks_h = 0, r = 0, re = 0, grid = 0;
 };
 
 JobSizes job_sizes(const Job& j) {
@@ -627,12 +627,11 @@ JobSizes job_sizes(const Job& j) {
     JobSizes z;
     z.s = npx * sizeof(float2);
     z.work = npx * sizeof(int);
-    z.means = npx * sizeof(float4);
+    z.means = (size_t)j.gi * j.gj * sizeof(float4);
     z.peaks = npx * sizeof(PeakRec);
     if (j.p->hires) z.peaks_h = npx * sizeof(PeakRecH);
     z.r = (size_t)j.gj * j.nx * sizeof(BoxSum);
     z.re = (size_t)j.gj * j.nx * sizeof(int);
-    z.b = (size_t)j.gi * j.gj * sizeof(BoxSum);
     if (j.interp) z.grid = (size_t)j.gi * j.gj * sizeof(float2);
     return z;
 }
@@ -698,8 +697,8 @@ BoxArgs box_args(const Job& j, const JobBufs& b) {
     ba.gj = j.gj;
     ba.rt1 = b.r1;
     ba.rt2 = b.r2;
-    ba.b1 = b.b1;
-    ba.b2 = b.b2;
+    ba.means = b.means;
+    ba.inv_n2 = 1. / ((double)j.n * j.n);
     ba.re1 = b.re1;
     ba.re2 = b.re2;
     return ba;
@@ -759,36 +758,8 @@ flct_status enqueue_box_cols(flct_ctx* ctx, const Job& j, const JobBufs& b, int 
     return FLCT_OK;
 }
 
-// FP64 local means of the work list b.work / b.ctr (flct.c:815-827), one
-// window per lane.
-MeansArgs means_args(const Job& j, const JobBufs& b) {
-    MeansArgs ma{};
-    ma.work = b.work;
-    ma.nwork = (const int*)b.ctr;
-    ma.ny = j.ny;
-    ma.gs = j.gs;
-    ma.xo = j.xo;
-    ma.yo = j.yo;
-    ma.gj = j.gj;
-    ma.bs1 = b.b1;
-    ma.bs2 = b.b2;
-    ma.inv_n2 = 1. / ((double)j.n * j.n);
-    ma.means = b.means;
-    return ma;
-}
-
-flct_status enqueue_means(flct_ctx* ctx, const Job& j, const JobBufs& b, long max_items, cudaStream_t st,
-                          int* launches, bool pdl = false) {
-    const MeansArgs ma = means_args(j, b);
-    long blocks = std::min<long>((max_items + 255) / 256, (long)ctx->nsm * 8);
-    CK(launch_kernel(k_means, dim3((unsigned)std::max(1l, blocks)), dim3(256), 0, st, pdl, ma));
-    ++*launches;
-    CK(cudaGetLastError());
-    return FLCT_OK;
-}
-
 // The whole-frame prepass: counters, relative threshold (flct.c:594-629),
-// classification, box sums and means.  With a side stream the
+// classification and the local means (box sums).  With a side stream the
 // classification runs there, beside the box sums (both only read the
 // frames), on half the blocks so that the two kernels share the SMs.
 flct_status enqueue_prepass(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaStream_t st, int* launches,
@@ -819,11 +790,11 @@ flct_status enqueue_prepass(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaS
         if (s == FLCT_OK) s = enqueue_box_rows(ctx, j, b, 0, j.nx, st, launches);
         if (s == FLCT_OK) s = enqueue_box_cols(ctx, j, b, 0, j.gi, st, launches);
     }
-    // device calls (with a side stream): the means launch as a programmatic
-    // dependent; the operation just before them on st is the wait for the
-    // classification, and k_means' grid_dep_wait (before any global access)
-    // keeps both the column sums and that join ordered, eager and captured
-    if (s == FLCT_OK) s = enqueue_means(ctx, j, b, (long)npx, st, launches, side != nullptr);
+    // device calls (with a side stream) launch the window kernel next as a
+    // programmatic dependent; the operation just before it on st is the wait
+    // for the classification, and the window kernels' grid_dep_wait (before
+    // any global access) keeps both the column sums and that join ordered,
+    // eager and captured
     return s;
 }
 
@@ -836,6 +807,7 @@ void make_wargs(const Job& j, const JobBufs& b, WinArgs* wa) {
     wa->s1 = b.s1;
     wa->s2 = b.s2;
     wa->means = b.means;
+    wa->mg = MeanGrid{j.gs, j.xo, j.yo, j.gj};
     wa->work = b.work;
     wa->nwork = (const int*)b.ctr;
     wa->nx = j.nx;
@@ -1128,7 +1100,7 @@ struct BatchPlan {
     std::vector<Job> jobs;
     std::vector<JobBufs> bufs;
     std::vector<BatchGroup> groups;
-    MultiSet m_abs, m_thr, m_cls, m_rows, m_cols, m_means, m_fit, m_fith, m_interp;
+    MultiSet m_abs, m_thr, m_cls, m_rows, m_cols, m_fit, m_fith, m_interp;
     WinSeg* segs = nullptr;  // device, group-major
     int* starts = nullptr;   // device, per group nseg + 1 entries
     int* seg_pair = nullptr; // device
@@ -1203,10 +1175,9 @@ flct_status plan_multi(flct_ctx* ctx, BatchPlan* bp) {
     std::vector<ThreshArgs> thr;
     std::vector<ClassifyArgs> cls;
     std::vector<BoxArgs> rows, cols;
-    std::vector<MeansArgs> means;
     std::vector<FitArgs> fit, fith;
     std::vector<InterpArgs> ia;
-    std::vector<long> babs, bthr, bcls, brows, bcols, bmeans, bfit, bfith, bia;
+    std::vector<long> babs, bthr, bcls, brows, bcols, bfit, bfith, bia;
     for (int k = 0; k < np; ++k) {
         const Job& j = bp->jobs[k];
         const JobBufs& b = bp->bufs[k];
@@ -1224,8 +1195,6 @@ flct_status plan_multi(flct_ctx* ctx, BatchPlan* bp) {
         brows.push_back((tasks + kBoxWarps - 1) / kBoxWarps);
         cols.push_back(box_cols_args(j, b, 0, j.gi, &threads));
         bcols.push_back((threads + 127) / 128);
-        means.push_back(means_args(j, b));
-        bmeans.push_back(std::max(1l, (npx + 255) / 256));
         const FitArgs fa = fit_args(j, b, Pub{});
         fit.push_back(fa);
         fith.push_back(fa);
@@ -1234,7 +1203,7 @@ flct_status plan_multi(flct_ctx* ctx, BatchPlan* bp) {
         ia.push_back(interp_args(j, b, 0, j.nx, Pub{}));
         bia.push_back(j.interp ? (long)((j.nx + kTileR - 1) / kTileR) * ((j.ny + kTileC - 1) / kTileC) : 0);
     }
-    for (const auto* v : {&babs, &bthr, &bcls, &brows, &bcols, &bmeans, &bfit, &bfith, &bia}) {
+    for (const auto* v : {&babs, &bthr, &bcls, &brows, &bcols, &bfit, &bfith, &bia}) {
         long tot = 0;
         for (long x : *v) tot += x;
         if (tot >= (1l << 31)) return fail(ctx, FLCT_ERR_UNSUPPORTED, "batch needs more than 2^31 blocks");
@@ -1244,7 +1213,6 @@ flct_status plan_multi(flct_ctx* ctx, BatchPlan* bp) {
     pack(cls, bcls, &bp->m_cls);
     pack(rows, brows, &bp->m_rows);
     pack(cols, bcols, &bp->m_cols);
-    pack(means, bmeans, &bp->m_means);
     pack(fit, bfit, &bp->m_fit);
     pack(fith, bfith, &bp->m_fith);
     pack(ia, bia, &bp->m_interp);
@@ -1306,7 +1274,7 @@ flct_status plan_batch(flct_ctx* ctx, int npairs, const flct_pair* pairs, BatchP
     }
     // workspace: per-pair arena slices, item-indexed arrays shared by all pairs
     struct Off {
-        size_t s1, s2, r1, r2, re1, re2, b1, b2, grid;
+        size_t s1, s2, r1, r2, re1, re2, grid;
         long long base;
     };
     std::vector<Off> off(npairs);
@@ -1326,8 +1294,6 @@ flct_status plan_batch(flct_ctx* ctx, int npairs, const flct_pair* pairs, BatchP
         o.r2 = take(z.r);
         o.re1 = take(z.re);
         o.re2 = take(z.re);
-        o.b1 = take(z.b);
-        o.b2 = take(z.b);
         o.grid = take(z.grid);
         o.base = items;
         items += (long long)bp->jobs[k].nx * bp->jobs[k].ny;
@@ -1340,7 +1306,7 @@ flct_status plan_batch(flct_ctx* ctx, int npairs, const flct_pair* pairs, BatchP
     const size_t first_bytes = align256((size_t)(ng + 1) * sizeof(int));
     ENSURE(ctx->bb_arena, arena);
     ENSURE(ctx->bb_work, (size_t)items * sizeof(int));
-    ENSURE(ctx->bb_means, (size_t)items * sizeof(float4));
+    ENSURE(ctx->bb_means, (size_t)items * sizeof(float4));  // a pair's grid has at most its pixels
     ENSURE(ctx->bb_peaks, (size_t)items * sizeof(PeakRec));
     bool any_hires = false;
     for (const auto& G : bp->groups) any_hires |= G.hires != 0;
@@ -1358,8 +1324,6 @@ flct_status plan_batch(flct_ctx* ctx, int npairs, const flct_pair* pairs, BatchP
         b.r2 = (BoxSum*)(A + o.r2);
         b.re1 = (int*)(A + o.re1);
         b.re2 = (int*)(A + o.re2);
-        b.b1 = (BoxSum*)(A + o.b1);
-        b.b2 = (BoxSum*)(A + o.b2);
         b.grid = (float2*)(A + o.grid);
         b.work = (int*)ctx->bb_work.p + o.base;
         b.means = (float4*)ctx->bb_means.p + o.base;
@@ -1382,6 +1346,7 @@ flct_status plan_batch(flct_ctx* ctx, int npairs, const flct_pair* pairs, BatchP
             sg.nx = bp->jobs[k].nx;
             sg.ny = bp->jobs[k].ny;
             sg.base = (int)off[k].base;
+            sg.mg = MeanGrid{bp->jobs[k].gs, bp->jobs[k].xo, bp->jobs[k].yo, bp->jobs[k].gj};
             hs[e] = sg;
             hpair[e] = k;
             ++e;
@@ -1421,7 +1386,7 @@ void group_wargs(flct_ctx* ctx, const BatchPlan& bp, int g, WinArgs* wa) {
 // The prepass of every pair of a batch as merged launches: one counter
 // memset, the relative thresholds, the classification (on a side stream,
 // beside the box sums: all three only read the frames), row and column box
-// sums, means, then the per-group prefix sums of the work counts.  With
+// sums with the means, then the per-group prefix sums of the work counts.  With
 // `side` null everything runs on bs.
 flct_status enqueue_batch_prepass(flct_ctx* ctx, BatchPlan& bp, cudaStream_t bs, cudaStream_t side, int* launches) {
     const int np = (int)bp.jobs.size();
@@ -1446,7 +1411,6 @@ flct_status enqueue_batch_prepass(flct_ctx* ctx, BatchPlan& bp, cudaStream_t bs,
         CK(cudaEventRecord(ctx->bev[1], side));
         CK(cudaStreamWaitEvent(bs, ctx->bev[1], 0));
     }
-    CK(launch_multi(ctx, k_means_multi, bp.m_means, 256, 0, bs, launches));
     k_batch_starts<<<(ng + 31) / 32, 32, 0, bs>>>((const unsigned char*)ctx->bb_ctr.p, bp.seg_pair, bp.first, ng,
                                                    bp.starts);
     ++*launches;
@@ -1594,6 +1558,9 @@ flct_status enqueue_device_tail(flct_ctx* ctx, const Job& j, const JobBufs& b, i
         s = enqueue_prepass(ctx, j, b, st, launches, ctx->prestream[0]);
         if (s != FLCT_OK) return s;
     }
+    // the last kernel copies the work count and status to page-locked
+    // memory; they are there once ev[3] completes
+    const Pub pub{(const unsigned*)b.ctr, ctx->hctr_dev};
     WinArgs wa;
     make_wargs(j, b, &wa);
     CK(stamp(ctx->ev[1]));
@@ -1603,9 +1570,6 @@ flct_status enqueue_device_tail(flct_ctx* ctx, const Job& j, const JobBufs& b, i
     if (s != FLCT_OK) return s;
     ++*launches;
     CK(stamp(ctx->ev[2]));
-    // the last kernel copies the work count and status to page-locked
-    // memory; they are there once ev[3] completes
-    const Pub pub{(const unsigned*)b.ctr, ctx->hctr_dev};
     s = enqueue_fit(ctx, j, b, st, launches, -1, j.interp ? Pub{} : pub, true);
     if (s != FLCT_OK) return s;
     CK(stamp(ctx->ev[7]));
@@ -1680,8 +1644,6 @@ flct_status banded_buffers(flct_ctx* ctx, const Job& j) {
     ENSURE(ctx->b_r2, z.r);
     ENSURE(ctx->b_re1, z.re);
     ENSURE(ctx->b_re2, z.re);
-    ENSURE(ctx->b_b1, z.b);
-    ENSURE(ctx->b_b2, z.b);
     ENSURE(ctx->b_means, z.means);
     ENSURE(ctx->b_peaks, z.peaks);
     if (z.peaks_h) ENSURE(ctx->b_peaks_h, z.peaks_h);
@@ -1711,19 +1673,17 @@ flct_status enqueue_banded(flct_ctx* ctx, const Job& j, const Bands& bd, int for
     base.peaks_h = (PeakRecH*)ctx->b_peaks_h.p;
     base.r1 = (BoxSum*)ctx->b_r1.p;
     base.r2 = (BoxSum*)ctx->b_r2.p;
-    base.b1 = (BoxSum*)ctx->b_b1.p;
-    base.b2 = (BoxSum*)ctx->b_b2.p;
     base.grid = (float2*)ctx->b_grid.p;
     base.re1 = (int*)ctx->b_re1.p;
     base.re2 = (int*)ctx->b_re2.p;
-    // band b's work items, means and peak records start at pixel R[b] * ny
-    // (a band has at most that many windows); its counters at ctr + 64 b
+    // band b's work items and peak records start at pixel R[b] * ny (a band
+    // has at most that many windows), its counters at ctr + 64 b; the means
+    // are one grid-indexed array, each band's column sums fill its grid rows
     JobBufs bb[flct_ctx::kMaxBands];
     for (int b = 0; b < nb; ++b) {
         bb[b] = base;
         const size_t off = (size_t)bd.R[b] * ny;
         bb[b].work = base.work + off;
-        bb[b].means = base.means + off;
         bb[b].peaks = base.peaks + off;
         bb[b].peaks_h = z.peaks_h ? base.peaks_h + off : nullptr;
         bb[b].ctr = (unsigned char*)ctx->b_ctr.p + 64 * b;
@@ -1768,32 +1728,26 @@ flct_status enqueue_banded(flct_ctx* ctx, const Job& j, const Bands& bd, int for
         CK(cudaEventRecord(ctx->hev[kK + b], pc));
         CK(cudaStreamWaitEvent(pb, ctx->hev[kR + b], 0));
         s = enqueue_box_cols(ctx, j, base, bd.Q[b], bd.Q[b + 1], pb, &launches);
-        // the band's means at the prepass priority too (on a band stream
-        // they waited behind the next chunks' prepass): they need its box
-        // sums and its complete work list (chunk b's classification)
-        CK(cudaStreamWaitEvent(pb, ctx->hev[kK + b], 0));
-        if (s == FLCT_OK) s = enqueue_means(ctx, j, bb[b], (long)(bd.Q[b + 1] - bd.Q[b]) * j.gj, pb, &launches);
         CK(cudaEventRecord(ctx->hev[kP + b], pb));
     }
     for (int b = 0; b < nb && s == FLCT_OK; ++b) {
         cudaStream_t sb = bs[b];
-        // the band's means (after its box sums and work list), and the
-        // float split of every row its windows read: chunks <= b
+        // the band's means (its column sums), its work list and the float
+        // split of every row its windows read (chunks <= b's classification)
         CK(cudaStreamWaitEvent(sb, ctx->hev[kP + b], 0));
         CK(cudaStreamWaitEvent(sb, ctx->hev[kK + b], 0));
         // the band's windows: at most its grid points
         const long items = (long)(bd.Q[b + 1] - bd.Q[b]) * j.gj;
+        // the band's last kernel copies its counters to page-locked memory
+        const Pub pub{(const unsigned*)bb[b].ctr, ctx->hctr_dev + 16 * b};
+        const bool interp = j.interp && bd.O[b + 1] > bd.O[b];
         WinArgs wb = wa;
-        wb.means = bb[b].means;
         wb.work = bb[b].work;
         wb.nwork = (const int*)bb[b].ctr;
         wb.peaks = bb[b].peaks;
         wb.peaks_h = j.p->hires ? bb[b].peaks_h : nullptr;
         s = launch_windows(ctx, form, j.we, j.n, wb, (unsigned*)(bb[b].ctr + 4), sb, grid_div, items);
         ++launches;
-        // the band's last kernel copies its counters to page-locked memory
-        const Pub pub{(const unsigned*)bb[b].ctr, ctx->hctr_dev + 16 * b};
-        const bool interp = j.interp && bd.O[b + 1] > bd.O[b];
         if (s == FLCT_OK) s = enqueue_fit(ctx, j, bb[b], sb, &launches, items, interp ? Pub{} : pub);
         if (s != FLCT_OK) break;
         CK(cudaEventRecord(ctx->hev[kF + b], sb));
@@ -2122,8 +2076,6 @@ flct_status flct_gpu_velocity_device(flct_ctx* ctx, const flct_params* p, const 
     ENSURE(ctx->b_r2, z.r);
     ENSURE(ctx->b_re1, z.re);
     ENSURE(ctx->b_re2, z.re);
-    ENSURE(ctx->b_b1, z.b);
-    ENSURE(ctx->b_b2, z.b);
     ENSURE(ctx->b_means, z.means);
     ENSURE(ctx->b_peaks, z.peaks);
     if (z.peaks_h) ENSURE(ctx->b_peaks_h, z.peaks_h);
@@ -2141,8 +2093,6 @@ flct_status flct_gpu_velocity_device(flct_ctx* ctx, const flct_params* p, const 
     b.r2 = (BoxSum*)ctx->b_r2.p;
     b.re1 = (int*)ctx->b_re1.p;
     b.re2 = (int*)ctx->b_re2.p;
-    b.b1 = (BoxSum*)ctx->b_b1.p;
-    b.b2 = (BoxSum*)ctx->b_b2.p;
     b.ctr = (unsigned char*)ctx->b_ctr.p;
     b.grid = (float2*)ctx->b_grid.p;
     unsigned* d_status = (unsigned*)(b.ctr + 4);

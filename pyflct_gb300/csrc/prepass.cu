@@ -5,8 +5,8 @@
 //                               float hi+lo split of both frames, and the
 //                               final values of pixels without a window
 //                               (flct.c:721-755, 918-930, 1125-1133)
-//   k_box_rows / k_box_cols     exact box sums for the local means
-//                               (flct.c:815-827, fixsum.cuh) as sliding
+//   k_box_rows / k_box_cols     the local means (flct.c:815-827) from
+//                               exact box sums (fixsum.cuh) as sliding
 //                               sums, at the boxes the skip grid needs
 //   k_interp_grid               skip-grid cubic-convolution interpolation
 //                               (flct.c:958-1120 with interpcc2d,
@@ -304,7 +304,10 @@ FLCT_MULTI_KERNEL(__launch_bounds__(kBoxWarps * 32), k_box_rows, BoxArgs)
 // kColLanes, and the lanes' partial sums meet by shuffles (integer sums:
 // the order does not matter).  The run's unit is the largest of the row
 // sums' units it reads.  A warp's loads cover 32 / kColLanes consecutive
-// columns of kColLanes rows, and each lane stores one word of the box sum.
+// columns of kColLanes rows.  Each box sum becomes the grid point's FP64
+// local mean, rounded once, and is stored as its float hi + lo split (the
+// form the window kernels subtract): lane 0 of the group writes this
+// frame's half of the grid point's float4.
 __device__ __forceinline__ void col_reduce(unsigned long long& lo, unsigned long long& hi,
                                            unsigned long long& cnt) {
 #pragma unroll
@@ -330,7 +333,8 @@ __device__ __forceinline__ void k_box_cols_body(const BoxArgs& a, const int vb, 
     const int img = lam >= a.gj, m = lam - img * a.gj;
     const BoxSum* __restrict__ v = (img ? a.rt2 : a.rt1) + m;  // row r at v[r * gj]
     const int* __restrict__ ve = (img ? a.re2 : a.re1) + m;
-    unsigned long long* __restrict__ o = reinterpret_cast<unsigned long long*>((img ? a.b2 : a.b1) + m);
+    // this line's half (hi, lo) of the grid points' float4 means
+    float2* __restrict__ o = reinterpret_cast<float2*>(a.means + m) + img;
     const size_t gj = (size_t)a.gj;
     const int q0 = a.q0 + run * kColRun, q1 = min(q0 + kColRun, a.q1);
     int t = box_start(a.xo + q0 * a.gs, a.nx, a.nsize);
@@ -350,9 +354,10 @@ __device__ __forceinline__ void k_box_cols_body(const BoxArgs& a, const int vb, 
     }
     col_reduce(lo, hi, cnt);
     for (int q = q0;;) {
-        if (act) {
-            const unsigned long long w = (p == 0) ? lo : (p == 1) ? hi : (p == 2) ? cnt : (unsigned long long)eb;
-            o[(size_t)q * gj * (sizeof(BoxSum) / 8) + p] = w;
+        if (act && p == 0) {
+            // the FP64 mean (flct.c:815-827), rounded once from the exact sum
+            const BoxSum bs{lo, hi, cnt, (unsigned long long)eb};
+            o[(size_t)q * gj * 2] = split_double_fast(__dmul_rn(fx_to_double(bs, eb), a.inv_n2));
         }
         if (++q >= q1) break;
         // slide down to the next grid row's box: rows [t, tn) leave, rows

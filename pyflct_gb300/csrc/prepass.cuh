@@ -35,9 +35,10 @@ constexpr int kColRun = 4;
 // Column pass: lanes that share one run's rows (a power of two <= 32)
 constexpr int kColLanes = 4;
 
-// Local-mean box sums for the boxes the grid needs, exact (fixsum.cuh).
-// Grid point (q, m) is pixel (xo + q gs, yo + m gs) (gs = 1, xo = yo = 0
-// without -s); its box starts at (box_start(xo + q gs), box_start(yo + m gs)).
+// Local means for the boxes the grid needs, from exact box sums
+// (fixsum.cuh).  Grid point (q, m) is pixel (xo + q gs, yo + m gs) (gs = 1,
+// xo = yo = 0 without -s); its box starts at (box_start(xo + q gs),
+// box_start(yo + m gs)).
 struct BoxArgs {
     const double* f1;
     const double* f2;
@@ -46,7 +47,8 @@ struct BoxArgs {
     int pass_r;               // row pass: grid columns per warp pass
     BoxSum *rt1, *rt2;        // row sums [nx][gj]
     int *re1, *re2;           // their exponents, compact [nx][gj]
-    BoxSum *b1, *b2;          // box sums [gi][gj]
+    float4* means;            // local means [gi][gj]: (f1 hi, f1 lo, f2 hi, f2 lo)
+    double inv_n2;            // 1 / n^2
     int r0, r1;               // frame rows of the row pass
     int q0, q1;               // grid rows of the column pass
 };

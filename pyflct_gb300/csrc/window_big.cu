@@ -98,6 +98,8 @@ __global__ void __launch_bounds__(kBigThreads) k_window_big(BigArgs a) {
             const float2* f1s = a.s1;
             const float2* f2s = a.s2;
             int nx = a.nx, ny = a.ny;
+            const float4* mp = a.means;
+            MeanGrid mg = a.mg;
             if (a.nseg > 0) {
                 const int k = seg_find(a.seg_start, a.nseg, gi);
                 const WinSeg sg = a.segs[k];
@@ -105,6 +107,8 @@ __global__ void __launch_bounds__(kBigThreads) k_window_big(BigArgs a) {
                 f2s = sg.s2;
                 nx = sg.nx;
                 ny = sg.ny;
+                if (mp) mp += sg.base;
+                mg = sg.mg;
                 gi = sg.base + (gi - __ldg(a.seg_start + k));
             }
             const int pix = a.work[gi];
@@ -128,7 +132,7 @@ __global__ void __launch_bounds__(kBigThreads) k_window_big(BigArgs a) {
             s_item[5] = ny;
             s_src[0] = f1s + (size_t)imin * ny + jmin;
             s_src[1] = f2s + (size_t)imin * ny + jmin;
-            *s_mean = a.means ? a.means[gi] : make_float4(0.f, 0.f, 0.f, 0.f);
+            *s_mean = (mp && !a.direct) ? mp[mean_slot(mg, ic, jc)] : make_float4(0.f, 0.f, 0.f, 0.f);
             s_max[0] = 0u;
             s_max[1] = 0u;
             *s_key = 0ull;

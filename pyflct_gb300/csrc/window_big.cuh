@@ -11,7 +11,8 @@ constexpr int kMaxBigBox = 128;  // largest box side of the big-box kernel
 struct BigArgs {
     const float2* s1;     // f1 split (hi, lo) [nx*ny]
     const float2* s2;
-    const float4* means;  // per work item, or null: zero means
+    const float4* means;  // per grid point at mean_slot(mg, i, j), or null: zero means
+    MeanGrid mg;
     const int* work;
     const int* nwork;
     int nx, ny, nsize, n;

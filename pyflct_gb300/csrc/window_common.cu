@@ -1,74 +1,7 @@
-// window_common.cu -- k_means and k_fit (see window_common.cuh).
+// window_common.cu -- k_fit and k_fit_hires (see window_common.cuh).
 #include "window_common.cuh"
 
 namespace flct {
-
-__device__ __forceinline__ double dm(double a, double b) { return __dmul_rn(a, b); }
-__device__ __forceinline__ double da(double a, double b) { return __dadd_rn(a, b); }
-__device__ __forceinline__ double ds(double a, double b) { return __dsub_rn(a, b); }
-
-__device__ __forceinline__ void k_means_body(const MeansArgs& a, const int vb, const int vg) {
-    grid_dep_wait();
-    const int nw = *a.nwork;
-    for (int w = vb * blockDim.x + threadIdx.x; w < nw; w += vg * blockDim.x) {
-        const int pix = a.work[w];
-        const int i = pix / a.ny, j = pix - (pix / a.ny) * a.ny;
-        const size_t b = (size_t)((i - a.xo) / a.gs) * a.gj + (j - a.yo) / a.gs;
-        const BoxSum s1 = a.bs1[b], s2 = a.bs2[b];
-        const float2 m1 = split_double_fast(dm(fx_to_double(s1, (int)s1.e), a.inv_n2));
-        const float2 m2 = split_double_fast(dm(fx_to_double(s2, (int)s2.e), a.inv_n2));
-        a.means[w] = make_float4(m1.x, m1.y, m2.x, m2.y);
-    }
-}
-FLCT_MULTI_KERNEL(, k_means, MeansArgs)
-
-// Shifts of work item w to velocity, mask and the skip-grid copy
-// (flct.c:901-942, 1125-1133), or to the raw-shift outputs.
-__device__ __forceinline__ void store_shift(const FitArgs& a, int w, double shx, double shy) {
-    if (a.shx) {
-        a.shx[w] = shx;
-        a.shy[w] = shy;
-    }
-    if (a.vx) {
-        const int pix = a.work[w];
-        const int i = pix / a.ny, j = pix - (pix / a.ny) * a.ny;
-        // transposed storage: vx from the fast-axis shift (flct.c:901-905),
-        // scaled by deltas / deltat in one product
-        double vxx = dm(shy, a.vscale);
-        double vyy = dm(shx, a.vscale);
-        double vmm = 1.;
-        if (a.grid) {
-            const int ic = (i - a.xoff) / a.skip, jc = (j - a.yoff) / a.skip;
-            a.grid[(size_t)ic * a.jcnt + jc] = make_float2(split_double_fast(vxx).x, split_double_fast(vyy).x);
-        }
-        // xmiss tests on the bit patterns (xmiss is a normal number)
-        const long long xm = __double_as_longlong(kXmiss);
-        if (__double_as_longlong(vxx) == xm) {
-            vmm = 0.;
-            vxx = 0.;
-        }
-        if (__double_as_longlong(vyy) == xm) vyy = 0.;
-        a.vx[pix] = vxx;
-        a.vy[pix] = vyy;
-        a.vm[pix] = vmm;
-    }
-}
-
-// The 3x3 Taylor fit (flct.c:1536-1553, 1607-1630) of v[3p+q] = f at
-// (peak-1+p, peak-1+q), in the reference's operation order without FMA
-// contraction, except that both shifts multiply by one reciprocal of the
-// determinant (one FP64 division instead of two).
-__device__ __forceinline__ void fit3x3(const double* v, double* sx, double* sy) {
-    const double fx = dm(0.5, ds(v[7], v[1]));
-    const double fy = dm(0.5, ds(v[5], v[3]));
-    const double fxx = ds(da(v[7], v[1]), dm(2., v[4]));
-    const double fyy = ds(da(v[5], v[3]), dm(2., v[4]));
-    const double fxy = dm(0.25, ds(ds(da(v[8], v[0]), v[6]), v[2]));
-    const double den = ds(dm(fxy, fxy), dm(fxx, fyy));
-    const double inv = 1.0 / den;  // one division for both shifts
-    *sx = dm(ds(dm(fyy, fx), dm(fy, fxy)), inv);
-    *sy = dm(ds(dm(fxx, fy), dm(fx, fxy)), inv);
-}
 
 // Work items go to warps in 32-item chunks dealt round the blocks (chunk c
 // to block c mod gridDim), so every SM gets about the same number of fits:
@@ -78,21 +11,11 @@ __device__ __forceinline__ void k_fit_body(const FitArgs& a, const int vb, const
     grid_dep_wait();
     publish_counters(a.pub_src, a.pub_dst);
     const int nw = *a.nwork;
-    const int half = a.n / 2, half1 = (a.n1 ? a.n1 : a.n) / 2;
     const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
     for (long c = vb + (long)vg * (threadIdx.x >> 5); c * 32 < nw; c += (long)vg * wpb) {
         const int w = (int)(c * 32) + lane;
         if (w >= nw) continue;
-        const PeakRec r = a.peaks[w];
-        const int I = meta_I(r.meta), J = meta_J(r.meta);
-        double sx = 0., sy = 0.;
-        if (meta_flag(r.meta)) {
-            double v[9];
-#pragma unroll
-            for (int k = 0; k < 9; ++k) v[k] = f2d(r.v[k]);
-            fit3x3(v, &sx, &sy);
-        }
-        store_shift(a, w, da((double)(I - half), sx), da((double)(J - half1), sy));
+        fit_item(a, w, a.peaks[w]);
     }
 }
 FLCT_MULTI_KERNEL(, k_fit, FitArgs)

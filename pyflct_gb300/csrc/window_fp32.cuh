@@ -6,9 +6,12 @@
 // local means, applies the Gaussian centred on the pixel, transforms both
 // sub-images, forms conj(A)*B (times the squared k-space filter for -k),
 // transforms back, takes |c| in the half-shifted frame and finds the first
-// strict maximum.  The FP64 parts run in one-window-per-lane passes around
-// it (window_common.cuh): k_means before, k_fit (3x3 Taylor fit, velocity,
-// mask) after; this kernel does no FP64 arithmetic.
+// strict maximum.  The FP64 parts run with one window per lane
+// (window_common.cuh): the local means in the box-sum column pass before,
+// and k_fit (3x3 Taylor fit, velocity, mask) after; this kernel does no
+// FP64 arithmetic.  (The fit run inside this kernel instead, one warp
+// fitting each 32 finished windows of its CTA, made the kernel 25 us slower
+// at 1024^2, sigma 8, -s 4i than k_fit takes on its own: measured.)
 //
 // Layout: a "team" of n threads owns one window; a CTA runs TEAMS teams
 // (teams that tile whole warps synchronise per warp).  The two real
@@ -35,7 +38,8 @@ namespace flct {
 struct WinArgs {
     const float2* s1;     // f1 split (hi, lo) [nx*ny]
     const float2* s2;     // f2 split
-    const float4* means;  // per work item (m1 hi, m1 lo, m2 hi, m2 lo), or null: zero means
+    const float4* means;  // per grid point at mean_slot(mg, i, j), or null: zero means
+    MeanGrid mg;
     const int* work;      // pixel indices i*ny + j
     const int* nwork;     // number of work items (device)
     int nx, ny, nsize;
@@ -114,10 +118,12 @@ k_window_fp32(WinArgs a) {
     for (int base = blockIdx.x * TEAMS; base < nwork; base += gridDim.x * TEAMS) {
         const int w = base + team;
         const bool valid = w < nwork;
-        int gi = valid ? w : base;  // item index into work / means / peaks
+        int gi = valid ? w : base;  // item index into work / peaks
         const float2* f1s = a.s1;
         const float2* f2s = a.s2;
         int nx = a.nx, ny = a.ny;
+        const float4* mp = a.means;
+        MeanGrid mg = a.mg;
         if (a.nseg > 0) {
             const int k = seg_find(a.seg_start, a.nseg, gi);
             const WinSeg sg = a.segs[k];
@@ -125,6 +131,8 @@ k_window_fp32(WinArgs a) {
             f2s = sg.s2;
             nx = sg.nx;
             ny = sg.ny;
+            if (mp) mp += sg.base;
+            mg = sg.mg;
             gi = sg.base + (gi - __ldg(a.seg_start + k));
         }
         const int pix = a.work[gi];
@@ -144,7 +152,8 @@ k_window_fp32(WinArgs a) {
         // windowed, mean-subtracted column jj = ln of both frames: z = g1 + i g2
         float2 x[N];
         {
-            const float4 mm = a.means ? __ldg(a.means + gi) : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float4 mm =
+                (mp && !a.direct) ? __ldg(mp + mean_slot(mg, i, j)) : make_float4(0.f, 0.f, 0.f, 0.f);
             const float2 m1 = make_float2(mm.x, mm.y), m2 = make_float2(mm.z, mm.w);
             const float wc = s_g[ln + jmin - j + N];
             const float2* p1 = f1s + (size_t)imin * ny + jmin + ln;

@@ -65,7 +65,8 @@ namespace flct {
 struct TcArgs {
     const float2* s1;
     const float2* s2;
-    const float4* means;  // per work item, or null (direct windows)
+    const float4* means;  // per grid point at mean_slot(mg, i, j), or null (direct windows)
+    MeanGrid mg;
     const int* work;
     const int* nwork;
     int nx, ny, nsize;
@@ -351,6 +352,8 @@ __global__ void __launch_bounds__(256, TcCfg<N>::MINB) k_window_tc(TcArgs a) {
         f.f2 = a.s2;
         f.nx = a.nx;
         f.ny = a.ny;
+        const float4* mp = a.means;
+        MeanGrid mg = a.mg;
         if (a.nseg > 0) {
             const int k = seg_find(a.seg_start, a.nseg, w);
             const WinSeg sg = a.segs[k];
@@ -358,11 +361,18 @@ __global__ void __launch_bounds__(256, TcCfg<N>::MINB) k_window_tc(TcArgs a) {
             f.f2 = sg.s2;
             f.nx = sg.nx;
             f.ny = sg.ny;
+            if (mp) mp += sg.base;
+            mg = sg.mg;
             w = sg.base + (w - __ldg(a.seg_start + k));
         }
         f.gi = w;
         f.pix = a.work[w];
-        f.mean = a.means ? a.means[w] : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (mp && !a.direct) {
+            const int i = f.pix / f.ny;
+            f.mean = mp[mean_slot(mg, i, f.pix - i * f.ny)];
+        } else {
+            f.mean = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
         return f;
     };
     Fetch nxt{};

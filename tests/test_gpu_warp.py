@@ -2,8 +2,10 @@
 against the FP64 oracle and the reference's golden outputs.
 
 The GPU evaluates the transforms in FP32 with FP64 phase bases and FP64
-circulant/twiddle tables; the tolerance is max |d| <= 2e-5 * max |image|
-(the golden files themselves are float32-rounded).
+circulant/twiddle tables.  Tolerances, relative to max |image|: warp_frac2d
+1.5e-6 (measured up to 9.3e-7 at 512^2), shift_frac2d 4e-6 (measured up to
+1.9e-6 at 512^2); against the reference's golden files, which are
+float32-rounded, 2e-6.
 """
 import numpy as np
 import pytest
@@ -12,7 +14,9 @@ import pyoracle as po
 from _golden import load
 
 pytestmark = pytest.mark.gpu
-REL = 2e-5
+REL = 2e-6        # against the float32-rounded golden files
+REL_WARP = 1.5e-6
+REL_SHIFT = 4e-6
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -22,8 +26,10 @@ def gpu():
     return _lib.context(0)
 
 
-def close(a, b, scale):
-    return np.abs(a - b).max() <= REL * scale
+def close(a, b, scale, rel=REL):
+    err = np.abs(a - b).max() / scale
+    print(f"max |d| / max |image| = {err:.3e} (bound {rel:.1e})")
+    return err <= rel
 
 
 def test_golden_warp_and_shift():
@@ -47,7 +53,7 @@ def test_shift_sizes(shape, transp):
     dx, dy = rng.uniform(-6, 6, 2)
     got = shift_frac2d(img, dx, dy, transp)
     ref = po.shift_frac2d(img, dx, dy, transp)
-    assert close(got, ref, np.abs(img).max())
+    assert close(got, ref, np.abs(img).max(), REL_SHIFT)
 
 
 @pytest.mark.parametrize("shape", [(37, 53), (64, 48), (20, 31), (9, 8)])
@@ -60,7 +66,7 @@ def test_warp_sizes(shape, transp):
     dfast, dslow = synth.smooth_shift(shape, rng, rms=1.5)
     got = warp_frac2d(img, dfast, dslow, transp)
     ref = po.warp_frac2d(img, dfast, dslow, transp)
-    assert close(got, ref, np.abs(img).max())
+    assert close(got, ref, np.abs(img).max(), REL_WARP)
 
 
 def test_warp_dispatch_and_constant_field():
@@ -69,7 +75,7 @@ def test_warp_dispatch_and_constant_field():
     img = rng.standard_normal((24, 30))
     a = warp(img, np.full(img.shape, 0.7), np.full(img.shape, -1.2))
     b = warp(img, 0.7, -1.2)
-    assert np.abs(a - b).max() <= REL * np.abs(img).max()
+    assert np.abs(a - b).max() <= REL_SHIFT * np.abs(img).max()
     with pytest.raises(FlctError) as e:
         warp(img, np.zeros((3, 3)), np.zeros((3, 3)))
     assert e.value.code == 11
@@ -82,8 +88,8 @@ def test_warp_crop_256_and_shift_512():
     rng = np.random.default_rng(20265)
     img = synth.kfield((512, 512), rng)
     got = shift_frac2d(img, 0.37, -2.6)
-    assert close(got, po.shift_frac2d(img, 0.37, -2.6), np.abs(img).max())
+    assert close(got, po.shift_frac2d(img, 0.37, -2.6), np.abs(img).max(), REL_SHIFT)
     crop = img[100:356, 40:296]
     dfast, dslow = synth.smooth_shift(crop.shape, rng, rms=0.3)
     got = warp_frac2d(crop, dfast, dslow)
-    assert close(got, po.warp_frac2d(crop, dfast, dslow), np.abs(crop).max())
+    assert close(got, po.warp_frac2d(crop, dfast, dslow), np.abs(crop).max(), REL_WARP)
