@@ -2,7 +2,7 @@
 //
 // A length-L complex transform of an array held in a thread's registers,
 // fully unrolled at compile time: decimation in time, L = R * M with R in
-// {4, 2, 3, 5, 7, ...} (a prime R > 5 uses a direct R-point DFT), so every
+// {4, 2, 3, 5, 7, ...} (a prime R > 5 uses the symmetric-pair DFT), so every
 // box size the sliding window can take (n = 2*nsize, a multiple of 4) has a
 // kernel.  Input n sits in register dit_in<L>(n) (a digit reversal), output
 // frequency k in register k; every index is a compile-time constant, so the
@@ -197,22 +197,37 @@ FLCT_HD void small_dft(float2* t) {
         t[2] = cadd(t2, u2);
         t[3] = csub(t2, u2);
     } else {
-        // direct R-point DFT for a prime R
-        float2 o[R];
-        sfor<0, R>([&](auto sc) {
-            constexpr int s = decltype(sc)::value;
-            float2 acc = t[0];
-            sfor<1, R>([&](auto rc) {
-                constexpr int r = decltype(rc)::value;
-                float2 v = twmul<DIR, (long)r * s, R>(t[r]);
-                acc = cadd(acc, v);
+        // odd prime R by symmetric pairs: with a_k = t[k] + t[R-k] and
+        // b_k = t[k] - t[R-k] (k = 1..H, H = (R-1)/2),
+        //   X[s]   = t[0] + sum_k a_k cos(2 pi k s / R) + DIR i sum_k b_k sin(2 pi k s / R)
+        //   X[R-s] = the same with - DIR i,
+        // real coefficients on packed FMAs: 2H^2 + O(H) operations instead
+        // of the (R-1)^2 complex products of a direct DFT
+        static_assert(R % 2 == 1, "symmetric DFT needs an odd length");
+        constexpr int H = (R - 1) / 2;
+        float2 a[H + 1], b[H + 1];
+        sfor<1, H + 1>([&](auto kc) {
+            constexpr int k = decltype(kc)::value;
+            a[k] = cadd(t[k], t[R - k]);
+            b[k] = csub(t[k], t[R - k]);
+        });
+        const float2 x0 = t[0];
+        float2 sum = x0;
+        sfor<1, H + 1>([&](auto kc) { sum = cadd(sum, a[decltype(kc)::value]); });
+        sfor<1, H + 1>([&](auto sc) {
+            constexpr int sidx = decltype(sc)::value;
+            float2 tr = x0, ui = make_float2(0.f, 0.f);
+            sfor<1, H + 1>([&](auto kc) {
+                constexpr int k = decltype(kc)::value;
+                constexpr CS w = ct_cossin((long)k * sidx, R);
+                tr = cfma(a[k], (float)w.c, tr);
+                ui = cfma(b[k], (float)w.s, ui);
             });
-            o[s] = acc;
+            const float2 v = mul_i<DIR>(ui);
+            t[sidx] = cadd_s(tr, v);
+            t[R - sidx] = csub_s(tr, v);
         });
-        sfor<0, R>([&](auto sc) {
-            constexpr int s = decltype(sc)::value;
-            t[s] = o[s];
-        });
+        t[0] = sum;
     }
 }
 

@@ -58,15 +58,18 @@ struct WinArgs {
 
 template <int N>
 struct WinShape {
-    static constexpr int TEAMS = (N <= 8) ? (128 / N) : (N <= 20) ? 8 : (N <= 40) ? 4 : 2;
+    static constexpr int TEAMS = (N <= 8) ? (128 / N) : (N <= 20 || N == 32) ? 8 : (N <= 40) ? 4 : 2;
     static constexpr int THREADS = N * TEAMS;
     static constexpr int BUF = N * (N + 1);  // float2 per team
     static constexpr size_t tw_off = 32 * TEAMS + ((3 * N + 1) * 4 + 15) / 16 * 16;
     static constexpr size_t head = tw_off + (size_t)N * 8;
     static constexpr size_t smem = head + (size_t)TEAMS * BUF * 8;  // |c| reuses the buffer
     // CTAs per SM the register allocation is held to (0: no constraint).
-    // Box 32: 5 CTAs at 96 registers beat 4 at 119 (measured).
-    static constexpr int MINB = (N == 32) ? 5 : 0;
+    // Box 32: 2 CTAs of 8 teams at 128 registers, no spills, beat 5 CTAs of
+    // 4 teams at 96 registers with 12 bytes spilled (175.8 against 181.9 us
+    // for 65,536 windows; 4 CTAs of 4 teams at 128 registers: 179.9 us;
+    // measured).
+    static constexpr int MINB = (N == 32) ? 2 : 0;
 };
 
 template <int N>

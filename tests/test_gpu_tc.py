@@ -5,7 +5,9 @@ at every box size the library compiles (n = 4..64, multiples of 4).
 Tolerances: the split-FP16 form is held to the same bar as the FP32 form
 (max |dv| <= 1e-3 px/frame, bit-exact mask, integer peaks identical except at
 documented ties).  The BF16 hi+lo form keeps ~16 significant bits per
-operand; it is held to 1e-2 px and its measured error is reported.
+operand; it is held to 1e-2 px and its measured error is reported.  The
+every-box and every-sigma cases run the FP32 form too (its radix-4/2/3/5
+and odd-prime register transforms differ by box size).
 """
 import numpy as np
 import pytest
@@ -15,7 +17,7 @@ from _compare import TIE_REL, compare
 from _golden import parse_cli_args, window_cases
 
 pytestmark = pytest.mark.gpu
-TOL = {"tc_fp16": 1e-3, "tc_bf16": 1e-2}
+TOL = {"fp32": 1e-3, "tc_fp16": 1e-3, "tc_bf16": 1e-2}
 BOXES = list(range(4, 68, 4))
 # sigma -> box side through flct.c:567-580 (frames large enough not to shrink it)
 SIGMA_BOX = {1: 4, 2: 8, 3: 12, 4: 16, 5: 20, 6: 24, 7: 28, 8: 32, 9: 36, 10: 40, 11: 44, 12: 48,
@@ -77,7 +79,7 @@ def test_golden_windows(form):
     assert {12, 20, 32, 48} <= seen
 
 
-@pytest.mark.parametrize("form", ["tc_fp16", "tc_bf16"])
+@pytest.mark.parametrize("form", ["fp32", "tc_fp16", "tc_bf16"])
 @pytest.mark.parametrize("n", BOXES)
 def test_direct_windows_every_box(form, n):
     """Random windows at every box size, with and without the -k filter."""
@@ -112,7 +114,7 @@ def test_random_fields_every_sigma(sigma, shape, extra):
     kw = parse_cli_args(args)
     assert 2 * po.derive(f1, f2, **kw).nsize == SIGMA_BOX[int(sigma)]
     ref = po.velocity(f1, f2, **kw)
-    for form in ("tc_fp16", "tc_bf16"):
+    for form in ("fp32", "tc_fp16", "tc_bf16"):
         rep = compare(f1, f2, run(f1, f2, form, sigma=sigma, **extra), ref, kw, tol=TOL[form])
         print(form, sigma, extra, rep)
 
