@@ -36,14 +36,20 @@ constexpr double kTol = 1e-2;  // flct.c:278
 
 // ------------------------------------------------------ window kernels --
 
+// The FP32 form per box size: launchers, occupancy and windows per CTA
+// iteration of its two launch shapes (WinShape<N, V>, V = 0 default).
 struct WinEntry {
     int n;
-    cudaError_t (*launch)(const WinArgs&, int, cudaStream_t, bool);
-    int (*bps)();
-    int teams;  // windows per CTA iteration
+    cudaError_t (*launch[2])(const WinArgs&, int, cudaStream_t, bool);
+    int (*bps[2])();
+    int teams[2];
 };
 
-#define FLCT_WIN(N) {N, &launch_window_fp32<N>, &window_fp32_blocks_per_sm<N>, WinShape<N>::TEAMS}
+#define FLCT_WIN(N)                                                                  \
+    {N,                                                                              \
+     {&launch_window_fp32<N, 0>, &launch_window_fp32<N, 1>},                         \
+     {&window_fp32_blocks_per_sm<N, 0>, &window_fp32_blocks_per_sm<N, 1>},           \
+     {WinShape<N, 0>::TEAMS, WinShape<N, 1>::TEAMS}}
 const WinEntry kWin[] = {FLCT_WIN(4),  FLCT_WIN(8),  FLCT_WIN(12), FLCT_WIN(16),
                          FLCT_WIN(20), FLCT_WIN(24), FLCT_WIN(28), FLCT_WIN(32),
                          FLCT_WIN(36), FLCT_WIN(40), FLCT_WIN(44), FLCT_WIN(48),
@@ -123,7 +129,7 @@ struct flct_ctx {
                 &bb_work, &bb_means, &bb_peaks, &bb_ctr, &bb_meta, &b_peaks_h, &bb_peaks_h, &b_re1, &b_re2,
                 &bb_multi};
     }
-    int bps[sizeof(kWin) / sizeof(kWin[0])] = {0};
+    int bps[sizeof(kWin) / sizeof(kWin[0])][2] = {};
     int bps_tc[kNumTc][2] = {};
     int bps_big = 0;
     Buf b_tc;              // tensor-core DFT matrices of every box size and split type
@@ -135,6 +141,7 @@ struct flct_ctx {
     struct Tune {
         int form = FLCT_FORM_FP32;
         int grid_div = 1;        // CTAs per SM = occupancy limit / grid_div
+        int variant = 0;         // FP32 form: launch shape WinShape<n, variant>
         float ns_per_window = 0.f;
     };
     std::map<int, Tune> tune;
@@ -296,11 +303,18 @@ int win_index(int n) {
     return -1;
 }
 
-int win_grid(flct_ctx* ctx, int n) {
+// How a window launch is shaped: CTAs per SM = occupancy limit / grid_div,
+// and for the FP32 form the launch shape WinShape<n, variant>.
+struct WinCfg {
+    int grid_div = 1;
+    int variant = 0;
+};
+
+int win_grid(flct_ctx* ctx, int n, int v = 0) {
     int k = win_index(n);
     if (k < 0) return 0;
-    if (ctx->bps[k] == 0) ctx->bps[k] = std::max(1, kWin[k].bps());
-    return ctx->nsm * ctx->bps[k];
+    if (ctx->bps[k][v] == 0) ctx->bps[k][v] = std::max(1, kWin[k].bps[v]());
+    return ctx->nsm * ctx->bps[k][v];
 }
 
 // The tensor-core form's constant matrices, built once per context in FP64
@@ -354,8 +368,8 @@ flct_status pick_form(flct_ctx* ctx, int requested, int n, int* form) {
 // instead of a persistent grid, so that CTAs retire often and kernels of
 // higher-priority streams get SMs in between (banded host calls).
 flct_status launch_windows(flct_ctx* ctx, int form, const WinEntry* we, int n, const WinArgs& wa, unsigned* status,
-                           cudaStream_t st, int grid_div = 1, long max_items = -1, bool pdl = false) {
-    if (grid_div < 1) grid_div = 1;
+                           cudaStream_t st, WinCfg cfg = {}, long max_items = -1, bool pdl = false) {
+    const int grid_div = std::max(1, cfg.grid_div), v = cfg.variant ? 1 : 0;
     if (n > kMaxBox) {
         // boxes above 64: the big-box FP32 kernel, one window per CTA
         if (form != FLCT_FORM_FP32 || n > kMaxBigBox)
@@ -401,9 +415,9 @@ flct_status launch_windows(flct_ctx* ctx, int form, const WinEntry* we, int n, c
         return FLCT_OK;
     }
     if (form == FLCT_FORM_FP32) {
-        int grid = std::max(ctx->nsm, win_grid(ctx, n) / grid_div);
-        if (max_items >= 0) grid = (int)std::max<long>(1, (max_items + we->teams - 1) / we->teams);
-        CK(we->launch(wa, grid, st, pdl));
+        int grid = std::max(ctx->nsm, win_grid(ctx, n, v) / grid_div);
+        if (max_items >= 0) grid = (int)std::max<long>(1, (max_items + we->teams[v] - 1) / we->teams[v]);
+        CK(we->launch[v](wa, grid, st, pdl));
         return FLCT_OK;
     }
     flct_status s = ensure_tc_tables(ctx);
@@ -449,8 +463,9 @@ void tune_save(flct_ctx* ctx) {
     fprintf(f, "{\"device\": \"%s\", \"entries\": [\n", ctx->device_name.c_str());
     size_t k = 0;
     for (const auto& e : ctx->tune) {
-        fprintf(f, "  {\"box\": %d, \"form\": %d, \"grid_div\": %d, \"ns_per_window\": %.4f}%s\n", e.first,
-                e.second.form, e.second.grid_div, e.second.ns_per_window, (++k < ctx->tune.size()) ? "," : "");
+        fprintf(f, "  {\"box\": %d, \"form\": %d, \"grid_div\": %d, \"ns_per_window\": %.4f, \"variant\": %d}%s\n",
+                e.first, e.second.form, e.second.grid_div, e.second.ns_per_window, e.second.variant,
+                (++k < ctx->tune.size()) ? "," : "");
     }
     fprintf(f, "]}\n");
     fclose(f);
@@ -476,6 +491,10 @@ void tune_load(flct_ctx* ctx) {
             t.form = form;
             t.grid_div = gd;
             t.ns_per_window = ns;
+            // entries written before the shape variants existed have none: 0
+            int v = 0;
+            const char* qv = strstr(q, "\"variant\"");
+            if (qv && sscanf(qv, "\"variant\": %d", &v) == 1 && (v == 0 || v == 1)) t.variant = v;
             ctx->tune[box] = t;
         }
     }
@@ -488,15 +507,18 @@ void tune_load(flct_ctx* ctx) {
 flct_status tune_windows(flct_ctx* ctx, const WinEntry* we, int n, const WinArgs& wa, unsigned* status,
                          const int* d_nwork, cudaStream_t st) {
     struct Cand {
-        int form, grid_div;
+        int form;
+        WinCfg cfg;
     };
     // FLCT_FORM_AUTO chooses among the forms whose error is FP32-like: the
-    // radix form and the split-FP16 tensor-core form (the BF16 split keeps
-    // fewer mantissa bits and is only used when asked for)
-    std::vector<Cand> cands = {{FLCT_FORM_FP32, 1}, {FLCT_FORM_FP32, 2}};
+    // radix form (both launch shapes: windows per CTA) and the split-FP16
+    // tensor-core form (the BF16 split keeps fewer mantissa bits and is only
+    // used when asked for), each at its occupancy limit or half of it
+    std::vector<Cand> cands = {{FLCT_FORM_FP32, {1, 0}}, {FLCT_FORM_FP32, {2, 0}}, {FLCT_FORM_FP32, {1, 1}},
+                               {FLCT_FORM_FP32, {2, 1}}};
     if (tc_index(n) >= 0) {
-        cands.push_back({FLCT_FORM_TC_FP16, 1});
-        if (tc_bps(ctx, tc_index(n), 0) > 1) cands.push_back({FLCT_FORM_TC_FP16, 2});
+        cands.push_back({FLCT_FORM_TC_FP16, {1, 0}});
+        if (tc_bps(ctx, tc_index(n), 0) > 1) cands.push_back({FLCT_FORM_TC_FP16, {2, 0}});
     }
     int nwork = 0;
     CK(cudaMemcpyAsync(&nwork, d_nwork, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -508,7 +530,7 @@ flct_status tune_windows(flct_ctx* ctx, const WinEntry* we, int n, const WinArgs
         float ms = 1e30f;
         for (int rep = 0; rep < 3; ++rep) {
             CK(cudaEventRecord(ctx->tev[0], st));
-            flct_status s = launch_windows(ctx, c.form, we, n, wa, status, st, c.grid_div);
+            flct_status s = launch_windows(ctx, c.form, we, n, wa, status, st, c.cfg);
             if (s != FLCT_OK) return s;
             CK(cudaEventRecord(ctx->tev[1], st));
             CK(cudaEventSynchronize(ctx->tev[1]));
@@ -517,7 +539,8 @@ flct_status tune_windows(flct_ctx* ctx, const WinEntry* we, int n, const WinArgs
         if (ms < best) {
             best = ms;
             bt.form = c.form;
-            bt.grid_div = c.grid_div;
+            bt.grid_div = c.cfg.grid_div;
+            bt.variant = c.cfg.variant;
         }
     }
     bt.ns_per_window = best * 1e6f / (float)nwork;
@@ -907,7 +930,8 @@ flct_status prime_form(flct_ctx* ctx, int form, int n) {
         return FLCT_OK;
     }
     if (form == FLCT_FORM_FP32) {
-        if (win_grid(ctx, n) <= 0) return fail(ctx, FLCT_ERR_CUDA, "no occupancy for the box-%d window kernel", n);
+        if (win_grid(ctx, n, 0) <= 0 || win_grid(ctx, n, 1) <= 0)
+            return fail(ctx, FLCT_ERR_CUDA, "no occupancy for the box-%d window kernel", n);
         return FLCT_OK;
     }
     flct_status s = ensure_tc_tables(ctx);
@@ -918,10 +942,10 @@ flct_status prime_form(flct_ctx* ctx, int form, int n) {
     return FLCT_OK;
 }
 
-// Form and CTAs-per-SM divisor for box size n: the request, or for
-// FLCT_FORM_AUTO the autotuner's measured choice.
-void resolved_config(flct_ctx* ctx, int requested, int n, int* form, int* grid_div) {
-    *grid_div = 1;
+// Form, CTAs-per-SM divisor and launch shape for box size n: the request
+// (default shape), or for FLCT_FORM_AUTO the autotuner's measured choice.
+void resolved_config(flct_ctx* ctx, int requested, int n, int* form, WinCfg* cfg) {
+    *cfg = WinCfg{};
     if (requested != FLCT_FORM_AUTO) {
         *form = requested;
         return;
@@ -932,7 +956,8 @@ void resolved_config(flct_ctx* ctx, int requested, int n, int* form, int* grid_d
         return;
     }
     *form = it->second.form;
-    *grid_div = it->second.grid_div;
+    cfg->grid_div = it->second.grid_div;
+    cfg->variant = it->second.variant;
 }
 
 // ------------------------------------------------------ sigma <= 0 --
@@ -1086,7 +1111,7 @@ struct BatchGroup {
     double sigma = 0., kr = 0.;
     std::vector<int> pairs;
     int form = FLCT_FORM_FP32;
-    int grid_div = 1;
+    WinCfg cfg;
 };
 
 // One kernel's launches for many pairs merged into one grid: the per-pair
@@ -1438,7 +1463,7 @@ flct_status enqueue_batch(flct_ctx* ctx, BatchPlan& bp, cudaStream_t bs, bool br
         WinArgs wa;
         group_wargs(ctx, bp, g, &wa);
         unsigned* status = (unsigned*)(bp.bufs[G.pairs[0]].ctr + 4);
-        s = launch_windows(ctx, G.form, find_win(G.n), G.n, wa, status, lane(g), G.grid_div);
+        s = launch_windows(ctx, G.form, find_win(G.n), G.n, wa, status, lane(g), G.cfg);
         ++*launches;
     }
     if (s != FLCT_OK) return s;
@@ -1506,7 +1531,7 @@ flct_status rebuild_batch(flct_ctx* ctx, int npairs, const flct_pair* pairs, cud
     s = tune_batch(ctx, bp, bs);
     if (s != FLCT_OK) return s;
     for (auto& G : bp.groups) {
-        resolved_config(ctx, G.req_form, G.n, &G.form, &G.grid_div);
+        resolved_config(ctx, G.req_form, G.n, &G.form, &G.cfg);
         s = prime_form(ctx, G.form, G.n);
         if (s != FLCT_OK) return s;
     }
@@ -1538,7 +1563,7 @@ flct_status rebuild_batch(flct_ctx* ctx, int npairs, const flct_pair* pairs, cud
 // prepass): stage events for flct_gpu_last_timing (recorded as graph nodes
 // when capturing), windows, fit, interpolation and the counters' copy to
 // page-locked memory.
-flct_status enqueue_device_tail(flct_ctx* ctx, const Job& j, const JobBufs& b, int form, int grid_div,
+flct_status enqueue_device_tail(flct_ctx* ctx, const Job& j, const JobBufs& b, int form, WinCfg cfg,
                                 cudaStream_t st, bool graph, int* launches, bool from_start = false) {
     // Stage events.  Eager: plain records.  Captured: ev[0] and ev[3] are
     // recorded on the caller's stream around the graph launch, and the
@@ -1566,7 +1591,7 @@ flct_status enqueue_device_tail(flct_ctx* ctx, const Job& j, const JobBufs& b, i
     CK(stamp(ctx->ev[1]));
     // the window, fit and interpolation kernels launch as programmatic
     // dependents: each one's launch overlaps the tail of the kernel before it
-    s = launch_windows(ctx, form, j.we, j.n, wa, (unsigned*)(b.ctr + 4), st, grid_div, -1, true);
+    s = launch_windows(ctx, form, j.we, j.n, wa, (unsigned*)(b.ctr + 4), st, cfg, -1, true);
     if (s != FLCT_OK) return s;
     ++*launches;
     CK(stamp(ctx->ev[2]));
@@ -1659,7 +1684,7 @@ flct_status banded_buffers(flct_ctx* ctx, const Job& j) {
 // in the one-band call, and the box sums are exact, so the results are
 // identical.  Every stream joins ctx->stream at the end, so the enqueue can
 // also run inside a stream capture.
-flct_status enqueue_banded(flct_ctx* ctx, const Job& j, const Bands& bd, int form, int grid_div, const double* f1,
+flct_status enqueue_banded(flct_ctx* ctx, const Job& j, const Bands& bd, int form, WinCfg cfg, const double* f1,
                            const double* f2, double* vx, double* vy, double* vm, int* nlaunch) {
     const int nb = bd.nb;
     const size_t ny = (size_t)j.ny;
@@ -1746,7 +1771,7 @@ flct_status enqueue_banded(flct_ctx* ctx, const Job& j, const Bands& bd, int for
         wb.nwork = (const int*)bb[b].ctr;
         wb.peaks = bb[b].peaks;
         wb.peaks_h = j.p->hires ? bb[b].peaks_h : nullptr;
-        s = launch_windows(ctx, form, j.we, j.n, wb, (unsigned*)(bb[b].ctr + 4), sb, grid_div, items);
+        s = launch_windows(ctx, form, j.we, j.n, wb, (unsigned*)(bb[b].ctr + 4), sb, cfg, items);
         ++launches;
         if (s == FLCT_OK) s = enqueue_fit(ctx, j, bb[b], sb, &launches, items, interp ? Pub{} : pub);
         if (s != FLCT_OK) break;
@@ -1790,7 +1815,7 @@ bool page_locked(const void* p) {
 // whole enqueue is captured once as a CUDA graph and replayed while the
 // call's parameters, sizes and pointers stay the same: one launch instead
 // of ~100 stream operations per call.
-flct_status velocity_banded(flct_ctx* ctx, const Job& j, const Bands& bd, int form, int grid_div,
+flct_status velocity_banded(flct_ctx* ctx, const Job& j, const Bands& bd, int form, WinCfg cfg,
                             const double* f1, const double* f2, double* vx, double* vy, double* vm) {
     flct_status s = banded_buffers(ctx, j);
     if (s != FLCT_OK) return s;
@@ -1804,7 +1829,7 @@ flct_status velocity_banded(flct_ctx* ctx, const Job& j, const Bands& bd, int fo
             key.insert(key.end(), c, c + n);
         };
         const flct_params& p = *j.p;
-        const int ints[] = {j.nx, j.ny, bd.nb, form, grid_div, p.thresh_abs, p.skip, p.poffset, p.qoffset,
+        const int ints[] = {j.nx, j.ny, bd.nb, form, cfg.grid_div, cfg.variant, p.thresh_abs, p.skip, p.poffset, p.qoffset,
                             p.interpolate, p.filter, p.hires};
         const double dbl[] = {p.deltat, p.deltas, p.sigma, p.thresh, p.kr};
         const void* ptrs[] = {f1, f2, vx, vy, vm, ctx->b_f1.p, ctx->b_f2.p, ctx->b_vx.p, ctx->b_vy.p, ctx->b_vm.p,
@@ -1821,7 +1846,7 @@ flct_status velocity_banded(flct_ctx* ctx, const Job& j, const Bands& bd, int fo
             }
             ctx->hkey.clear();
             CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
-            s = enqueue_banded(ctx, j, bd, form, grid_div, f1, f2, vx, vy, vm, &launches);
+            s = enqueue_banded(ctx, j, bd, form, cfg, f1, f2, vx, vy, vm, &launches);
             cudaGraph_t g = nullptr;
             const cudaError_t ec = cudaStreamEndCapture(st, &g);
             if (s != FLCT_OK || ec != cudaSuccess) {
@@ -1846,7 +1871,7 @@ flct_status velocity_banded(flct_ctx* ctx, const Job& j, const Bands& bd, int fo
         CK(cudaGraphLaunch(ctx->hexec, st));
     } else {
         CK(cudaEventRecord(ctx->ev[4], st));
-        s = enqueue_banded(ctx, j, bd, form, grid_div, f1, f2, vx, vy, vm, &launches);
+        s = enqueue_banded(ctx, j, bd, form, cfg, f1, f2, vx, vy, vm, &launches);
         if (s != FLCT_OK) {
             cudaStreamSynchronize(st);
             return s;
@@ -2098,7 +2123,8 @@ flct_status flct_gpu_velocity_device(flct_ctx* ctx, const flct_params* p, const 
     unsigned* d_status = (unsigned*)(b.ctr + 4);
 
     ctx->batch_pending = 0;
-    int launches = 0, grid_div = 1;
+    int launches = 0;
+    WinCfg cfg;
     // first FLCT_FORM_AUTO call for this box size: time the candidates on
     // this work list, eagerly (not possible inside a stream capture)
     if (p->form == FLCT_FORM_AUTO && !ctx->tune.count(n) && !capturing(st)) {
@@ -2114,11 +2140,11 @@ flct_status flct_gpu_velocity_device(flct_ctx* ctx, const flct_params* p, const 
         }
         s = tune_windows(ctx, j.we, n, wa, d_status, (const int*)b.ctr, st);
         if (s != FLCT_OK) return s;
-        resolved_config(ctx, p->form, n, &form, &grid_div);
-        s = enqueue_device_tail(ctx, j, b, form, grid_div, st, false, &launches);
+        resolved_config(ctx, p->form, n, &form, &cfg);
+        s = enqueue_device_tail(ctx, j, b, form, cfg, st, false, &launches);
         if (s != FLCT_OK) return s;
     } else {
-        resolved_config(ctx, p->form, n, &form, &grid_div);
+        resolved_config(ctx, p->form, n, &form, &cfg);
         s = prime_form(ctx, form, n);
         if (s != FLCT_OK) return s;
         // a call repeated with the same parameters and buffers is captured
@@ -2129,7 +2155,7 @@ flct_status flct_gpu_velocity_device(flct_ctx* ctx, const flct_params* p, const 
                 const unsigned char* c = (const unsigned char*)v;
                 key.insert(key.end(), c, c + nb);
             };
-            const int ints[] = {nx, ny, form, grid_div, p->thresh_abs, p->skip, p->poffset, p->qoffset,
+            const int ints[] = {nx, ny, form, cfg.grid_div, cfg.variant, p->thresh_abs, p->skip, p->poffset, p->qoffset,
                                 p->interpolate, p->filter, p->hires};
             const double dbl[] = {p->deltat, p->deltas, p->sigma, p->thresh, p->kr};
             const void* ptrs[] = {d_f1, d_f2, d_vx, d_vy, d_vm, ctx->b_s1.p, ctx->b_s2.p, ctx->b_work.p,
@@ -2153,7 +2179,7 @@ flct_status flct_gpu_velocity_device(flct_ctx* ctx, const flct_params* p, const 
             ctx->dkey.clear();
             cudaStream_t cs = ctx->stream;
             CK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed));
-            s = enqueue_device_tail(ctx, j, b, form, grid_div, cs, true, &launches, true);
+            s = enqueue_device_tail(ctx, j, b, form, cfg, cs, true, &launches, true);
             cudaGraph_t g = nullptr;
             const cudaError_t ec = cudaStreamEndCapture(cs, &g);
             if (s != FLCT_OK || ec != cudaSuccess) {
@@ -2175,7 +2201,7 @@ flct_status flct_gpu_velocity_device(flct_ctx* ctx, const flct_params* p, const 
             CK(cudaEventRecord(ctx->ev[3], st));
         } else {
             ctx->dlast = key;
-            s = enqueue_device_tail(ctx, j, b, form, grid_div, st, false, &launches, true);
+            s = enqueue_device_tail(ctx, j, b, form, cfg, st, false, &launches, true);
             if (s != FLCT_OK) return s;
         }
     }
@@ -2263,14 +2289,15 @@ flct_status flct_gpu_velocity(flct_ctx* ctx, const flct_params* p, const double*
         if (s != FLCT_OK) return s;
         Bands bd;
         if (!j.d.global && (p->form != FLCT_FORM_AUTO || ctx->tune.count(j.n)) && plan_bands(ctx, j, &bd)) {
-            int form = FLCT_FORM_FP32, grid_div = 1;
+            int form = FLCT_FORM_FP32;
+            WinCfg cfg;
             s = pick_form(ctx, p->form, j.n, &form);
             if (s != FLCT_OK) return s;
-            resolved_config(ctx, p->form, j.n, &form, &grid_div);
+            resolved_config(ctx, p->form, j.n, &form, &cfg);
             s = prime_form(ctx, form, j.n);
             if (s != FLCT_OK) return s;
             ctx->batch_pending = 0;
-            s = velocity_banded(ctx, j, bd, form, grid_div, f1, f2, vx, vy, vm);
+            s = velocity_banded(ctx, j, bd, form, cfg, f1, f2, vx, vy, vm);
             if (s != FLCT_OK) return s;
             CK(cudaEventSynchronize(ctx->ev[6]));
             s = collect_timing(ctx);

@@ -56,26 +56,44 @@ struct WinArgs {
     double sigma, kr;
 };
 
+// Launch shape of the box-N kernel.  Variant V = 0 is the default; V = 1
+// is the autotuner's alternative: twice the teams per CTA where that CTA
+// still fits twice per SM in shared memory and has at most 512 threads,
+// else half the teams, with no register cap.  A window's arithmetic is the
+// same in both; only the windows per CTA and the occupancy differ.
 template <int N>
+constexpr int win_teams0() { return (N <= 8) ? (128 / N) : (N <= 20 || N == 32) ? 8 : (N <= 40) ? 4 : 2; }
+template <int N>
+constexpr size_t win_smem(int teams) {
+    return 32 * teams + ((3 * N + 1) * 4 + 15) / 16 * 16 + (size_t)N * 8 + (size_t)teams * N * (N + 1) * 8;
+}
+template <int N>
+constexpr int win_teams_alt() {
+    constexpr int t = win_teams0<N>();
+    return (2 * t * N <= 512 && 2 * win_smem<N>(2 * t) <= 227 * 1024) ? 2 * t : (t > 1 ? t / 2 : 1);
+}
+
+template <int N, int V = 0>
 struct WinShape {
-    static constexpr int TEAMS = (N <= 8) ? (128 / N) : (N <= 20 || N == 32) ? 8 : (N <= 40) ? 4 : 2;
+    static constexpr int TEAMS = V == 0 ? win_teams0<N>() : win_teams_alt<N>();
     static constexpr int THREADS = N * TEAMS;
     static constexpr int BUF = N * (N + 1);  // float2 per team
     static constexpr size_t tw_off = 32 * TEAMS + ((3 * N + 1) * 4 + 15) / 16 * 16;
     static constexpr size_t head = tw_off + (size_t)N * 8;
     static constexpr size_t smem = head + (size_t)TEAMS * BUF * 8;  // |c| reuses the buffer
+    static_assert(smem == win_smem<N>(TEAMS), "shared-memory layout");
     // CTAs per SM the register allocation is held to (0: no constraint).
     // Box 32: 2 CTAs of 8 teams at 128 registers, no spills, beat 5 CTAs of
     // 4 teams at 96 registers with 12 bytes spilled (175.8 against 181.9 us
     // for 65,536 windows; 4 CTAs of 4 teams at 128 registers: 179.9 us;
     // measured).
-    static constexpr int MINB = (N == 32) ? 2 : 0;
+    static constexpr int MINB = (V == 0 && N == 32) ? 2 : 0;
 };
 
-template <int N>
-__global__ void __launch_bounds__(WinShape<N>::THREADS, WinShape<N>::MINB)
+template <int N, int V>
+__global__ void __launch_bounds__(WinShape<N, V>::THREADS, WinShape<N, V>::MINB)
 k_window_fp32(WinArgs a) {
-    using S = WinShape<N>;
+    using S = WinShape<N, V>;
     constexpr int TEAMS = S::TEAMS;
     extern __shared__ __align__(16) unsigned char sm[];
     unsigned long long* s_key = reinterpret_cast<unsigned long long*>(sm + 16 * TEAMS);
@@ -404,11 +422,12 @@ k_window_fp32(WinArgs a) {
     }
 }
 
-// Host-side launcher for one box size (defined in the per-size .cu files);
-// pdl: launch as a programmatic dependent of the stream's previous kernel.
-template <int N>
+// Host-side launcher for one box size and shape variant (defined in the
+// per-size .cu files); pdl: launch as a programmatic dependent of the
+// stream's previous kernel.
+template <int N, int V>
 cudaError_t launch_window_fp32(const WinArgs& a, int grid, cudaStream_t st, bool pdl);
-template <int N>
+template <int N, int V>
 int window_fp32_blocks_per_sm();
 
 }  // namespace flct
