@@ -558,6 +558,19 @@ def run_warp(a, dev):
         out[name] = {"mpix_s": img.size / dt / 1e6, "ms_per_call": dt * 1e3}
     out["size"] = list(img.shape)
     out["note"] = "host buffers in and out, wall clock per call"
+    # a 4096^2 uniform shift: power-of-two axes take the transform path
+    from pyflct_gb300 import _lib
+    big = synth.kfield((4096, 4096), rng)
+    shift_frac2d(big, 0.37, -2.6, device=dev.index or 0)
+    walls, devs = [], []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        shift_frac2d(big, 0.37, -2.6, device=dev.index or 0)
+        walls.append(time.perf_counter() - t0)
+        devs.append(_lib.context(dev.index or 0).timing().ms_total)
+    out["shift_frac2d_4096"] = {"ms_per_call": min(walls) * 1e3, "device_ms": min(devs),
+                                "mpix_s_device": big.size / (min(devs) / 1e3) / 1e6,
+                                "note": "wall clock with 134 MB copied each way; device_ms = the kernels alone"}
     return out
 
 

@@ -2516,24 +2516,31 @@ flct_status flct_gpu_shift_frac2d(flct_ctx* ctx, const double* arr, double delx,
     ENSURE(ctx->b_s1, n * sizeof(float2));
     ENSURE(ctx->b_s2, n * sizeof(float2));
     ENSURE(ctx->b_aux1, (size_t)(nx + ny) * sizeof(float2) + 64);
-    ENSURE(ctx->b_aux2, (size_t)2 * std::max(nx, ny) * sizeof(double2));
+    ENSURE(ctx->b_aux2, (size_t)2 * (nx + ny) * sizeof(double2));
     float2* sx = (float2*)ctx->b_aux1.p;
     float2* sy = sx + nx;
     // warp.c:811-820: shifts normalised by the axis lengths; transp swaps them
     const double dxarg = transp ? -dely / ((double)nx) : -delx / ((double)nx);
     const double dyarg = transp ? -delx / ((double)ny) : -dely / ((double)ny);
+    const bool fft = shift_fft_axis(nx) && shift_fft_axis(ny);
     CK(cudaMemcpyAsync(ctx->b_f1.p, arr, n * sizeof(double), cudaMemcpyHostToDevice, st));
     CK(cudaEventRecord(ctx->ev[0], st));
-    CK(launch_shift_vector(nx, dxarg, (double2*)ctx->b_aux2.p, sx, st));
-    CK(launch_shift_vector(ny, dyarg, (double2*)ctx->b_aux2.p, sy, st));
-    CK(launch_axis_fast(0, true, ctx->b_f1.p, nx, ny, sy, (float2*)ctx->b_s1.p, st));
-    CK(launch_axis_slow(0, (const float2*)ctx->b_s1.p, ny, nx, sx, (float2*)ctx->b_s2.p, st));
-    CK(launch_real_part((const float2*)ctx->b_s2.p, (long)n, (double*)ctx->b_vx.p, st));
+    if (fft) {
+        // power-of-two axes: the same linear map by transforms, O(N log N)
+        CK(launch_shift_fft((const double*)ctx->b_f1.p, nx, ny, dxarg, dyarg, (double2*)ctx->b_aux2.p, sx,
+                            (float2*)ctx->b_s1.p, (float2*)ctx->b_s2.p, (double*)ctx->b_vx.p, ctx->nsm, st));
+    } else {
+        CK(launch_shift_vector(nx, dxarg, (double2*)ctx->b_aux2.p, sx, st));
+        CK(launch_shift_vector(ny, dyarg, (double2*)ctx->b_aux2.p, sy, st));
+        CK(launch_axis_fast(0, true, ctx->b_f1.p, nx, ny, sy, (float2*)ctx->b_s1.p, st));
+        CK(launch_axis_slow(0, (const float2*)ctx->b_s1.p, ny, nx, sx, (float2*)ctx->b_s2.p, st));
+        CK(launch_real_part((const float2*)ctx->b_s2.p, (long)n, (double*)ctx->b_vx.p, st));
+    }
     CK(cudaEventRecord(ctx->ev[1], st));
     CK(cudaMemcpyAsync(out, ctx->b_vx.p, n * sizeof(double), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     ctx->timing = flct_timing{};
-    ctx->timing.launches = 7;
+    ctx->timing.launches = fft ? 8 : 7;
     ctx->timing.ms_total = ev_ms(ctx->ev[0], ctx->ev[1]);
     return FLCT_OK;
 }

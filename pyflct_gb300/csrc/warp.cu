@@ -5,8 +5,12 @@
 // The phase factor is separable, so the operation is a circulant matrix
 // along each axis: out = Re(Sx . X . Sy^T) with
 //   sx[d] = (1/nx) sum_kx exp(i 2 pi kx (d/nx + dxarg)).
-// Two passes of k_axis_* (one per axis) apply it; the circulant vectors are
-// built in FP64 from the reference's phase expression.
+// Power-of-two axes (64 .. kWarpMaxAxis) apply it as transforms, one CTA
+// per line (k_shift_lines_fft: forward FFT, phase factors, inverse FFT,
+// O(L log L) per line), the slow axis after a transpose.  Other lengths
+// take two passes of k_axis_* (one per axis), O(L) per output; the
+// circulant vectors are built in FP64 from the reference's phase
+// expression.
 //
 // warp_frac2d (source/warp.c:883-1011): F = DFT2(image) (the same axis
 // kernels with the DFT matrix), then for every pixel the direct spectral sum
@@ -187,6 +191,93 @@ __global__ void __launch_bounds__(256) k_axis_slow(const float2* __restrict__ in
     }
 }
 
+// --------------------------------------------------- transform path ----
+
+// Each line of length L (a power of two): X = FFT(line) by radix-2
+// decimation in time in shared memory (inputs placed at bit-reversed
+// positions), X[k] *= ph[k], then the inverse by radix-2 decimation in
+// frequency (natural order in, bit-reversed out), read back in natural
+// order, times `scale`.  tw[t] = exp(-2 pi i t / L) (FP64, rounded once);
+// ph[k] = exp(i 2 pi kf darg) in FP64 from k_shift_tables.
+template <bool REAL_IN>
+__global__ void __launch_bounds__(512) k_shift_lines_fft(const void* __restrict__ in_, int nlines, int L, int logL,
+                                                         const float2* __restrict__ tw,
+                                                         const double2* __restrict__ ph, float scale,
+                                                         float2* __restrict__ out) {
+    extern __shared__ float2 x[];  // L
+    const int half = L >> 1;
+    for (int line = blockIdx.x; line < nlines; line += gridDim.x) {
+        for (int k = threadIdx.x; k < L; k += blockDim.x) {
+            const size_t o = (size_t)line * L + k;
+            float2 v;
+            if (REAL_IN) v = make_float2((float)static_cast<const double*>(in_)[o], 0.f);
+            else v = static_cast<const float2*>(in_)[o];
+            x[__brev((unsigned)k) >> (32 - logL)] = v;
+        }
+        __syncthreads();
+        for (int m = 1; m < L; m <<= 1) {  // butterflies of half-size m
+            const int ts = half / m;
+            for (int b = threadIdx.x; b < half; b += blockDim.x) {
+                const int j = b & (m - 1), k = ((b - j) << 1) + j;
+                const float2 w = __ldg(tw + j * ts);  // exp(-2 pi i j / 2m)
+                const float2 u = x[k], v = x[k + m];
+                const float2 t = make_float2(v.x * w.x - v.y * w.y, v.x * w.y + v.y * w.x);
+                x[k] = make_float2(u.x + t.x, u.y + t.y);
+                x[k + m] = make_float2(u.x - t.x, u.y - t.y);
+            }
+            __syncthreads();
+        }
+        for (int k = threadIdx.x; k < L; k += blockDim.x) {
+            const double2 p = ph[k];
+            const float px = (float)p.x, py = (float)p.y;
+            const float2 a = x[k];
+            x[k] = make_float2(a.x * px - a.y * py, a.x * py + a.y * px);
+        }
+        __syncthreads();
+        for (int m = half; m >= 1; m >>= 1) {
+            const int ts = half / m;
+            for (int b = threadIdx.x; b < half; b += blockDim.x) {
+                const int j = b & (m - 1), k = ((b - j) << 1) + j;
+                const float2 w = __ldg(tw + j * ts);
+                const float2 u = x[k], v = x[k + m];
+                const float2 d = make_float2(u.x - v.x, u.y - v.y);
+                x[k] = make_float2(u.x + v.x, u.y + v.y);
+                x[k + m] = make_float2(d.x * w.x + d.y * w.y, d.y * w.x - d.x * w.y);  // d exp(+2 pi i j / 2m)
+            }
+            __syncthreads();
+        }
+        for (int k = threadIdx.x; k < L; k += blockDim.x) {
+            const float2 v = x[__brev((unsigned)k) >> (32 - logL)];
+            out[(size_t)line * L + k] = make_float2(v.x * scale, v.y * scale);
+        }
+        __syncthreads();  // the next line overwrites x
+    }
+}
+
+// out[c][r] = in[r][c] (complex), 32 x 32 tiles.
+__global__ void __launch_bounds__(256) k_transpose_c(const float2* __restrict__ in, int rows, int cols,
+                                                     float2* __restrict__ out) {
+    __shared__ float2 t[32][33];
+    const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+    for (int i = threadIdx.y; i < 32; i += 8)
+        if (r0 + i < rows && c0 + threadIdx.x < cols) t[i][threadIdx.x] = in[(size_t)(r0 + i) * cols + c0 + threadIdx.x];
+    __syncthreads();
+    for (int i = threadIdx.y; i < 32; i += 8)
+        if (c0 + i < cols && r0 + threadIdx.x < rows) out[(size_t)(c0 + i) * rows + r0 + threadIdx.x] = t[threadIdx.x][i];
+}
+
+// out[c][r] = Re(in[r][c]) as double, 32 x 32 tiles.
+__global__ void __launch_bounds__(256) k_transpose_re(const float2* __restrict__ in, int rows, int cols,
+                                                      double* __restrict__ out) {
+    __shared__ float t[32][33];
+    const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+    for (int i = threadIdx.y; i < 32; i += 8)
+        if (r0 + i < rows && c0 + threadIdx.x < cols) t[i][threadIdx.x] = in[(size_t)(r0 + i) * cols + c0 + threadIdx.x].x;
+    __syncthreads();
+    for (int i = threadIdx.y; i < 32; i += 8)
+        if (c0 + i < cols && r0 + threadIdx.x < rows) out[(size_t)(c0 + i) * rows + r0 + threadIdx.x] = (double)t[threadIdx.x][i];
+}
+
 __global__ void k_real_part(const float2* __restrict__ in, long n, double* __restrict__ out) {
     for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x)
         out[k] = (double)in[k].x;
@@ -338,6 +429,42 @@ cudaError_t launch_axis_slow(int mode, const float2* in, int ncols, int L, const
 cudaError_t launch_shift_vector(int n, double darg, double2* scratch, float2* v, cudaStream_t st) {
     k_shift_tables<<<(n + 127) / 128, 128, 0, st>>>(n, darg, scratch, scratch + n);
     k_shift_vector<<<(n + 63) / 64, 64, 0, st>>>(n, scratch, scratch + n, v);
+    return cudaGetLastError();
+}
+
+bool shift_fft_axis(int n) { return n >= 64 && n <= kWarpMaxAxis && (n & (n - 1)) == 0; }
+
+cudaError_t launch_shift_fft(const double* in, int nx, int ny, double dxarg, double dyarg, double2* scratch,
+                             float2* tw, float2* buf1, float2* buf2, double* out, int nsm, cudaStream_t st) {
+    // FP64 phase factors (and roots, unused here) of both axes, twiddles
+    double2* rx = scratch;
+    double2* phx = rx + nx;
+    double2* ry = phx + nx;
+    double2* phy = ry + ny;
+    k_shift_tables<<<(nx + 127) / 128, 128, 0, st>>>(nx, dxarg, rx, phx);
+    k_shift_tables<<<(ny + 127) / 128, 128, 0, st>>>(ny, dyarg, ry, phy);
+    float2* twx = tw;
+    float2* twy = tw + nx;
+    k_twiddles<<<(nx + 255) / 256, 256, 0, st>>>(nx, -1, twx);
+    k_twiddles<<<(ny + 255) / 256, 256, 0, st>>>(ny, -1, twy);
+    auto log2i = [](int n) {
+        int l = 0;
+        while ((1 << l) < n) ++l;
+        return l;
+    };
+    cudaError_t e;
+    const size_t smy = (size_t)ny * sizeof(float2), smx = (size_t)nx * sizeof(float2);
+    e = cudaFuncSetAttribute(k_shift_lines_fft<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smy);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_shift_lines_fft<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
+    if (e != cudaSuccess) return e;
+    // fast axis: rows of the image, then the slow axis as rows of the transpose
+    k_shift_lines_fft<true><<<std::min(nx, nsm * 4), std::min(512, ny / 2), smy, st>>>(
+        in, nx, ny, log2i(ny), twy, phy, 1.0f / (float)ny, buf1);
+    k_transpose_c<<<dim3((ny + 31) / 32, (nx + 31) / 32), dim3(32, 8), 0, st>>>(buf1, nx, ny, buf2);
+    k_shift_lines_fft<false><<<std::min(ny, nsm * 4), std::min(512, nx / 2), smx, st>>>(
+        buf2, ny, nx, log2i(nx), twx, phx, 1.0f / (float)nx, buf1);
+    k_transpose_re<<<dim3((nx + 31) / 32, (ny + 31) / 32), dim3(32, 8), 0, st>>>(buf1, ny, nx, out);
     return cudaGetLastError();
 }
 

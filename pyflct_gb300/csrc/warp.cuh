@@ -14,6 +14,12 @@ cudaError_t launch_axis_slow(int mode, const float2* in, int ncols, int L, const
 // scratch: 2n double2
 cudaError_t launch_shift_vector(int n, double darg, double2* scratch, float2* v, cudaStream_t st);
 cudaError_t launch_twiddles(int L, int sign, float2* tw, cudaStream_t st);
+// shift_frac2d by transforms, for axes where shift_fft_axis holds (powers of
+// two, 64 .. kWarpMaxAxis): scratch 2 (nx + ny) double2, tw nx + ny float2,
+// buf1 / buf2 nx * ny float2 each; out nx * ny doubles on the device
+bool shift_fft_axis(int n);
+cudaError_t launch_shift_fft(const double* in, int nx, int ny, double dxarg, double dyarg, double2* scratch,
+                             float2* tw, float2* buf1, float2* buf2, double* out, int nsm, cudaStream_t st);
 cudaError_t launch_real_part(const float2* in, long n, double* out, cudaStream_t st);
 cudaError_t launch_warp_phase(const double* delx, const double* dely, int nx, int ny, int transp, float4* ph,
                               cudaStream_t st);

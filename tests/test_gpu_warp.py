@@ -56,6 +56,21 @@ def test_shift_sizes(shape, transp):
     assert close(got, ref, np.abs(img).max(), REL_SHIFT)
 
 
+@pytest.mark.parametrize("shape", [(64, 128), (256, 64), (1024, 512), (2048, 2048)])
+@pytest.mark.parametrize("transp", [1, 0])
+def test_shift_power_of_two_transform(shape, transp):
+    """Power-of-two axes take the transform path (forward FFT, phase
+    factors, inverse FFT per line); the oracle follows the reference's own
+    2-D FFT."""
+    from pyflct_gb300.flct import shift_frac2d
+    rng = np.random.default_rng(shape[0] * 31 + shape[1] + transp)
+    img = rng.standard_normal(shape) + 3.0
+    dx, dy = rng.uniform(-40, 40, 2)
+    got = shift_frac2d(img, dx, dy, transp)
+    ref = po.shift_frac2d(img, dx, dy, transp)
+    assert close(got, ref, np.abs(img).max(), REL_SHIFT)
+
+
 @pytest.mark.parametrize("shape", [(37, 53), (64, 48), (20, 31), (9, 8)])
 @pytest.mark.parametrize("transp", [1, 0])
 def test_warp_sizes(shape, transp):
