@@ -698,7 +698,7 @@ flct_status enqueue_classify(flct_ctx* ctx, const Job& j, const JobBufs& b, int 
         ca.nwork2 = (int*)b2->ctr;
         ca.rsplit = rsplit;
     }
-    const long tiles = (long)(r1 - r0) * ((j.ny + 255) / 256);
+    const long tiles = (long)(r1 - r0) * ((j.ny + kClassPix - 1) / kClassPix);
     k_classify<<<(int)std::max(1l, std::min<long>(tiles, (long)ctx->nsm * blocks_per_sm)), 256, 0, st>>>(ca);
     ++*launches;
     CK(cudaGetLastError());
@@ -1214,7 +1214,7 @@ flct_status plan_multi(flct_ctx* ctx, BatchPlan* bp) {
         thr.push_back(ThreshArgs{j.f1, j.f2, d_absmax, j.p->thresh, d_thr});
         bthr.push_back(j.d.rel_thresh ? 1 : 0);
         cls.push_back(classify_args(j, b, 0, j.nx, j.d.rel_thresh ? d_thr : nullptr));
-        bcls.push_back((long)j.nx * ((j.ny + 255) / 256));
+        bcls.push_back((long)j.nx * ((j.ny + kClassPix - 1) / kClassPix));
         long tasks = 0, threads = 0;
         rows.push_back(box_rows_args(j, b, 0, j.nx, &tasks));
         brows.push_back((tasks + kBoxWarps - 1) / kBoxWarps);

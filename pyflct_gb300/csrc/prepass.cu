@@ -68,12 +68,15 @@ __device__ __forceinline__ bool finite_bits(double x) {
 }
 
 
-// One tile = 256 consecutive pixels of one row, one per thread.  The work
-// list grows by one atomic per tile (block-wide ballot counts); the float
-// split of both frames uses integer operations, and the threshold test
-// 0.5*|f1+f2| < thresh (flct.c:721-722) needs one FP64 add only when the
-// threshold is positive (otherwise no pixel is below it).
+// One tile = kClassPix consecutive pixels of one row, kClassPpt per thread
+// (thread t owns pixels t * kClassPpt ...).  The work list grows by one
+// atomic per tile (block-wide ballot counts); the float split of both
+// frames uses integer operations, and the threshold test 0.5*|f1+f2| <
+// thresh (flct.c:721-722) needs one FP64 add only when the threshold is
+// positive (otherwise no pixel is below it).  The row's grid test is one
+// division per tile, the column's one per thread, then stepped per pixel.
 __device__ __forceinline__ void k_classify_body(const ClassifyArgs& a, const int vb, const int vg) {
+    constexpr int P = kClassPpt;
     __shared__ int s_cnt[8];
     __shared__ int s_base;
     const double thr = a.thr_ptr ? *a.thr_ptr : a.thr_val;
@@ -81,68 +84,74 @@ __device__ __forceinline__ void k_classify_body(const ClassifyArgs& a, const int
     // thr in (0, +inf]: compare |s|/2 with it as bit patterns
     const bool thr_pos = (long long)tb > 0ll && tb <= 0x7ff0000000000000ull;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int tpr = (a.ny + 255) >> 8;  // tiles per row
-    const int ntile = (a.r1 - a.r0) * tpr;  // < 2^31: sides are limited to 2^31 pixels
-    // the grid test's column remainder: (j - yoff) mod skip = tile base + this thread's offset
+    const int tpr = (a.ny + kClassPix - 1) / kClassPix;  // tiles per row
+    const int ntile = (a.r1 - a.r0) * tpr;               // < 2^31: sides are limited to 2^31 pixels
     const int sk = a.skip > 0 ? a.skip : 1;
-    const int tmod = (int)threadIdx.x % sk;
-    // this thread's pixel of tile t, its frames' values loaded a tile ahead
     auto pixel = [&](int t, int& i, int& j0) {
         const int ti = t / tpr;
         i = a.r0 + ti;
-        j0 = (t - ti * tpr) * 256;
+        j0 = (t - ti * tpr) * kClassPix + (int)threadIdx.x * P;  // this thread's first pixel
     };
-    double fa = 0., fb = 0.;
-    if (vb < ntile) {
+    double fa[P], fb[P];
+    auto load = [&](int t, double (&x)[P], double (&y)[P]) {
         int i, j0;
-        pixel(vb, i, j0);
-        if (j0 + (int)threadIdx.x < a.ny) {
-            fa = a.f1[(size_t)i * a.ny + j0 + threadIdx.x];
-            fb = a.f2[(size_t)i * a.ny + j0 + threadIdx.x];
+        pixel(t, i, j0);
+        const size_t o = (size_t)i * a.ny + j0;
+#pragma unroll
+        for (int q = 0; q < P; ++q) {
+            const bool in = j0 + q < a.ny;
+            x[q] = in ? a.f1[o + q] : 0.;
+            y[q] = in ? a.f2[o + q] : 0.;
         }
-    }
+    };
+    if (vb < ntile) load(vb, fa, fb);
     for (int t = vb; t < ntile; t += vg) {
         int i, j0;
         pixel(t, i, j0);
-        const int j = j0 + threadIdx.x;
-        double na = 0., nb = 0.;
-        if (t + (int)vg < ntile) {
-            int i2, j2;
-            pixel(t + vg, i2, j2);
-            if (j2 + (int)threadIdx.x < a.ny) {
-                na = a.f1[(size_t)i2 * a.ny + j2 + threadIdx.x];
-                nb = a.f2[(size_t)i2 * a.ny + j2 + threadIdx.x];
+        double na[P], nb[P];
+        if (t + vg < ntile) load(t + vg, na, nb);
+        // the reference's C test !((i-xoff)%skip) && !((j-yoff)%skip): an
+        // offset pixel (j < yoff) has a nonzero C remainder
+        const bool grid_row = (a.skip > 0) ? !((i - a.xoff) % a.skip) : true;
+        int rj = ((j0 - a.yoff) % sk + sk) % sk;  // (j - yoff) mod skip of the first pixel
+        const size_t k0 = (size_t)i * a.ny + j0;
+        bool comp[P], grid[P];
+        unsigned range = 0u;
+#pragma unroll
+        for (int q = 0; q < P; ++q) {
+            const int j = j0 + q;
+            comp[q] = grid[q] = false;
+            if (j < a.ny) {
+                const float2 sa = split_double_fast(fa[q]), sb = split_double_fast(fb[q]);
+                a.s1[k0 + q] = sa;
+                a.s2[k0 + q] = sb;
+                // a finite value beyond the FP32 range (integer tests on the bits)
+                if (((__float_as_uint(sa.x) & 0x7fffffffu) == 0x7f800000u && finite_bits(fa[q])) ||
+                    ((__float_as_uint(sb.x) & 0x7fffffffu) == 0x7f800000u && finite_bits(fb[q])))
+                    range = kStatusRange;
+                bool below = false;
+                if (thr_pos) {
+                    const unsigned long long sb2 =
+                        (unsigned long long)__double_as_longlong(__dadd_rn(fa[q], fb[q])) & 0x7fffffffffffffffull;
+                    const unsigned E = (unsigned)(sb2 >> 52);
+                    if (E >= 2u && E < 0x7ffu) below = (sb2 - (1ull << 52)) < tb;  // exact halving
+                    else if (E == 0x7ffu) below = sb2 < tb;                         // inf / NaN
+                    else below = __dmul_rn(0.5, __longlong_as_double((long long)sb2)) < thr;
+                }
+                grid[q] = (a.skip > 0) ? (grid_row && j >= a.yoff && rj == 0) : true;
+                comp[q] = !below && grid[q];
             }
+            rj = (rj + 1 == sk) ? 0 : rj + 1;
         }
-        int rj = ((j0 - a.yoff) % sk + sk) % sk + tmod;  // uniform part + per-thread part
-        rj = rj >= sk ? rj - sk : rj;
-        const bool act = j < a.ny;
-        const size_t k = (size_t)i * a.ny + j;
-        bool comp = false, grid = false;
-        if (act) {
-            const float2 sa = split_double_fast(fa), sb = split_double_fast(fb);
-            a.s1[k] = sa;
-            a.s2[k] = sb;
-            // a finite value beyond the FP32 range (integer tests on the bits)
-            if (((__float_as_uint(sa.x) & 0x7fffffffu) == 0x7f800000u && finite_bits(fa)) ||
-                ((__float_as_uint(sb.x) & 0x7fffffffu) == 0x7f800000u && finite_bits(fb)))
-                atomicOr(a.status, kStatusRange);
-            bool below = false;
-            if (thr_pos) {
-                const unsigned long long sb2 =
-                    (unsigned long long)__double_as_longlong(__dadd_rn(fa, fb)) & 0x7fffffffffffffffull;
-                const unsigned E = (unsigned)(sb2 >> 52);
-                if (E >= 2u && E < 0x7ffu) below = (sb2 - (1ull << 52)) < tb;  // exact halving
-                else if (E == 0x7ffu) below = sb2 < tb;                         // inf / NaN
-                else below = __dmul_rn(0.5, __longlong_as_double((long long)sb2)) < thr;
-            }
-            // the reference's C test !((i-xoff)%skip) && !((j-yoff)%skip): an
-            // offset pixel (j < yoff) has a nonzero C remainder
-            grid = (a.skip > 0) ? (!((i - a.xoff) % a.skip) && j >= a.yoff && rj == 0) : true;
-            comp = !below && grid;
+        if (range) atomicOr(a.status, range);
+        unsigned m[P];
+        int wc = 0;
+#pragma unroll
+        for (int q = 0; q < P; ++q) {
+            m[q] = __ballot_sync(0xffffffffu, comp[q]);
+            wc += __popc(m[q]);
         }
-        const unsigned m = __ballot_sync(0xffffffffu, comp);
-        if (lane == 0) s_cnt[warp] = __popc(m);
+        if (lane == 0) s_cnt[warp] = wc;
         // a tile is one row: its windows go to one list
         const bool second = a.work2 && i >= a.rsplit;
         int* const wl = second ? a.work2 : a.work;
@@ -158,29 +167,40 @@ __device__ __forceinline__ void k_classify_body(const ClassifyArgs& a, const int
             s_base = tot ? atomicAdd(second ? a.nwork2 : a.nwork, tot) : 0;
         }
         __syncthreads();
-        if (comp) {
-            wl[s_base + s_cnt[warp] + __popc(m & ((1u << lane) - 1u))] = (int)k;
-        } else if (act) {
-            // pixels without a window: (xmiss, xmiss, 0) then the reset gives
-            // (0, 0, 0); skipped pixels that will be interpolated are left to
-            // the interpolation.
-            if (grid) {
-                a.vx[k] = 0.;
-                a.vy[k] = 0.;
-                a.vm[k] = 0.;
-                if (a.grid) {
-                    const int ic = (i - a.xoff) / a.skip, jc = (j - a.yoff) / a.skip;
-                    a.grid[(size_t)ic * a.jcnt + jc] = make_float2(kXmissF, kXmissF);
+        int pos = s_base + s_cnt[warp];
+        const unsigned below_me = (1u << lane) - 1u;
+#pragma unroll
+        for (int q = 0; q < P; ++q) {
+            const int j = j0 + q;
+            const size_t k = k0 + q;
+            if (comp[q]) {
+                wl[pos + __popc(m[q] & below_me)] = (int)k;
+            } else if (j < a.ny) {
+                // pixels without a window: (xmiss, xmiss, 0) then the reset gives
+                // (0, 0, 0); skipped pixels that will be interpolated are left to
+                // the interpolation.
+                if (grid[q]) {
+                    a.vx[k] = 0.;
+                    a.vy[k] = 0.;
+                    a.vm[k] = 0.;
+                    if (a.grid) {
+                        const int ic = (i - a.xoff) / a.skip, jc = (j - a.yoff) / a.skip;
+                        a.grid[(size_t)ic * a.jcnt + jc] = make_float2(kXmissF, kXmissF);
+                    }
+                } else if (!a.interpolate) {
+                    a.vx[k] = 0.;
+                    a.vy[k] = 0.;
+                    a.vm[k] = 0.;
                 }
-            } else if (!a.interpolate) {
-                a.vx[k] = 0.;
-                a.vy[k] = 0.;
-                a.vm[k] = 0.;
             }
+            pos += __popc(m[q]);
         }
         __syncthreads();  // s_cnt / s_base are rewritten by the next tile
-        fa = na;
-        fb = nb;
+#pragma unroll
+        for (int q = 0; q < P; ++q) {
+            fa[q] = na[q];
+            fb[q] = nb[q];
+        }
     }
 }
 FLCT_MULTI_KERNEL(__launch_bounds__(256), k_classify, ClassifyArgs)

@@ -25,6 +25,10 @@ struct ClassifyArgs {
     int rsplit;
 };
 
+// Classification: pixels per thread, and per tile (256 threads).
+constexpr int kClassPpt = 4;
+constexpr int kClassPix = 256 * kClassPpt;
+
 // Row pass of the box sums: warps per block, and the longest input span a
 // warp converts into shared memory per pass.
 constexpr int kBoxWarps = 4;
