@@ -771,11 +771,11 @@ flct_status enqueue_box_rows(flct_ctx* ctx, const Job& j, const JobBufs& b, int 
 // Exact box sums of grid rows [q0, q1) (their row sums must be complete; q0
 // a multiple of kColRun, so the runs are those of the whole frame).
 flct_status enqueue_box_cols(flct_ctx* ctx, const Job& j, const JobBufs& b, int q0, int q1, cudaStream_t st,
-                             int* launches) {
+                             int* launches, bool pdl = false) {
     if (q1 <= q0) return FLCT_OK;
     long t = 0;
     BoxArgs ba = box_cols_args(j, b, q0, q1, &t);
-    k_box_cols<<<(int)((t + 127) / 128), 128, 0, st>>>(ba);
+    CK(launch_kernel(k_box_cols, dim3((unsigned)((t + 127) / 128)), dim3(128), 0, st, pdl, ba));
     ++*launches;
     CK(cudaGetLastError());
     return FLCT_OK;
@@ -806,7 +806,8 @@ flct_status enqueue_prepass(flct_ctx* ctx, const Job& j, const JobBufs& b, cudaS
         if (s == FLCT_OK) s = enqueue_classify(ctx, j, b, 0, j.nx, thr, side, launches, 4);
         if (s != FLCT_OK) return s;
         CK(cudaEventRecord(ctx->pev[1], side));
-        s = enqueue_box_cols(ctx, j, b, 0, j.gi, st, launches);
+        // the column pass launches as a programmatic dependent of the row pass
+        s = enqueue_box_cols(ctx, j, b, 0, j.gi, st, launches, true);
         CK(cudaStreamWaitEvent(st, ctx->pev[1], 0));
     } else {
         s = enqueue_classify(ctx, j, b, 0, j.nx, thr, st, launches);

@@ -340,6 +340,7 @@ __device__ __forceinline__ void col_reduce(unsigned long long& lo, unsigned long
 }
 
 __device__ __forceinline__ void k_box_cols_body(const BoxArgs& a, const int vb, const int vg) {
+    grid_dep_wait();  // the row sums come from the kernel before
     const int lines = 2 * a.gj;
     const int runs = (a.q1 - a.q0 + kColRun - 1) / kColRun;
     const long gid = vb * (long)blockDim.x + threadIdx.x;
