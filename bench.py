@@ -102,7 +102,9 @@ def peaks():
 
 
 class Clocks:
-    """nvidia-smi sampling during the timed region."""
+    """nvidia-smi sampling during the timed region: every 20 ms, started
+    before the region and entered only once the first sample has arrived
+    (nvidia-smi takes ~0.1 s to start), so the samples cover the region."""
 
     def __init__(self, index: int):
         self.index = index
@@ -113,11 +115,15 @@ class Clocks:
         cmd = ["nvidia-smi", "-i", str(self.index),
                "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
                "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-               "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "100"]
+               "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "20"]
         try:
             self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            t0 = time.perf_counter()
+            while not self.lines and time.perf_counter() - t0 < 3.0:
+                time.sleep(0.005)
+            self.lines = []  # samples from here on belong to the timed region
         except Exception:
             self.proc = None
         return self
@@ -313,9 +319,9 @@ class DeviceRunner:
         evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
         win_ms = []
         torch.cuda.synchronize()
-        wall0 = time.perf_counter()
         if clocks:
             clocks.__enter__()
+        wall0 = time.perf_counter()
         for k in range(steps):
             self.flush.zero_()
             evs[k][0].record(self.stream)
@@ -758,7 +764,7 @@ def run_ours(a):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--form", default="auto", choices=["auto", "fp32", "tc_fp16", "tc_bf16"])

@@ -375,8 +375,7 @@ flct_status launch_windows(flct_ctx* ctx, int form, const WinEntry* we, int n, c
         if (form != FLCT_FORM_FP32 || n > kMaxBigBox)
             return fail(ctx, FLCT_ERR_UNSUPPORTED, "box %d has no kernel of this form", n);
         BigArgs ba{};
-        ba.s1 = wa.s1;
-        ba.s2 = wa.s2;
+        ba.s12 = wa.s12;
         ba.means = wa.means;
         ba.mg = wa.mg;
         ba.work = wa.work;
@@ -425,8 +424,7 @@ flct_status launch_windows(flct_ctx* ctx, int form, const WinEntry* we, int n, c
     const int k = tc_index(n);
     if (k < 0) return fail(ctx, FLCT_ERR_UNSUPPORTED, "the tensor-core form has no kernel for box %d", n);
     TcArgs ta{};
-    ta.s1 = wa.s1;
-    ta.s2 = wa.s2;
+    ta.s12 = wa.s12;
     ta.means = wa.means;
     ta.mg = wa.mg;
     ta.work = wa.work;
@@ -624,8 +622,7 @@ flct_status plan_job(flct_ctx* ctx, const flct_params* p, const double* f1, cons
 // Device workspace of one job: the context's single-call buffers, or a
 // slice of a batch's buffers.
 struct JobBufs {
-    float2* s1 = nullptr;
-    float2* s2 = nullptr;
+    float4* s12 = nullptr;  // both frames' float split per pixel
     int* work = nullptr;
     float4* means = nullptr;  // local means [gi][gj] (MeanGrid)
     PeakRec* peaks = nullptr;
@@ -648,7 +645,7 @@ struct JobSizes {
 JobSizes job_sizes(const Job& j) {
     const size_t npx = (size_t)j.nx * j.ny;
     JobSizes z;
-    z.s = npx * sizeof(float2);
+    z.s = npx * sizeof(float4);
     z.work = npx * sizeof(int);
     z.means = (size_t)j.gi * j.gj * sizeof(float4);
     z.peaks = npx * sizeof(PeakRec);
@@ -675,8 +672,7 @@ ClassifyArgs classify_args(const Job& j, const JobBufs& b, int r0, int r1, const
     ca.yoff = j.d.yoff;
     ca.interpolate = j.interp;
     ca.jcnt = j.d.jcnt;
-    ca.s1 = b.s1;
-    ca.s2 = b.s2;
+    ca.s12 = b.s12;
     ca.work = b.work;
     ca.nwork = (int*)b.ctr;
     ca.vx = j.vx;
@@ -828,8 +824,7 @@ void make_wargs(const Job& j, const JobBufs& b, WinArgs* wa) {
     wa->sigma = j.p->sigma;
     wa->kr = j.p->kr;
     wa->use_filter = j.p->filter;
-    wa->s1 = b.s1;
-    wa->s2 = b.s2;
+    wa->s12 = b.s12;
     wa->means = b.means;
     wa->mg = MeanGrid{j.gs, j.xo, j.yo, j.gj};
     wa->work = b.work;
@@ -1300,7 +1295,7 @@ flct_status plan_batch(flct_ctx* ctx, int npairs, const flct_pair* pairs, BatchP
     }
     // workspace: per-pair arena slices, item-indexed arrays shared by all pairs
     struct Off {
-        size_t s1, s2, r1, r2, re1, re2, grid;
+        size_t s12, r1, r2, re1, re2, grid;
         long long base;
     };
     std::vector<Off> off(npairs);
@@ -1314,8 +1309,7 @@ flct_status plan_batch(flct_ctx* ctx, int npairs, const flct_pair* pairs, BatchP
     for (int k = 0; k < npairs; ++k) {
         const JobSizes z = job_sizes(bp->jobs[k]);
         Off& o = off[k];
-        o.s1 = take(z.s);
-        o.s2 = take(z.s);
+        o.s12 = take(z.s);
         o.r1 = take(z.r);
         o.r2 = take(z.r);
         o.re1 = take(z.re);
@@ -1344,8 +1338,7 @@ flct_status plan_batch(flct_ctx* ctx, int npairs, const flct_pair* pairs, BatchP
     for (int k = 0; k < npairs; ++k) {
         const Off& o = off[k];
         JobBufs& b = bp->bufs[k];
-        b.s1 = (float2*)(A + o.s1);
-        b.s2 = (float2*)(A + o.s2);
+        b.s12 = (float4*)(A + o.s12);
         b.r1 = (BoxSum*)(A + o.r1);
         b.r2 = (BoxSum*)(A + o.r2);
         b.re1 = (int*)(A + o.re1);
@@ -1367,8 +1360,7 @@ flct_status plan_batch(flct_ctx* ctx, int npairs, const flct_pair* pairs, BatchP
         hfirst[g] = e;
         for (int k : bp->groups[g].pairs) {
             WinSeg sg{};
-            sg.s1 = bp->bufs[k].s1;
-            sg.s2 = bp->bufs[k].s2;
+            sg.s12 = bp->bufs[k].s12;
             sg.nx = bp->jobs[k].nx;
             sg.ny = bp->jobs[k].ny;
             sg.base = (int)off[k].base;
@@ -1663,7 +1655,6 @@ bool plan_bands(const flct_ctx* ctx, const Job& j, Bands* bd) {
 flct_status banded_buffers(flct_ctx* ctx, const Job& j) {
     const JobSizes z = job_sizes(j);
     ENSURE(ctx->b_s1, z.s);
-    ENSURE(ctx->b_s2, z.s);
     ENSURE(ctx->b_work, z.work);
     ENSURE(ctx->b_ctr, 64 * flct_ctx::kMaxBands);
     ENSURE(ctx->b_r1, z.r);
@@ -1691,8 +1682,7 @@ flct_status enqueue_banded(flct_ctx* ctx, const Job& j, const Bands& bd, int for
     const size_t ny = (size_t)j.ny;
     const JobSizes z = job_sizes(j);
     JobBufs base;
-    base.s1 = (float2*)ctx->b_s1.p;
-    base.s2 = (float2*)ctx->b_s2.p;
+    base.s12 = (float4*)ctx->b_s1.p;
     base.work = (int*)ctx->b_work.p;
     base.means = (float4*)ctx->b_means.p;
     base.peaks = (PeakRec*)ctx->b_peaks.p;
@@ -2101,7 +2091,6 @@ flct_status flct_gpu_velocity_device(flct_ctx* ctx, const flct_params* p, const 
 
     const JobSizes z = job_sizes(j);
     ENSURE(ctx->b_s1, z.s);
-    ENSURE(ctx->b_s2, z.s);
     ENSURE(ctx->b_work, z.work);
     ENSURE(ctx->b_ctr, 64);
     ENSURE(ctx->b_r1, z.r);
@@ -2115,8 +2104,7 @@ flct_status flct_gpu_velocity_device(flct_ctx* ctx, const flct_params* p, const 
         ENSURE(ctx->b_grid, z.grid);
     }
     JobBufs b;
-    b.s1 = (float2*)ctx->b_s1.p;
-    b.s2 = (float2*)ctx->b_s2.p;
+    b.s12 = (float4*)ctx->b_s1.p;
     b.work = (int*)ctx->b_work.p;
     b.means = (float4*)ctx->b_means.p;
     b.peaks = (PeakRec*)ctx->b_peaks.p;
@@ -2357,8 +2345,7 @@ flct_status flct_gpu_cross_cor_batch(flct_ctx* ctx, const double* g1, const doub
     // own box with zero mean and unit Gaussian
     ENSURE(ctx->b_f1, npx * sizeof(double));
     ENSURE(ctx->b_f2, npx * sizeof(double));
-    ENSURE(ctx->b_s1, npx * sizeof(float2));
-    ENSURE(ctx->b_s2, npx * sizeof(float2));
+    ENSURE(ctx->b_s1, npx * sizeof(float4));
     ENSURE(ctx->b_work, (size_t)nwin * sizeof(int));
     ENSURE(ctx->b_ctr, 64);
     ENSURE(ctx->b_vx, (size_t)nwin * sizeof(double));
@@ -2378,8 +2365,7 @@ flct_status flct_gpu_cross_cor_batch(flct_ctx* ctx, const double* g1, const doub
     ca.nx = nwin * n;
     ca.ny = n;
     ca.thr_val = -INFINITY;
-    ca.s1 = (float2*)ctx->b_s1.p;
-    ca.s2 = (float2*)ctx->b_s2.p;
+    ca.s12 = (float4*)ctx->b_s1.p;
     ENSURE(ctx->b_aux2, npx * sizeof(int) + 64);
     ca.work = (int*)ctx->b_aux2.p;  // discarded list
     ca.nwork = (int*)(ctr + 32);
@@ -2404,8 +2390,7 @@ flct_status flct_gpu_cross_cor_batch(flct_ctx* ctx, const double* g1, const doub
     wa.sigma = 1.0;
     wa.kr = kr;
     wa.use_filter = filter;
-    wa.s1 = (const float2*)ctx->b_s1.p;
-    wa.s2 = (const float2*)ctx->b_s2.p;
+    wa.s12 = (const float4*)ctx->b_s1.p;
     wa.means = nullptr;
     wa.work = (const int*)ctx->b_work.p;
     wa.nwork = (const int*)ctr;

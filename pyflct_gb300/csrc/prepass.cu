@@ -123,8 +123,7 @@ __device__ __forceinline__ void k_classify_body(const ClassifyArgs& a, const int
             comp[q] = grid[q] = false;
             if (j < a.ny) {
                 const float2 sa = split_double_fast(fa[q]), sb = split_double_fast(fb[q]);
-                a.s1[k0 + q] = sa;
-                a.s2[k0 + q] = sb;
+                a.s12[k0 + q] = make_float4(sa.x, sa.y, sb.x, sb.y);
                 // a finite value beyond the FP32 range (integer tests on the bits)
                 if (((__float_as_uint(sa.x) & 0x7fffffffu) == 0x7f800000u && finite_bits(fa[q])) ||
                     ((__float_as_uint(sb.x) & 0x7fffffffu) == 0x7f800000u && finite_bits(fb[q])))

@@ -12,8 +12,7 @@ struct ClassifyArgs {
     double thr_val;           // absolute threshold, used when thr_ptr is null
     const double* thr_ptr;    // device threshold from k_thresh_final
     int skip, xoff, yoff, interpolate, jcnt;
-    float2* s1;
-    float2* s2;
+    float4* s12;              // both frames' float split per pixel: (f1 hi, f1 lo, f2 hi, f2 lo)
     int* work;
     int* nwork;
     double *vx, *vy, *vm;

@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(kBigThreads) k_window_big(BigArgs a) {
     unsigned* s_max = reinterpret_cast<unsigned*>(s_mean + 1);
     unsigned long long* s_key = reinterpret_cast<unsigned long long*>(s_max + 4);
     int* s_item = reinterpret_cast<int*>(s_key + 1);  // gi, imin, jmin, gr offset, gc offset, ny
-    const float2** s_src = reinterpret_cast<const float2**>(s_item + 8);
+    const float4** s_src = reinterpret_cast<const float4**>(s_item + 8);
 
     const int t = threadIdx.x;
     for (int k = t; k < n; k += kBigThreads) {
@@ -95,16 +95,14 @@ __global__ void __launch_bounds__(kBigThreads) k_window_big(BigArgs a) {
     for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
         if (t == 0) {
             int gi = w;
-            const float2* f1s = a.s1;
-            const float2* f2s = a.s2;
+            const float4* f12 = a.s12;
             int nx = a.nx, ny = a.ny;
             const float4* mp = a.means;
             MeanGrid mg = a.mg;
             if (a.nseg > 0) {
                 const int k = seg_find(a.seg_start, a.nseg, gi);
                 const WinSeg sg = a.segs[k];
-                f1s = sg.s1;
-                f2s = sg.s2;
+                f12 = sg.s12;
                 nx = sg.nx;
                 ny = sg.ny;
                 if (mp) mp += sg.base;
@@ -130,8 +128,7 @@ __global__ void __launch_bounds__(kBigThreads) k_window_big(BigArgs a) {
             s_item[3] = imin - ic + n;
             s_item[4] = jmin - jc + n;
             s_item[5] = ny;
-            s_src[0] = f1s + (size_t)imin * ny + jmin;
-            s_src[1] = f2s + (size_t)imin * ny + jmin;
+            s_src[0] = f12 + (size_t)imin * ny + jmin;
             *s_mean = (mp && !a.direct) ? mp[mean_slot(mg, ic, jc)] : make_float4(0.f, 0.f, 0.f, 0.f);
             s_max[0] = 0u;
             s_max[1] = 0u;
@@ -147,8 +144,8 @@ __global__ void __launch_bounds__(kBigThreads) k_window_big(BigArgs a) {
         float mx1 = 0.f, mx2 = 0.f;
         for (int p = t; p < n * n; p += kBigThreads) {
             const int i = p / n, j = p - i * n;
-            const float2 u = s_src[0][(size_t)i * ny + j];
-            const float2 v = s_src[1][(size_t)i * ny + j];
+            const float4 q = s_src[0][(size_t)i * ny + j];
+            const float2 u = make_float2(q.x, q.y), v = make_float2(q.z, q.w);
             const float wgt = s_g[gco + j] * s_g[gro + i];
             const float2 zz = make_float2(wgt * ((u.x - m1.x) + (u.y - m1.y)), wgt * ((v.x - m2.x) + (v.y - m2.y)));
             z[(size_t)i * ld + j] = zz;

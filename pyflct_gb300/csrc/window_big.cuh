@@ -9,8 +9,7 @@ namespace flct {
 constexpr int kMaxBigBox = 128;  // largest box side of the big-box kernel
 
 struct BigArgs {
-    const float2* s1;     // f1 split (hi, lo) [nx*ny]
-    const float2* s2;
+    const float4* s12;    // both frames split per pixel (WinArgs::s12)
     const float4* means;  // per grid point at mean_slot(mg, i, j), or null: zero means
     MeanGrid mg;
     const int* work;

@@ -145,8 +145,7 @@ __device__ __forceinline__ void fit_item(const FitArgs& a, int w, const PeakRec&
 // of the work counts, one more entry than segments) maps a launch-wide
 // item index to its pair.
 struct WinSeg {
-    const float2* s1;
-    const float2* s2;
+    const float4* s12;  // the pair's split frames (WinArgs::s12)
     int nx, ny;
     int base;
     MeanGrid mg;

@@ -36,8 +36,7 @@
 namespace flct {
 
 struct WinArgs {
-    const float2* s1;     // f1 split (hi, lo) [nx*ny]
-    const float2* s2;     // f2 split
+    const float4* s12;    // both frames split per pixel: (f1 hi, f1 lo, f2 hi, f2 lo) [nx*ny]
     const float4* means;  // per grid point at mean_slot(mg, i, j), or null: zero means
     MeanGrid mg;
     const int* work;      // pixel indices i*ny + j
@@ -140,16 +139,14 @@ k_window_fp32(WinArgs a) {
         const int w = base + team;
         const bool valid = w < nwork;
         int gi = valid ? w : base;  // item index into work / peaks
-        const float2* f1s = a.s1;
-        const float2* f2s = a.s2;
+        const float4* f12 = a.s12;
         int nx = a.nx, ny = a.ny;
         const float4* mp = a.means;
         MeanGrid mg = a.mg;
         if (a.nseg > 0) {
             const int k = seg_find(a.seg_start, a.nseg, gi);
             const WinSeg sg = a.segs[k];
-            f1s = sg.s1;
-            f2s = sg.s2;
+            f12 = sg.s12;
             nx = sg.nx;
             ny = sg.ny;
             if (mp) mp += sg.base;
@@ -177,15 +174,16 @@ k_window_fp32(WinArgs a) {
                 (mp && !a.direct) ? __ldg(mp + mean_slot(mg, i, j)) : make_float4(0.f, 0.f, 0.f, 0.f);
             const float2 m1 = make_float2(mm.x, mm.y), m2 = make_float2(mm.z, mm.w);
             const float wc = s_g[ln + jmin - j + N];
-            const float2* p1 = f1s + (size_t)imin * ny + jmin + ln;
-            const float2* p2 = f2s + (size_t)imin * ny + jmin + ln;
+            const float4* p12 = f12 + (size_t)imin * ny + jmin + ln;
             const float* gr = a.gauss + (imin - i + N);  // row weights: uniform, from the parameter bank
             float mx1 = 0.f, mx2 = 0.f;
             sfor<0, N>([&](auto ic) {
                 constexpr int ii = decltype(ic)::value;
-                // (hi - mean hi) + (lo - mean lo), the hi and lo halves packed
-                const float2 u = csub(__ldg(p1 + (size_t)ii * ny), m1);
-                const float2 v = csub(__ldg(p2 + (size_t)ii * ny), m2);
+                // (hi - mean hi) + (lo - mean lo), the hi and lo halves
+                // packed; both frames' pixel in one 16-byte load
+                const float4 q = __ldg(p12 + (size_t)ii * ny);
+                const float2 u = csub(make_float2(q.x, q.y), m1);
+                const float2 v = csub(make_float2(q.z, q.w), m2);
                 const float wgt = wc * gr[ii];
                 const float2 z = make_float2(wgt * (u.x + u.y), wgt * (v.x + v.y));
                 x[fft_in<N>(ii)] = z;  // row ii where the column transform takes it

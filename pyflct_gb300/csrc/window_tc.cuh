@@ -63,8 +63,7 @@
 namespace flct {
 
 struct TcArgs {
-    const float2* s1;
-    const float2* s2;
+    const float4* s12;    // both frames split per pixel (WinArgs::s12)
     const float4* means;  // per grid point at mean_slot(mg, i, j), or null (direct windows)
     MeanGrid mg;
     const int* work;
@@ -254,7 +253,7 @@ __global__ void __launch_bounds__(256, TcCfg<N>::MINB) k_window_tc(TcArgs a) {
     int* s_gi = reinterpret_cast<int*>(misc + 848);                          // WIT
     int4* s_geo = reinterpret_cast<int4*>(misc + 912);                       // WIT: imin, jmin, gr off, gc off
     float4* s_mean = reinterpret_cast<float4*>(misc + 1168);                 // WIT
-    const float2** s_src = reinterpret_cast<const float2**>(misc + 1424);   // 2 WIT: box origins
+    const float4** s_src = reinterpret_cast<const float4**>(misc + 1424);   // WIT box origins (2 WIT slots)
     int* s_ny = reinterpret_cast<int*>(misc + 1680);                         // WIT
     unsigned* s_wmax = reinterpret_cast<unsigned*>(misc + 1744);             // WIT
     int* s_widx = reinterpret_cast<int*>(misc + 1808);                       // WIT
@@ -339,8 +338,7 @@ __global__ void __launch_bounds__(256, TcCfg<N>::MINB) k_window_tc(TcArgs a) {
     // threads t < WIT (their global-load latency then overlaps the previous
     // iteration's tensor-core stages).
     struct Fetch {
-        const float2* f1;
-        const float2* f2;
+        const float4* f12;
         float4 mean;
         int gi, pix, nx, ny, valid;
     };
@@ -348,8 +346,7 @@ __global__ void __launch_bounds__(256, TcCfg<N>::MINB) k_window_tc(TcArgs a) {
         Fetch f;
         f.valid = b + t < nwork;
         int w = f.valid ? b + t : nwork - 1;
-        f.f1 = a.s1;
-        f.f2 = a.s2;
+        f.f12 = a.s12;
         f.nx = a.nx;
         f.ny = a.ny;
         const float4* mp = a.means;
@@ -357,8 +354,7 @@ __global__ void __launch_bounds__(256, TcCfg<N>::MINB) k_window_tc(TcArgs a) {
         if (a.nseg > 0) {
             const int k = seg_find(a.seg_start, a.nseg, w);
             const WinSeg sg = a.segs[k];
-            f.f1 = sg.s1;
-            f.f2 = sg.s2;
+            f.f12 = sg.s12;
             f.nx = sg.nx;
             f.ny = sg.ny;
             if (mp) mp += sg.base;
@@ -398,8 +394,7 @@ __global__ void __launch_bounds__(256, TcCfg<N>::MINB) k_window_tc(TcArgs a) {
             s_gi[t] = nxt.gi;
             s_valid[t] = nxt.valid;
             s_geo[t] = make_int4(imin, jmin, imin - ic + N, jmin - jc + N);
-            s_src[2 * t] = nxt.f1 + (size_t)imin * nxt.ny + jmin;
-            s_src[2 * t + 1] = nxt.f2 + (size_t)imin * nxt.ny + jmin;
+            s_src[t] = nxt.f12 + (size_t)imin * nxt.ny + jmin;
             s_ny[t] = nxt.ny;
             s_mean[t] = nxt.mean;
             s_wmax[t] = 0u;
@@ -423,6 +418,53 @@ __global__ void __launch_bounds__(256, TcCfg<N>::MINB) k_window_tc(TcArgs a) {
                 float mx[PJ];
                 int sub[PJ];
                 const int jl = lane % C::LW;
+                // one sub-image per warp pass and two passes at once: the
+                // warp takes both images of one window, so a 16-byte load
+                // gives both frames' (hi, lo) of a pixel
+                constexpr bool kPair = C::SPW == 1 && PJ == 2 && NPASS == 2;
+                if constexpr (kPair) {
+                    const int w = wp;  // sub-images 2 wp (f1) and 2 wp + 1 (f2)
+                    const bool sval = 2 * w + 1 < C::SUBS;
+                    sub[0] = sval ? 2 * w : -1;
+                    sub[1] = sval ? 2 * w + 1 : -1;
+                    const int wv = sval ? w : 0;
+                    const int4 geo = s_geo[wv];
+                    const int ny = s_ny[wv];
+                    const float4 mm = s_mean[wv];
+                    const float4* src = s_src[wv];
+                    const float* gr = s_g + geo.z;
+                    mx[0] = mx[1] = 0.f;
+#pragma unroll
+                    for (int cb = 0; cb < C::CB; ++cb) {
+                        const int j = cb * 32 + jl;
+                        const bool jv = sval && j < N;
+                        const float gc = jv ? s_g[geo.w + j] : 0.f;
+                        gcol[0][cb] = gcol[1][cb] = gc;
+                        float m0 = 0.f, m1 = 0.f;
+                        if (jv) {
+                            const float4* col = src + j;
+#pragma unroll
+                            for (int i = 0; i < N8; ++i) {
+                                if (i < N) {
+                                    const float4 q = __ldg(col + (size_t)i * ny);
+                                    const float2 d0 = csub(make_float2(q.x, q.y), make_float2(mm.x, mm.y));
+                                    const float2 d1 = csub(make_float2(q.z, q.w), make_float2(mm.z, mm.w));
+                                    x[0][cb][i] = (d0.x + d0.y) * gr[i];
+                                    x[1][cb][i] = (d1.x + d1.y) * gr[i];
+                                    m0 = fmaxf(m0, fabsf(x[0][cb][i]));
+                                    m1 = fmaxf(m1, fabsf(x[1][cb][i]));
+                                } else {
+                                    x[0][cb][i] = x[1][cb][i] = 0.f;
+                                }
+                            }
+                        } else {
+#pragma unroll
+                            for (int i = 0; i < N8; ++i) x[0][cb][i] = x[1][cb][i] = 0.f;
+                        }
+                        mx[0] = fmaxf(mx[0], m0 * gc);
+                        mx[1] = fmaxf(mx[1], m1 * gc);
+                    }
+                } else {
 #pragma unroll
                 for (int pj = 0; pj < PJ; ++pj) {
                     const int s = (p0 + pj) * 8 * C::SPW + wp * C::SPW + lane / C::LW;
@@ -435,7 +477,7 @@ __global__ void __launch_bounds__(256, TcCfg<N>::MINB) k_window_tc(TcArgs a) {
                     // x = (f - mean) g_r(i): the column weight g_c(j) >= 0 is
                     // folded into the lane's final scale
                     const float2 mhl = img ? make_float2(mm.z, mm.w) : make_float2(mm.x, mm.y);
-                    const float2* src = s_src[2 * w + img];
+                    const float4* src = s_src[w];
                     const float* gr = s_g + geo.z;
                     mx[pj] = 0.f;
 #pragma unroll
@@ -445,11 +487,13 @@ __global__ void __launch_bounds__(256, TcCfg<N>::MINB) k_window_tc(TcArgs a) {
                         gcol[pj][cb] = jv ? s_g[geo.w + j] : 0.f;
                         float mc = 0.f;
                         if (jv) {
-                            const float2* col = src + j;
+                            // this image's (hi, lo) half of each pixel's float4
+                            const float2* col = reinterpret_cast<const float2*>(src + j) + img;
+                            const int ld = 2 * ny;  // float2 per frame row of the interleaved split
 #pragma unroll
                             for (int i = 0; i < N8; ++i) {
                                 if (i < N) {
-                                    const float2 d = csub(__ldg(col + (size_t)i * ny), mhl);
+                                    const float2 d = csub(__ldg(col + (size_t)i * ld), mhl);
                                     x[pj][cb][i] = (d.x + d.y) * gr[i];
                                     mc = fmaxf(mc, fabsf(x[pj][cb][i]));
                                 } else {
@@ -462,6 +506,7 @@ __global__ void __launch_bounds__(256, TcCfg<N>::MINB) k_window_tc(TcArgs a) {
                         }
                         mx[pj] = fmaxf(mx[pj], mc * gcol[pj][cb]);
                     }
+                }
                 }
 #pragma unroll
                 for (int pj = 0; pj < PJ; ++pj) {
