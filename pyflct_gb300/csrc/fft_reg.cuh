@@ -101,6 +101,15 @@ FLCT_HD float2 cadd(float2 a, float2 b) { FLCT_PACKED_OP("add.rn.f32x2") }
 FLCT_HD float2 csub(float2 a, float2 b) { FLCT_PACKED_OP("sub.rn.f32x2") }
 // element-wise product (a.x * b.x, a.y * b.y)
 FLCT_HD float2 emul(float2 a, float2 b) { FLCT_PACKED_OP("mul.rn.f32x2") }
+// a * k for a real k
+FLCT_HD float2 cscale(float2 a, float k) {
+    float2 r;
+    asm("{\n.reg .b64 ra, rk, rd;\nmov.b64 ra, {%2, %3};\nmov.b64 rk, {%4, %4};\n"
+        "mul.rn.f32x2 rd, ra, rk;\nmov.b64 {%0, %1}, rd;\n}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a.x), "f"(a.y), "f"(k));
+    return r;
+}
 // a * k + b for a real k
 FLCT_HD float2 cfma(float2 a, float k, float2 b) {
     float2 r;
@@ -115,6 +124,7 @@ FLCT_HD float2 cfma(float2 a, float k, float2 b) {
 FLCT_HD float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 FLCT_HD float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 FLCT_HD float2 cfma(float2 a, float k, float2 b) { return make_float2(fmaf(a.x, k, b.x), fmaf(a.y, k, b.y)); }
+FLCT_HD float2 cscale(float2 a, float k) { return make_float2(a.x * k, a.y * k); }
 FLCT_HD float2 emul(float2 a, float2 b) { return make_float2(a.x * b.x, a.y * b.y); }
 #endif
 // Scalar forms, for operands that are swapped or negated halves of a pair

@@ -123,7 +123,7 @@ __device__ __forceinline__ void k_classify_body(const ClassifyArgs& a, const int
             comp[q] = grid[q] = false;
             if (j < a.ny) {
                 const float2 sa = split_double_fast(fa[q]), sb = split_double_fast(fb[q]);
-                a.s12[k0 + q] = make_float4(sa.x, sa.y, sb.x, sb.y);
+                a.s12[k0 + q] = make_float4(sa.x, sb.x, sa.y, sb.y);
                 // a finite value beyond the FP32 range (integer tests on the bits)
                 if (((__float_as_uint(sa.x) & 0x7fffffffu) == 0x7f800000u && finite_bits(fa[q])) ||
                     ((__float_as_uint(sb.x) & 0x7fffffffu) == 0x7f800000u && finite_bits(fb[q])))
@@ -353,8 +353,9 @@ __device__ __forceinline__ void k_box_cols_body(const BoxArgs& a, const int vb, 
     const int img = lam >= a.gj, m = lam - img * a.gj;
     const BoxSum* __restrict__ v = (img ? a.rt2 : a.rt1) + m;  // row r at v[r * gj]
     const int* __restrict__ ve = (img ? a.re2 : a.re1) + m;
-    // this line's half (hi, lo) of the grid points' float4 means
-    float2* __restrict__ o = reinterpret_cast<float2*>(a.means + m) + img;
+    // this line's hi and lo in the grid points' float4 means (f1 hi, f2 hi,
+    // f1 lo, f2 lo): floats img and 2 + img
+    float* __restrict__ o = reinterpret_cast<float*>(a.means + m) + img;
     const size_t gj = (size_t)a.gj;
     const int q0 = a.q0 + run * kColRun, q1 = min(q0 + kColRun, a.q1);
     int t = box_start(a.xo + q0 * a.gs, a.nx, a.nsize);
@@ -377,7 +378,9 @@ __device__ __forceinline__ void k_box_cols_body(const BoxArgs& a, const int vb, 
         if (act && p == 0) {
             // the FP64 mean (flct.c:815-827), rounded once from the exact sum
             const BoxSum bs{lo, hi, cnt, (unsigned long long)eb};
-            o[(size_t)q * gj * 2] = split_double_fast(__dmul_rn(fx_to_double(bs, eb), a.inv_n2));
+            const float2 mhl = split_double_fast(__dmul_rn(fx_to_double(bs, eb), a.inv_n2));
+            o[(size_t)q * gj * 4] = mhl.x;
+            o[(size_t)q * gj * 4 + 2] = mhl.y;
         }
         if (++q >= q1) break;
         // slide down to the next grid row's box: rows [t, tn) leave, rows

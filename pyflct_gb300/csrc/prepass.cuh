@@ -12,7 +12,7 @@ struct ClassifyArgs {
     double thr_val;           // absolute threshold, used when thr_ptr is null
     const double* thr_ptr;    // device threshold from k_thresh_final
     int skip, xoff, yoff, interpolate, jcnt;
-    float4* s12;              // both frames' float split per pixel: (f1 hi, f1 lo, f2 hi, f2 lo)
+    float4* s12;              // both frames' float split per pixel: (f1 hi, f2 hi, f1 lo, f2 lo)
     int* work;
     int* nwork;
     double *vx, *vy, *vm;
@@ -50,7 +50,7 @@ struct BoxArgs {
     int pass_r;               // row pass: grid columns per warp pass
     BoxSum *rt1, *rt2;        // row sums [nx][gj]
     int *re1, *re2;           // their exponents, compact [nx][gj]
-    float4* means;            // local means [gi][gj]: (f1 hi, f1 lo, f2 hi, f2 lo)
+    float4* means;            // local means [gi][gj]: (f1 hi, f2 hi, f1 lo, f2 lo)
     double inv_n2;            // 1 / n^2
     int r0, r1;               // frame rows of the row pass
     int q0, q1;               // grid rows of the column pass

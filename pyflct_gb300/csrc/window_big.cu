@@ -138,14 +138,14 @@ __global__ void __launch_bounds__(kBigThreads) k_window_big(BigArgs a) {
         const int gi = s_item[0];
         const int gro = s_item[3], gco = s_item[4], ny = s_item[5];
         const float4 mm = *s_mean;
-        const float2 m1 = make_float2(mm.x, mm.y), m2 = make_float2(mm.z, mm.w);
+        const float2 m1 = make_float2(mm.x, mm.z), m2 = make_float2(mm.y, mm.w);  // (hi, lo) per frame
 
         // windowed, mean-subtracted sub-images, z = g1 + i g2
         float mx1 = 0.f, mx2 = 0.f;
         for (int p = t; p < n * n; p += kBigThreads) {
             const int i = p / n, j = p - i * n;
             const float4 q = s_src[0][(size_t)i * ny + j];
-            const float2 u = make_float2(q.x, q.y), v = make_float2(q.z, q.w);
+            const float2 u = make_float2(q.x, q.z), v = make_float2(q.y, q.w);  // (hi, lo) per frame
             const float wgt = s_g[gco + j] * s_g[gro + i];
             const float2 zz = make_float2(wgt * ((u.x - m1.x) + (u.y - m1.y)), wgt * ((v.x - m2.x) + (v.y - m2.y)));
             z[(size_t)i * ld + j] = zz;

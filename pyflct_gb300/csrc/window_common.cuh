@@ -46,7 +46,7 @@ __host__ __device__ __forceinline__ int meta_J(unsigned m) { return (int)((m >> 
 __host__ __device__ __forceinline__ bool meta_flag(unsigned m) { return (m >> 30) & 1u; }
 
 // Where the window of pixel (i, j) finds its local means: one float4
-// (f1 hi, f1 lo, f2 hi, f2 lo) per grid point [gi][gj], grid point (q, m) =
+// (f1 hi, f2 hi, f1 lo, f2 lo) per grid point [gi][gj], grid point (q, m) =
 // pixel (xo + q gs, yo + m gs).
 struct MeanGrid {
     int gs, xo, yo, gj;

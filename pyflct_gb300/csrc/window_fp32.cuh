@@ -36,7 +36,7 @@
 namespace flct {
 
 struct WinArgs {
-    const float4* s12;    // both frames split per pixel: (f1 hi, f1 lo, f2 hi, f2 lo) [nx*ny]
+    const float4* s12;    // both frames split per pixel: (f1 hi, f2 hi, f1 lo, f2 lo) [nx*ny]
     const float4* means;  // per grid point at mean_slot(mg, i, j), or null: zero means
     MeanGrid mg;
     const int* work;      // pixel indices i*ny + j
@@ -172,20 +172,20 @@ k_window_fp32(WinArgs a) {
         {
             const float4 mm =
                 (mp && !a.direct) ? __ldg(mp + mean_slot(mg, i, j)) : make_float4(0.f, 0.f, 0.f, 0.f);
-            const float2 m1 = make_float2(mm.x, mm.y), m2 = make_float2(mm.z, mm.w);
+            const float2 mh = make_float2(mm.x, mm.y), ml = make_float2(mm.z, mm.w);  // (f1, f2) hi, lo
             const float wc = s_g[ln + jmin - j + N];
             const float4* p12 = f12 + (size_t)imin * ny + jmin + ln;
             const float* gr = a.gauss + (imin - i + N);  // row weights: uniform, from the parameter bank
             float mx1 = 0.f, mx2 = 0.f;
             sfor<0, N>([&](auto ic) {
                 constexpr int ii = decltype(ic)::value;
-                // (hi - mean hi) + (lo - mean lo), the hi and lo halves
-                // packed; both frames' pixel in one 16-byte load
+                // (hi - mean hi) + (lo - mean lo) for both frames at once
+                // (packed f1/f2 pairs), both frames' pixel in one 16-byte load
                 const float4 q = __ldg(p12 + (size_t)ii * ny);
-                const float2 u = csub(make_float2(q.x, q.y), m1);
-                const float2 v = csub(make_float2(q.z, q.w), m2);
+                const float2 dh = csub(make_float2(q.x, q.y), mh);
+                const float2 dl = csub(make_float2(q.z, q.w), ml);
                 const float wgt = wc * gr[ii];
-                const float2 z = make_float2(wgt * (u.x + u.y), wgt * (v.x + v.y));
+                const float2 z = cscale(cadd(dh, dl), wgt);
                 x[fft_in<N>(ii)] = z;  // row ii where the column transform takes it
                 mx1 = fmaxf(mx1, fabsf(z.x));
                 mx2 = fmaxf(mx2, fabsf(z.y));

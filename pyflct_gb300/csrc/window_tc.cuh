@@ -63,7 +63,7 @@
 namespace flct {
 
 struct TcArgs {
-    const float4* s12;    // both frames split per pixel (WinArgs::s12)
+    const float4* s12;    // both frames split per pixel (WinArgs::s12: f1 hi, f2 hi, f1 lo, f2 lo)
     const float4* means;  // per grid point at mean_slot(mg, i, j), or null (direct windows)
     MeanGrid mg;
     const int* work;
@@ -446,11 +446,10 @@ __global__ void __launch_bounds__(256, TcCfg<N>::MINB) k_window_tc(TcArgs a) {
 #pragma unroll
                             for (int i = 0; i < N8; ++i) {
                                 if (i < N) {
+                                    // (f1, f2): (hi - mean hi) + (lo - mean lo)
                                     const float4 q = __ldg(col + (size_t)i * ny);
-                                    const float2 d0 = csub(make_float2(q.x, q.y), make_float2(mm.x, mm.y));
-                                    const float2 d1 = csub(make_float2(q.z, q.w), make_float2(mm.z, mm.w));
-                                    x[0][cb][i] = (d0.x + d0.y) * gr[i];
-                                    x[1][cb][i] = (d1.x + d1.y) * gr[i];
+                                    x[0][cb][i] = ((q.x - mm.x) + (q.z - mm.z)) * gr[i];
+                                    x[1][cb][i] = ((q.y - mm.y) + (q.w - mm.w)) * gr[i];
                                     m0 = fmaxf(m0, fabsf(x[0][cb][i]));
                                     m1 = fmaxf(m1, fabsf(x[1][cb][i]));
                                 } else {
@@ -476,7 +475,8 @@ __global__ void __launch_bounds__(256, TcCfg<N>::MINB) k_window_tc(TcArgs a) {
                     const float4 mm = s_mean[w];
                     // x = (f - mean) g_r(i): the column weight g_c(j) >= 0 is
                     // folded into the lane's final scale
-                    const float2 mhl = img ? make_float2(mm.z, mm.w) : make_float2(mm.x, mm.y);
+                    // this image's (hi, lo) mean: floats img and 2 + img of the float4
+                    const float2 mhl = img ? make_float2(mm.y, mm.w) : make_float2(mm.x, mm.z);
                     const float4* src = s_src[w];
                     const float* gr = s_g + geo.z;
                     mx[pj] = 0.f;
@@ -487,13 +487,14 @@ __global__ void __launch_bounds__(256, TcCfg<N>::MINB) k_window_tc(TcArgs a) {
                         gcol[pj][cb] = jv ? s_g[geo.w + j] : 0.f;
                         float mc = 0.f;
                         if (jv) {
-                            // this image's (hi, lo) half of each pixel's float4
-                            const float2* col = reinterpret_cast<const float2*>(src + j) + img;
-                            const int ld = 2 * ny;  // float2 per frame row of the interleaved split
+                            // this image's hi and lo: floats img and 2 + img of each pixel's float4
+                            const float* col = reinterpret_cast<const float*>(src + j) + img;
+                            const int ld = 4 * ny;  // floats per row of the interleaved split
 #pragma unroll
                             for (int i = 0; i < N8; ++i) {
                                 if (i < N) {
-                                    const float2 d = csub(__ldg(col + (size_t)i * ld), mhl);
+                                    const float2 d = make_float2(__ldg(col + (size_t)i * ld) - mhl.x,
+                                                                 __ldg(col + (size_t)i * ld + 2) - mhl.y);
                                     x[pj][cb][i] = (d.x + d.y) * gr[i];
                                     mc = fmaxf(mc, fabsf(x[pj][cb][i]));
                                 } else {
