@@ -577,6 +577,7 @@ __device__ __forceinline__ void k_interp_grid_body(const InterpArgs& a, const in
         // item / pw = umulhi(item, ceil(2^32 / pw)), exact for items below 2^32 / pw
         const unsigned mpw = 0xffffffffu / (unsigned)max(pw, 1) + 1u;
         __syncthreads();  // the previous tile's tables are consumed
+        int tb = 0;       // this thread's patch values hold an xmiss
         for (int e = threadIdx.x; e < ph * pw; e += kInterpThreads) {
             const int pr = (int)__umulhi((unsigned)e, mpw), pc = e - pr * pw;
             const int ra = r0 + pr, cb = c0 + pc;
@@ -585,7 +586,9 @@ __device__ __forceinline__ void k_interp_grid_body(const InterpArgs& a, const in
                                  : cdata_f(a.grid, a.gx, a.gy, ra, cb);
             const int pe = pr * kPatchC + pc;
             s_p[pe] = v;
-            s_pb[pe] = (v.x == kXmissF ? 1 : 0) | (v.y == kXmissF ? 2 : 0);
+            const unsigned char f = (v.x == kXmissF ? 1 : 0) | (v.y == kXmissF ? 2 : 0);
+            s_pb[pe] = f;
+            tb |= f;
         }
         // per-column and per-row stencil tables
         if (threadIdx.x < kTileC) {
@@ -608,7 +611,8 @@ __device__ __forceinline__ void k_interp_grid_body(const InterpArgs& a, const in
             for (int p = 0; p < 4; ++p)
                 s_rx[r][p] = oki ? keys_f(fabsf((float)(di - (iz + p - 1) * a.skip) * inv)) : 0.f;
         }
-        __syncthreads();
+        // a tile whose patch holds no xmiss (the usual case) skips the flags
+        const int tile_bad = __syncthreads_or(tb);
         // V[r][b] = sum_p rx[r][p] patch[iz_r - r0 + p][b]
         for (int e = threadIdx.x; e < kTileR * pw; e += kInterpThreads) {
             const int r = (int)__umulhi((unsigned)e, mpw), b = e - r * pw;
@@ -622,7 +626,7 @@ __device__ __forceinline__ void k_interp_grid_body(const InterpArgs& a, const in
                     const float rx = s_rx[r][p];
                     const int pe = (iz - r0 + p) * kPatchC + b;
                     const float2 c = s_p[pe];
-                    bad |= s_pb[pe];
+                    if (tile_bad) bad |= s_pb[pe];
                     v.x = fmaf(rx, c.x, v.x);
                     v.y = fmaf(rx, c.y, v.y);
                 }
@@ -664,7 +668,7 @@ __device__ __forceinline__ void k_interp_grid_body(const InterpArgs& a, const in
 #pragma unroll
                     for (int q = 0; q < 4; ++q) {
                         const float2 v = s_v[vb + q];
-                        bad |= s_vb[vb + q];
+                        if (tile_bad) bad |= s_vb[vb + q];
                         sx = fmaf(ry[c][q], v.x, sx);
                         sy = fmaf(ry[c][q], v.y, sy);
                     }
