@@ -30,6 +30,7 @@ from __future__ import annotations
 
 import argparse
 import ctypes as C
+import functools
 import json
 import os
 import statistics
@@ -178,6 +179,30 @@ def reduce_max(value: float, device=None) -> float:
     return float(t.item())
 
 
+@functools.lru_cache(maxsize=1)
+def cpu_model() -> str:
+    """The host CPU's model name and core count (lscpu, else /proc/cpuinfo)."""
+    name = ""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.lower().startswith("model name"):
+                name = ln.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    if not name:
+        try:
+            with open("/proc/cpuinfo") as fh:
+                for ln in fh:
+                    if ln.lower().startswith(("model name", "cpu part")):
+                        name = ln.split(":", 1)[1].strip()
+                        break
+        except OSError:
+            pass
+    return f"{name or 'unknown'}, {os.cpu_count()} cores"
+
+
 def oracle():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle as po
@@ -215,11 +240,11 @@ def run_reference(a):
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * dt / a.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "config": {"workload": WORKLOAD, "l2": "n/a (CPU)"},
-        "cpu_baseline": {"value": v, "unit": "windows/s", "cores": threads, "kind": "port",
+        "cpu_baseline": {"value": v, "unit": "windows/s", "cores": threads, "cpu": cpu_model(), "kind": "port",
                          "sample": "full frame per step (65,536 windows + interpolation), "
                                    f"{threads} threads, C restatement of flct.c over the "
                                    "project double FFT (FFTW unavailable)"},
-        "cpu_1core": {"value": one, "unit": "windows/s", "cores": 1, "kind": "port",
+        "cpu_1core": {"value": one, "unit": "windows/s", "cores": 1, "cpu": cpu_model(), "kind": "port",
                       "sample": "one full frame, 1 thread (the reference program is single-threaded)"},
         "e2e": {"value": v, "unit": "windows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -379,7 +404,7 @@ def config_record(name, desc, f1, f2, kw_gpu, kw_oracle, a, runner_args, po):
         t0 = time.perf_counter()
         po.velocity(f1, f2, nthreads=1, **kw_oracle)
         dt = time.perf_counter() - t0
-        rec["cpu_1core"] = {"windows_s": rec["windows_per_step"] / dt, "cores": 1, "kind": "port",
+        rec["cpu_1core"] = {"windows_s": rec["windows_per_step"] / dt, "cores": 1, "cpu": cpu_model(), "kind": "port",
                             "sample": "one full frame, " + CPU_SAMPLE}
     rec["tc_fp16_speedup_over_fp32_form"] = rec["forms"]["tc_fp16"]["windows_s"] / rec["forms"]["fp32"]["windows_s"]
     return rec
@@ -473,9 +498,9 @@ def run_batch(a, dev, flush, po):
             o = po.velocity(pairs[k][0], pairs[k][1], nthreads=os.cpu_count(), sigma=pairs[k][2]["sigma"])
             nwin += int((o[2] == 1).sum())
         allc = nwin / (time.perf_counter() - t0)
-        res["cpu_1core"] = {"windows_s": one, "cores": 1, "kind": "port",
+        res["cpu_1core"] = {"windows_s": one, "cores": 1, "cpu": cpu_model(), "kind": "port",
                             "sample": f"pairs {sample[:4]}, " + CPU_SAMPLE}
-        res["cpu_nproc"] = {"windows_s": allc, "cores": os.cpu_count(), "kind": "port",
+        res["cpu_nproc"] = {"windows_s": allc, "cores": os.cpu_count(), "cpu": cpu_model(), "kind": "port",
                             "sample": f"{len(sample)} of the 64 pairs, the oracle's windows on every host thread"}
     return res
 
@@ -515,7 +540,7 @@ def run_config5(a, runner_args, po):
         t0 = time.perf_counter()
         w = [po.extract_window(f1, f2, i, j, sigma=15.0) for i, j in pts[:400]]
         po.cross_cor_batch(np.stack([x for x, _ in w]), np.stack([y for _, y in w]), nthreads=1)
-        rec["cpu_1core"] = {"windows_s": 400 / (time.perf_counter() - t0), "cores": 1, "kind": "port",
+        rec["cpu_1core"] = {"windows_s": 400 / (time.perf_counter() - t0), "cores": 1, "cpu": cpu_model(), "kind": "port",
                             "sample": "400 of the sampled windows (extraction + cross_cor), " + CPU_SAMPLE}
     for form in ("fp32", "tc_fp16"):
         p = make_params(1.0, 1.0, 15.0, form=form)
@@ -714,7 +739,7 @@ def run_ours(a):
         t0 = time.perf_counter()
         po.velocity(f1, f2, nthreads=1, **kw)
         cdt = time.perf_counter() - t0
-        cpu = {"value": windows / cdt, "unit": "windows/s", "cores": 1, "kind": "port",
+        cpu = {"value": windows / cdt, "unit": "windows/s", "cores": 1, "cpu": cpu_model(), "kind": "port",
                "sample": "one full frame (65,536 windows + interpolation), 1 thread, C restatement "
                          "of flct.c over the project double FFT (FFTW unavailable)"}
 
