@@ -572,7 +572,7 @@ def run_warp(a, dev):
     uniform shift and warp_frac2d with a smooth per-pixel displacement
     (RMS 0.3 px), Mpixel/s per call through the host-buffer C ABI (copies
     included; the spectral warp is O(N^2) per pixel, so it dominates)."""
-    from pyflct_gb300 import synth
+    from pyflct_gb300 import _lib, synth
     from pyflct_gb300.flct import shift_frac2d, warp_frac2d
     rng = np.random.default_rng(20265)
     img = synth.kfield((512, 512), rng)
@@ -587,10 +587,23 @@ def run_warp(a, dev):
             fn()
         dt = (time.perf_counter() - t0) / reps
         out[name] = {"mpix_s": img.size / dt / 1e6, "ms_per_call": dt * 1e3}
+        if name == "warp_frac2d":
+            # the spectral sum on the tensor cores: the half-spectrum GEMM's
+            # executed flops (3 split products, 2 nx x 32 ceil((ny/2+1)/16)
+            # real K per pixel) and the reference loop's 8 nx ny flops per pixel
+            tm = _lib.context(dev.index or 0).timing()
+            nx, ny = img.shape
+            gemm = 6.0 * (2 * nx) * (32 * ((ny // 2 + 1 + 15) // 16)) * img.size
+            pk, src = peaks()
+            out[name].update({
+                "sum_ms": tm.ms_window, "dft_ms": tm.ms_prepass,
+                "tensor_tflops": gemm / (tm.ms_window * 1e-3) / 1e12,
+                "tensor_frac_of_bf16_peak": gemm / (tm.ms_window * 1e-3) / 1e12 / pk["bf16_tflops"],
+                "peak_source": f"{src} bf16_tflops (dense 16-bit rate)",
+                "reference_equivalent_tflops": 8.0 * nx * ny * img.size / (tm.ms_window * 1e-3) / 1e12})
     out["size"] = list(img.shape)
     out["note"] = "host buffers in and out, wall clock per call"
     # a 4096^2 uniform shift: power-of-two axes take the transform path
-    from pyflct_gb300 import _lib
     big = synth.kfield((4096, 4096), rng)
     shift_frac2d(big, 0.37, -2.6, device=dev.index or 0)
     walls, devs = [], []

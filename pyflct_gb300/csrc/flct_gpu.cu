@@ -122,12 +122,13 @@ struct flct_ctx {
     };
     Buf b_s1, b_s2, b_work, b_ctr, b_r1, b_r2, b_b1, b_b2, b_gvx, b_gvy, b_ix, b_iy;
     Buf b_f1, b_f2, b_vx, b_vy, b_vm, b_aux1, b_aux2, b_means, b_peaks, b_grid, b_peaks_h, b_re1, b_re2;
+    Buf b_whs, b_wmisc;  // warp_frac2d on the tensor cores: split spectrum stages, scale + status words
     std::vector<Buf*> all() {
         return {&b_s1,   &b_s2,   &b_work,   &b_ctr,    &b_r1,     &b_r2,     &b_b1,     &b_b2,
                 &b_gvx,  &b_gvy,  &b_ix,     &b_iy,     &b_f1,     &b_f2,     &b_vx,     &b_vy,
                 &b_vm,   &b_aux1, &b_aux2,   &b_means,  &b_peaks,  &b_grid,   &b_tc,     &bb_arena,
                 &bb_work, &bb_means, &bb_peaks, &bb_ctr, &bb_meta, &b_peaks_h, &bb_peaks_h, &b_re1, &b_re2,
-                &bb_multi};
+                &bb_multi, &b_whs,  &b_wmisc};
     }
     int bps[sizeof(kWin) / sizeof(kWin[0])][2] = {};
     int bps_tc[kNumTc][2] = {};
@@ -2562,15 +2563,31 @@ flct_status flct_gpu_warp_frac2d(flct_ctx* ctx, const double* arr, const double*
     CK(launch_warp_phase((const double*)ctx->b_f2.p, (const double*)ctx->b_vy.p, nx, ny, transp,
                          (float4*)ctx->b_means.p, st));
     CK(cudaEventRecord(ctx->ev[1], st));
-    CK(launch_warp_sum((const float2*)ctx->b_s2.p, (const float4*)ctx->b_means.p, nx, ny, (double*)ctx->b_vx.p, st));
+    // the spectral sum: tensor cores (split FP16, half spectrum) unless
+    // FLCT_WARP_SUM=fp32 asks for the FP32 CUDA-core kernel
+    const char* form = getenv("FLCT_WARP_SUM");
+    const bool tc = !(form && strcmp(form, "fp32") == 0);
+    unsigned wstatus = 0;
+    if (tc) {
+        ENSURE(ctx->b_whs, warp_tc_split_bytes(nx, ny));
+        ENSURE(ctx->b_wmisc, 64);
+        CK(launch_warp_sum_tc((const float2*)ctx->b_s2.p, (const float4*)ctx->b_means.p, nx, ny, ctx->b_whs.p,
+                              (unsigned*)ctx->b_wmisc.p, (double*)ctx->b_vx.p, st));
+    } else {
+        CK(launch_warp_sum((const float2*)ctx->b_s2.p, (const float4*)ctx->b_means.p, nx, ny, (double*)ctx->b_vx.p,
+                           st));
+    }
     CK(cudaEventRecord(ctx->ev[2], st));
     CK(cudaMemcpyAsync(out, ctx->b_vx.p, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (tc) CK(cudaMemcpyAsync(&wstatus, (unsigned*)ctx->b_wmisc.p + 1, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     ctx->timing = flct_timing{};
-    ctx->timing.launches = 6;
+    ctx->timing.launches = tc ? 8 : 6;
     ctx->timing.ms_prepass = ev_ms(ctx->ev[0], ctx->ev[1]);
     ctx->timing.ms_window = ev_ms(ctx->ev[1], ctx->ev[2]);
     ctx->timing.ms_total = ev_ms(ctx->ev[0], ctx->ev[2]);
+    if (wstatus & kStatusTimeout)
+        return fail(ctx, FLCT_ERR_TIMEOUT, "a tensor-core stage of the warp sum did not complete within its wait limit");
     return FLCT_OK;
 }
 

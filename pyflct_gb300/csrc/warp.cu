@@ -24,6 +24,7 @@
 // Arithmetic is FP32 on the CUDA cores except the FP64 phase bases and the
 // circulant / twiddle tables.
 #include "warp.cuh"
+#include "warp_math.cuh"
 
 #include <algorithm>
 
@@ -40,13 +41,6 @@ __global__ void k_twiddles(int L, int sign, float2* __restrict__ tw) {
     double s, c;
     sincospi(2.0 * (double)k / (double)L, &s, &c);
     tw[k] = make_float2((float)c, (float)(sign * s));
-}
-
-// Integer wavenumber of FFT index k (make_freq, warp.c:316-360).
-__device__ __forceinline__ int freq_of(int k, int n) {
-    const int h = n / 2;
-    if (n % 2 == 0) return (k <= h) ? k : k - n;
-    return (k <= h) ? k : k - n;
 }
 
 // FP64 tables for the circulant vector of the uniform shift along an axis of
@@ -299,18 +293,6 @@ __global__ void k_warp_phase(const double* __restrict__ delx, const double* __re
         const float txh = (float)tx, tyh = (float)ty;
         ph[k] = make_float4(txh, (float)(tx - (double)txh), tyh, (float)(ty - (double)tyh));
     }
-}
-
-// cos/sin of 2 pi * frac(kf * (h + l)) with kf an integer wavenumber:
-// the product is formed exactly enough in float-float (fma error term) and
-// reduced to (-1/2, 1/2] turn before the trigonometric evaluation.
-__device__ __forceinline__ float2 turn_cs(float kf, float h, float l) {
-    const float p = kf * h;
-    const float e = fmaf(kf, h, -p);       // exact error of the product
-    const float fr = (p - rintf(p)) + fmaf(kf, l, e);
-    float s, c;
-    sincospif(2.0f * fr, &s, &c);
-    return make_float2(c, s);
 }
 
 // Tile: 64 pixels x 128 wavenumbers ii, contraction over jj in chunks of 16.

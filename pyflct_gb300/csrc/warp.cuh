@@ -1,6 +1,7 @@
 // warp.cuh -- launchers for warp.cu (uniform shift and non-uniform warp).
 #pragma once
 #include <cuda_runtime.h>
+#include <stddef.h>
 
 namespace flct {
 
@@ -24,5 +25,11 @@ cudaError_t launch_real_part(const float2* in, long n, double* out, cudaStream_t
 cudaError_t launch_warp_phase(const double* delx, const double* dely, int nx, int ny, int transp, float4* ph,
                               cudaStream_t st);
 cudaError_t launch_warp_sum(const float2* F, const float4* ph, int nx, int ny, double* out, cudaStream_t st);
+// the same sum on the tensor cores (split FP16, half spectrum): hs is
+// warp_tc_split_bytes(nx, ny) of scratch, misc two words (the spectrum's
+// largest |component| and the status word, misc[1]: kStatusTimeout bits)
+size_t warp_tc_split_bytes(int nx, int ny);
+cudaError_t launch_warp_sum_tc(const float2* F, const float4* ph, int nx, int ny, void* hs, unsigned* misc,
+                               double* out, cudaStream_t st);
 
 }  // namespace flct

@@ -2,10 +2,12 @@
 against the FP64 oracle and the reference's golden outputs.
 
 The GPU evaluates the transforms in FP32 with FP64 phase bases and FP64
-circulant/twiddle tables.  Tolerances, relative to max |image|: warp_frac2d
-1.5e-6 (measured up to 9.3e-7 at 512^2), shift_frac2d 4e-6 (measured up to
-1.9e-6 at 512^2); against the reference's golden files, which are
-float32-rounded, 2e-6.
+circulant/twiddle tables; warp_frac2d's spectral sum runs on the tensor
+cores (split FP16) by default, or as FP32 on the CUDA cores with
+FLCT_WARP_SUM=fp32.  Tolerances, relative to max |image|: warp_frac2d 1e-6
+(measured up to 7.7e-7 at 256^2 for the tensor-core sum, 6.4e-7 over the
+test shapes), shift_frac2d 4e-6 (measured up to 1.9e-6 at 512^2); against
+the reference's golden files, which are float32-rounded, 2e-6.
 """
 import numpy as np
 import pytest
@@ -15,7 +17,7 @@ from _golden import load
 
 pytestmark = pytest.mark.gpu
 REL = 2e-6        # against the float32-rounded golden files
-REL_WARP = 1.5e-6
+REL_WARP = 1e-6
 REL_SHIFT = 4e-6
 
 
@@ -82,6 +84,32 @@ def test_warp_sizes(shape, transp):
     got = warp_frac2d(img, dfast, dslow, transp)
     ref = po.warp_frac2d(img, dfast, dslow, transp)
     assert close(got, ref, np.abs(img).max(), REL_WARP)
+
+
+@pytest.mark.parametrize("shape", [(300, 130), (129, 257), (130, 33), (2, 2), (1, 4), (4, 1), (3, 5)])
+@pytest.mark.parametrize("form", ["tc", "fp32"])
+def test_warp_sum_forms(shape, form, monkeypatch):
+    """Both spectral-sum kernels against the oracle: the tensor-core form
+    (half spectrum, split FP16) over several 128-row chunks and stage-ring
+    wraps, odd and even axes (Nyquist row and column), degenerate axes; the
+    FP32 CUDA-core form (FLCT_WARP_SUM=fp32) on the same inputs."""
+    if form == "fp32":
+        monkeypatch.setenv("FLCT_WARP_SUM", "fp32")
+    else:
+        monkeypatch.delenv("FLCT_WARP_SUM", raising=False)
+    from pyflct_gb300 import synth
+    from pyflct_gb300.flct import warp_frac2d
+    rng = np.random.default_rng(shape[0] * 131 + shape[1])
+    if min(shape) >= 8:
+        img = synth.kfield(shape, rng)
+        dfast, dslow = synth.smooth_shift(shape, rng, rms=1.5)
+    else:
+        img = rng.standard_normal(shape) + 2.0
+        dfast, dslow = rng.uniform(-2, 2, shape), rng.uniform(-2, 2, shape)
+    for transp in (1, 0):
+        got = warp_frac2d(img, dfast, dslow, transp)
+        ref = po.warp_frac2d(img, dfast, dslow, transp)
+        assert close(got, ref, np.abs(img).max(), REL_WARP)
 
 
 def test_warp_dispatch_and_constant_field():
