@@ -29,15 +29,16 @@
 // order is chosen to keep large partial sums out of most of the chain: the
 // stages of a chunk run from the highest columns down, each K step adds the
 // two cross products before hi*hi, and the DC term F[0][0] (the largest)
-// bypasses the GEMM and is added in FP64; the epilogue sums each 16-row
+// bypasses the GEMM and is added in FP64; the epilogue sums each 8-row
 // group in FP32 and the groups in FP64.
 //
 // CTA: 256 pixels (two 128-lane accumulators of 256 columns each, all 512
-// TMEM columns), 9 warps: warps 0-7 generate the A stages (one pixel per
-// thread: exp(2 pi i c ty) as base(16 kc) x step(j), both from exact
-// float-float turn reductions) and run the epilogue of their own TMEM lane;
-// lane 0 of warp 8 copies the pre-split B stages (one 32 KB bulk copy each)
-// and issues the MMAs.  Three 64 KB stages in shared memory.  Every wait is
+// TMEM columns), 17 warps: warps 0-15 generate the A stages (two threads
+// per pixel, 8 columns each: exp(2 pi i c ty) as base(16 kc) x step(j),
+// both from exact float-float turn reductions), warps 0-7 also run the
+// epilogue of their own TMEM lane (row phases likewise as base x step per
+// 8 rows); lane 0 of warp 16 copies the pre-split B stages (one 32 KB bulk
+// copy each) and issues the MMAs.  Three 64 KB stages in shared memory.  Every wait is
 // bounded (2 s); a wait that runs out sets the status word's timeout bit,
 // the CTA drains its own copies and MMAs (bounded), frees its tensor memory
 // and returns.
@@ -54,6 +55,8 @@ namespace flct {
 namespace {
 
 constexpr int kWtPx = 256;                       // pixels per CTA
+constexpr int kWtGen = 16;                       // generator warps: two threads per pixel
+constexpr int kWtThreads = 32 * (kWtGen + 1);    // + the copy / MMA warp
 constexpr int kWtStages = 3;
 constexpr int kWtAT = 128 * 32 * 2;              // one 128-pixel A tile (hi or lo), bytes
 constexpr int kWtBH = 256 * 32 * 2;              // the B tile's hi (or lo) half, bytes
@@ -80,15 +83,16 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
     return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
 }
 
-__device__ __forceinline__ unsigned pack_h2(__half a, __half b) {
-    return (unsigned)__half_as_ushort(a) | ((unsigned)__half_as_ushort(b) << 16);
+__device__ __forceinline__ unsigned h2_bits(__half2 h) {
+    return (unsigned)__half_as_ushort(__low2half(h)) | ((unsigned)__half_as_ushort(__high2half(h)) << 16);
 }
 
 // hi / lo FP16 halves of two values, packed (first value in the low half)
 __device__ __forceinline__ void split2(float v0, float v1, unsigned& hi, unsigned& lo) {
-    const __half h0 = __float2half_rn(v0), h1 = __float2half_rn(v1);
-    hi = pack_h2(h0, h1);
-    lo = pack_h2(__float2half_rn(v0 - __half2float(h0)), __float2half_rn(v1 - __half2float(h1)));
+    const __half2 h = __floats2half2_rn(v0, v1);
+    const float2 f = __half22float2(h);
+    hi = h2_bits(h);
+    lo = h2_bits(__floats2half2_rn(v0 - f.x, v1 - f.y));
 }
 
 __device__ __forceinline__ void mbar_arrive(uint64_t* b) {
@@ -147,7 +151,7 @@ __global__ void k_wt_hsplit(const float2* __restrict__ F, int nx, int ny, int nk
     }
 }
 
-__global__ void __launch_bounds__(288, 1)
+__global__ void __launch_bounds__(kWtThreads, 1)
     k_wt_sum(const unsigned char* __restrict__ hs, const float4* __restrict__ ph, const float2* __restrict__ F,
              const unsigned* __restrict__ mx, int nx, int ny, int nq, int nkc, double normfac,
              double* __restrict__ out, unsigned* __restrict__ status) {
@@ -162,7 +166,7 @@ __global__ void __launch_bounds__(288, 1)
     const int t = threadIdx.x, w = t >> 5, lane = t & 31;
     if (t == 0) {
         for (int s = 0; s < kWtStages; ++s) {
-            tc::mbar_init(&s_fa[s], 8);
+            tc::mbar_init(&s_fa[s], kWtGen);
             tc::mbar_init(&s_fb[s], 1);
             tc::mbar_init(&s_em[s], 1);
         }
@@ -172,7 +176,7 @@ __global__ void __launch_bounds__(288, 1)
         s_abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (w == 8) tc::tmem_alloc(&s_tmem, 512);
+    if (w == kWtGen) tc::tmem_alloc(&s_tmem, 512);
     tc::fence_before();
     __syncthreads();
     tc::fence_after();
@@ -201,7 +205,7 @@ __global__ void __launch_bounds__(288, 1)
         }
     };
 
-    if (w == 8) {
+    if (w == kWtGen) {
         if (lane == 0) {
             bool ok = true;
             int gc = 0, gm = 0;  // stages copied, stages consumed
@@ -263,15 +267,19 @@ __global__ void __launch_bounds__(288, 1)
         }
         __syncwarp();
     } else {
-        const int T = w >> 2, m = t & 127;
+        // pixel t % 256 of the CTA; half h generates columns 8h .. 8h+7 of
+        // every stage; the threads of half 0 also run the epilogue (their
+        // warp w < 8 reads TMEM lane quadrant w % 4 of tile w / 4)
+        const int pix = t & (kWtPx - 1), h = t / kWtPx;
+        const int T = pix >> 7, m = pix & 127;
         const long npx = (long)nx * ny;
-        const long p = (long)blockIdx.x * kWtPx + t;
+        const long p = (long)blockIdx.x * kWtPx + pix;
         const bool live = p < npx;
         const float4 pb = live ? ph[p] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         const float sc = wt_scale(*mx);
-        float2 S[16];  // exp(2 pi i j ty), j < 16
+        float2 S[8];  // exp(2 pi i (8h + j) ty), j < 8
 #pragma unroll
-        for (int j = 0; j < 16; ++j) S[j] = turn_cs((float)j, pb.z, pb.w);
+        for (int j = 0; j < 8; ++j) S[j] = turn_cs((float)(8 * h + j), pb.z, pb.w);
         double acc = 0.0;
         bool ok = true;
         unsigned char* arow = sm + T * kWtAT + kmaj_off(m, 0);
@@ -283,18 +291,26 @@ __global__ void __launch_bounds__(288, 1)
             if (!__shfl_sync(0xffffffffu, done, 0)) return false;
             tc::fence_after();
             const uint32_t tb = tmem + lane_base + (uint32_t)(T * 256);
+            float2 Sx[8];  // exp(2 pi i j tx), j < 8
+#pragma unroll
+            for (int j = 0; j < 8; ++j) Sx[j] = turn_cs((float)j, pb.x, pb.y);
 #pragma unroll 1
-            for (int r0 = 0; r0 < 128; r0 += 16) {
-                if (q * 128 + r0 >= nx) break;
-                float gr[16], gi[16];
-                tc::tmem_ld<16>(tb + r0, gr);
-                tc::tmem_ld<16>(tb + 128 + r0, gi);
+            for (int r0 = 0; r0 < 128; r0 += 8) {
+                const int i0 = q * 128 + r0;
+                if (i0 >= nx) break;
+                // rows i0 .. i0+7 have wavenumbers kx(i0) + j unless the
+                // wrap to negative wavenumbers falls inside the group
+                const bool run = i0 + 7 <= nx / 2 || i0 > nx / 2;
+                const float2 xb = turn_cs((float)freq_of(i0, nx), pb.x, pb.y);
+                float gr[8], gi[8];
+                tc::tmem_ld<8>(tb + r0, gr);
+                tc::tmem_ld<8>(tb + 128 + r0, gi);
                 float part = 0.0f;
 #pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    const int ii = q * 128 + r0 + j;
+                for (int j = 0; j < 8; ++j) {
+                    const int ii = i0 + j;
                     if (ii < nx) {
-                        const float2 ex = turn_cs((float)freq_of(ii, nx), pb.x, pb.y);
+                        const float2 ex = run ? cmul(xb, Sx[j]) : turn_cs((float)freq_of(ii, nx), pb.x, pb.y);
                         if (2 * ii == nx) {
                             // the Nyquist row (weight 1 in every column)
                             float2 a0 = F[(size_t)ii * ny];
@@ -332,38 +348,34 @@ __global__ void __launch_bounds__(288, 1)
                 // stage kc of a chunk holds columns 16 (nkc - 1 - kc) .. +15
                 const float2 base = turn_cs((float)((nkc - 1 - kc) * 16), pb.z, pb.w);
                 unsigned char* dst = arow + s * kWtStage;
+                unsigned rh[4], rl[4], ih[4], il[4];
 #pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    unsigned rh[4], rl[4], ih[4], il[4];
-#pragma unroll
-                    for (int e = 0; e < 8; e += 2) {
-                        const float2 v0 = cmul(base, S[8 * h + e]);
-                        const float2 v1 = cmul(base, S[8 * h + e + 1]);
-                        split2(v0.x, v1.x, rh[e / 2], rl[e / 2]);
-                        split2(v0.y, v1.y, ih[e / 2], il[e / 2]);
-                    }
-                    *reinterpret_cast<uint4*>(dst + h * 128) = make_uint4(rh[0], rh[1], rh[2], rh[3]);
-                    *reinterpret_cast<uint4*>(dst + (2 + h) * 128) = make_uint4(ih[0], ih[1], ih[2], ih[3]);
-                    *reinterpret_cast<uint4*>(dst + 2 * kWtAT + h * 128) = make_uint4(rl[0], rl[1], rl[2], rl[3]);
-                    *reinterpret_cast<uint4*>(dst + 2 * kWtAT + (2 + h) * 128) =
-                        make_uint4(il[0], il[1], il[2], il[3]);
+                for (int e = 0; e < 8; e += 2) {
+                    const float2 v0 = cmul(base, S[e]);
+                    const float2 v1 = cmul(base, S[e + 1]);
+                    split2(v0.x, v1.x, rh[e / 2], rl[e / 2]);
+                    split2(v0.y, v1.y, ih[e / 2], il[e / 2]);
                 }
+                *reinterpret_cast<uint4*>(dst + h * 128) = make_uint4(rh[0], rh[1], rh[2], rh[3]);
+                *reinterpret_cast<uint4*>(dst + (2 + h) * 128) = make_uint4(ih[0], ih[1], ih[2], ih[3]);
+                *reinterpret_cast<uint4*>(dst + 2 * kWtAT + h * 128) = make_uint4(rl[0], rl[1], rl[2], rl[3]);
+                *reinterpret_cast<uint4*>(dst + 2 * kWtAT + (2 + h) * 128) = make_uint4(il[0], il[1], il[2], il[3]);
                 tc::fence_async_smem();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&s_fa[s]);
                 // the previous chunk's epilogue, once this chunk's first
                 // stages are queued for the tensor cores
-                if (q > 0 && kc == (nkc > 1 ? 1 : 0)) ok = epilogue(q - 1);
+                if (h == 0 && q > 0 && kc == (nkc > 1 ? 1 : 0)) ok = epilogue(q - 1);
             }
         }
-        if (ok) ok = epilogue(nq - 1);
-        if (ok && live) out[p] = acc * (normfac / (double)sc) + (double)F[0].x * normfac;
+        if (ok && h == 0) ok = epilogue(nq - 1);
+        if (ok && live && h == 0) out[p] = acc * (normfac / (double)sc) + (double)F[0].x * normfac;
         if (!ok && lane == 0) atomicOr(status, kStatusTimeout);
     }
     tc::fence_before();
     __syncthreads();
     tc::fence_after();
-    if (w == 8) tc::tmem_dealloc(tmem, 512);
+    if (w == kWtGen) tc::tmem_dealloc(tmem, 512);
 }
 
 }  // namespace
@@ -387,7 +399,7 @@ cudaError_t launch_warp_sum_tc(const float2* F, const float4* ph, int nx, int ny
                                                                                    reinterpret_cast<uint4*>(hs));
     e = cudaFuncSetAttribute(k_wt_sum, cudaFuncAttributeMaxDynamicSharedMemorySize, kWtSmem);
     if (e != cudaSuccess) return e;
-    k_wt_sum<<<(unsigned)((npx + kWtPx - 1) / kWtPx), 288, kWtSmem, st>>>(
+    k_wt_sum<<<(unsigned)((npx + kWtPx - 1) / kWtPx), kWtThreads, kWtSmem, st>>>(
         reinterpret_cast<const unsigned char*>(hs), ph, F, misc, nx, ny, nq, nkc, 1.0 / (double)npx, out, misc + 1);
     return cudaGetLastError();
 }
