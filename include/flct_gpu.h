@@ -166,7 +166,11 @@ FLCT_API flct_status flct_gpu_interpcc2d(flct_ctx *ctx, const double *fdata,
                                 const double *ywant, int nyi, double *out);
 
 /* shift_frac2d / warp_frac2d (host buffers), transp as in the reference
- * (1 for the CLI's transposed storage). */
+ * (1 for the CLI's transposed storage).  warp_frac2d's per-pixel spectral
+ * sum runs on the tensor cores (split FP16 over the half spectrum, within
+ * 1e-6 of max |arr| of the FP64 result); the environment variable
+ * FLCT_WARP_SUM=fp32, read at each call, selects the FP32 CUDA-core sum.
+ * A tensor-core wait that runs out returns FLCT_ERR_TIMEOUT. */
 FLCT_API flct_status flct_gpu_shift_frac2d(flct_ctx *ctx, const double *arr,
                                   double delx, double dely, double *out,
                                   int nx, int ny, int transp);
