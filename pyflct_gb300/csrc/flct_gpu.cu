@@ -2555,11 +2555,18 @@ flct_status flct_gpu_warp_frac2d(flct_ctx* ctx, const double* arr, const double*
     CK(cudaMemcpyAsync(ctx->b_f2.p, delx, n * sizeof(double), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(ctx->b_vy.p, dely, n * sizeof(double), cudaMemcpyHostToDevice, st));
     CK(cudaEventRecord(ctx->ev[0], st));
-    // F = forward DFT of the image (warp.c:899-934)
-    CK(launch_twiddles(nx, -1, twx, st));
-    CK(launch_twiddles(ny, -1, twy, st));
-    CK(launch_axis_fast(1, true, ctx->b_f1.p, nx, ny, twy, (float2*)ctx->b_s1.p, st));
-    CK(launch_axis_slow(1, (const float2*)ctx->b_s1.p, ny, nx, twx, (float2*)ctx->b_s2.p, st));
+    // F = forward DFT of the image (warp.c:899-934): FFTs along both axes
+    // when both are powers of two (64 .. kWarpMaxAxis), else DFT matrices
+    const bool fft = shift_fft_axis(nx) && shift_fft_axis(ny);
+    if (fft) {
+        CK(launch_dft2_fft((const double*)ctx->b_f1.p, nx, ny, twx, (float2*)ctx->b_s1.p, (float2*)ctx->b_s2.p,
+                           ctx->nsm, st));
+    } else {
+        CK(launch_twiddles(nx, -1, twx, st));
+        CK(launch_twiddles(ny, -1, twy, st));
+        CK(launch_axis_fast(1, true, ctx->b_f1.p, nx, ny, twy, (float2*)ctx->b_s1.p, st));
+        CK(launch_axis_slow(1, (const float2*)ctx->b_s1.p, ny, nx, twx, (float2*)ctx->b_s2.p, st));
+    }
     CK(launch_warp_phase((const double*)ctx->b_f2.p, (const double*)ctx->b_vy.p, nx, ny, transp,
                          (float4*)ctx->b_means.p, st));
     CK(cudaEventRecord(ctx->ev[1], st));
@@ -2582,7 +2589,7 @@ flct_status flct_gpu_warp_frac2d(flct_ctx* ctx, const double* arr, const double*
     if (tc) CK(cudaMemcpyAsync(&wstatus, (unsigned*)ctx->b_wmisc.p + 1, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     ctx->timing = flct_timing{};
-    ctx->timing.launches = tc ? 8 : 6;
+    ctx->timing.launches = (fft ? 6 : 4) + 1 + (tc ? 3 : 1);
     ctx->timing.ms_prepass = ev_ms(ctx->ev[0], ctx->ev[1]);
     ctx->timing.ms_window = ev_ms(ctx->ev[1], ctx->ev[2]);
     ctx->timing.ms_total = ev_ms(ctx->ev[0], ctx->ev[2]);

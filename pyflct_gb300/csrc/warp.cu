@@ -192,8 +192,10 @@ __global__ void __launch_bounds__(256) k_axis_slow(const float2* __restrict__ in
 // positions), X[k] *= ph[k], then the inverse by radix-2 decimation in
 // frequency (natural order in, bit-reversed out), read back in natural
 // order, times `scale`.  tw[t] = exp(-2 pi i t / L) (FP64, rounded once);
-// ph[k] = exp(i 2 pi kf darg) in FP64 from k_shift_tables.
-template <bool REAL_IN>
+// ph[k] = exp(i 2 pi kf darg) in FP64 from k_shift_tables.  FWD_ONLY stops
+// after the forward transform and writes X (natural order; ph and scale
+// unused): warp_frac2d's spectrum.
+template <bool REAL_IN, bool FWD_ONLY = false>
 __global__ void __launch_bounds__(512) k_shift_lines_fft(const void* __restrict__ in_, int nlines, int L, int logL,
                                                          const float2* __restrict__ tw,
                                                          const double2* __restrict__ ph, float scale,
@@ -221,28 +223,32 @@ __global__ void __launch_bounds__(512) k_shift_lines_fft(const void* __restrict_
             }
             __syncthreads();
         }
-        for (int k = threadIdx.x; k < L; k += blockDim.x) {
-            const double2 p = ph[k];
-            const float px = (float)p.x, py = (float)p.y;
-            const float2 a = x[k];
-            x[k] = make_float2(a.x * px - a.y * py, a.x * py + a.y * px);
-        }
-        __syncthreads();
-        for (int m = half; m >= 1; m >>= 1) {
-            const int ts = half / m;
-            for (int b = threadIdx.x; b < half; b += blockDim.x) {
-                const int j = b & (m - 1), k = ((b - j) << 1) + j;
-                const float2 w = __ldg(tw + j * ts);
-                const float2 u = x[k], v = x[k + m];
-                const float2 d = make_float2(u.x - v.x, u.y - v.y);
-                x[k] = make_float2(u.x + v.x, u.y + v.y);
-                x[k + m] = make_float2(d.x * w.x + d.y * w.y, d.y * w.x - d.x * w.y);  // d exp(+2 pi i j / 2m)
+        if constexpr (FWD_ONLY) {
+            for (int k = threadIdx.x; k < L; k += blockDim.x) out[(size_t)line * L + k] = x[k];
+        } else {
+            for (int k = threadIdx.x; k < L; k += blockDim.x) {
+                const double2 p = ph[k];
+                const float px = (float)p.x, py = (float)p.y;
+                const float2 a = x[k];
+                x[k] = make_float2(a.x * px - a.y * py, a.x * py + a.y * px);
             }
             __syncthreads();
-        }
-        for (int k = threadIdx.x; k < L; k += blockDim.x) {
-            const float2 v = x[__brev((unsigned)k) >> (32 - logL)];
-            out[(size_t)line * L + k] = make_float2(v.x * scale, v.y * scale);
+            for (int m = half; m >= 1; m >>= 1) {
+                const int ts = half / m;
+                for (int b = threadIdx.x; b < half; b += blockDim.x) {
+                    const int j = b & (m - 1), k = ((b - j) << 1) + j;
+                    const float2 w = __ldg(tw + j * ts);
+                    const float2 u = x[k], v = x[k + m];
+                    const float2 d = make_float2(u.x - v.x, u.y - v.y);
+                    x[k] = make_float2(u.x + v.x, u.y + v.y);
+                    x[k + m] = make_float2(d.x * w.x + d.y * w.y, d.y * w.x - d.x * w.y);  // d exp(+2 pi i j / 2m)
+                }
+                __syncthreads();
+            }
+            for (int k = threadIdx.x; k < L; k += blockDim.x) {
+                const float2 v = x[__brev((unsigned)k) >> (32 - logL)];
+                out[(size_t)line * L + k] = make_float2(v.x * scale, v.y * scale);
+            }
         }
         __syncthreads();  // the next line overwrites x
     }
@@ -447,6 +453,33 @@ cudaError_t launch_shift_fft(const double* in, int nx, int ny, double dxarg, dou
     k_shift_lines_fft<false><<<std::min(ny, nsm * 4), std::min(512, nx / 2), smx, st>>>(
         buf2, ny, nx, log2i(nx), twx, phx, 1.0f / (float)nx, buf1);
     k_transpose_re<<<dim3((nx + 31) / 32, (ny + 31) / 32), dim3(32, 8), 0, st>>>(buf1, ny, nx, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dft2_fft(const double* in, int nx, int ny, float2* tw, float2* buf1, float2* F, int nsm,
+                           cudaStream_t st) {
+    auto log2i = [](int n) {
+        int l = 0;
+        while ((1 << l) < n) ++l;
+        return l;
+    };
+    float2* twx = tw;
+    float2* twy = tw + nx;
+    k_twiddles<<<(nx + 255) / 256, 256, 0, st>>>(nx, -1, twx);
+    k_twiddles<<<(ny + 255) / 256, 256, 0, st>>>(ny, -1, twy);
+    const size_t smy = (size_t)ny * sizeof(float2), smx = (size_t)nx * sizeof(float2);
+    cudaError_t e;
+    e = cudaFuncSetAttribute(k_shift_lines_fft<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smy);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_shift_lines_fft<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
+    if (e != cudaSuccess) return e;
+    // rows (fast axis), then the slow axis as rows of the transpose, then back
+    k_shift_lines_fft<true, true><<<std::min(nx, nsm * 4), std::min(512, ny / 2), smy, st>>>(
+        in, nx, ny, log2i(ny), twy, nullptr, 1.0f, buf1);
+    k_transpose_c<<<dim3((ny + 31) / 32, (nx + 31) / 32), dim3(32, 8), 0, st>>>(buf1, nx, ny, F);
+    k_shift_lines_fft<false, true><<<std::min(ny, nsm * 4), std::min(512, nx / 2), smx, st>>>(
+        F, ny, nx, log2i(nx), twx, nullptr, 1.0f, buf1);
+    k_transpose_c<<<dim3((nx + 31) / 32, (ny + 31) / 32), dim3(32, 8), 0, st>>>(buf1, ny, nx, F);
     return cudaGetLastError();
 }
 

@@ -21,6 +21,11 @@ cudaError_t launch_twiddles(int L, int sign, float2* tw, cudaStream_t st);
 bool shift_fft_axis(int n);
 cudaError_t launch_shift_fft(const double* in, int nx, int ny, double dxarg, double dyarg, double2* scratch,
                              float2* tw, float2* buf1, float2* buf2, double* out, int nsm, cudaStream_t st);
+// F = forward 2-D DFT of a real nx x ny image by transforms, both axes
+// shift_fft_axis: tw nx + ny float2, buf1 nx * ny float2 scratch, F nx * ny
+// float2 (natural [ii][jj] order)
+cudaError_t launch_dft2_fft(const double* in, int nx, int ny, float2* tw, float2* buf1, float2* F, int nsm,
+                            cudaStream_t st);
 cudaError_t launch_real_part(const float2* in, long n, double* out, cudaStream_t st);
 cudaError_t launch_warp_phase(const double* delx, const double* dely, int nx, int ny, int transp, float4* ph,
                               cudaStream_t st);

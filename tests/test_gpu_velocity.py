@@ -221,7 +221,7 @@ def test_config5_4096_sigma15_sampled():
     ref = po.warp_frac2d(f1[crop], dfast[crop], dslow[crop])
     err = np.abs(got - ref).max() / np.abs(f1[crop]).max()
     print("config5 warp 512^2 crop max |d| / max |image|", err)
-    assert err <= 1.5e-6
+    assert err <= 1e-6  # measured 9.2e-7 (tensor-core sum, spectrum by FFTs)
 
 
 def test_config2_full_size_512_threshold():

@@ -4,10 +4,11 @@ against the FP64 oracle and the reference's golden outputs.
 The GPU evaluates the transforms in FP32 with FP64 phase bases and FP64
 circulant/twiddle tables; warp_frac2d's spectral sum runs on the tensor
 cores (split FP16) by default, or as FP32 on the CUDA cores with
-FLCT_WARP_SUM=fp32.  Tolerances, relative to max |image|: warp_frac2d 1e-6
-(measured up to 7.7e-7 at 256^2 for the tensor-core sum, 6.4e-7 over the
-test shapes), shift_frac2d 4e-6 (measured up to 1.9e-6 at 512^2); against
-the reference's golden files, which are float32-rounded, 2e-6.
+FLCT_WARP_SUM=fp32; power-of-two axes take warp_frac2d's spectrum by FFTs.
+Tolerances, relative to max |image|: warp_frac2d 1e-6 (measured up to
+6.5e-7 over the test shapes with the tensor-core sum), shift_frac2d 4e-6
+(measured up to 1.9e-6 at 512^2); against the reference's golden files,
+which are float32-rounded, 2e-6.
 """
 import numpy as np
 import pytest
@@ -86,13 +87,14 @@ def test_warp_sizes(shape, transp):
     assert close(got, ref, np.abs(img).max(), REL_WARP)
 
 
-@pytest.mark.parametrize("shape", [(300, 130), (129, 257), (130, 33), (2, 2), (1, 4), (4, 1), (3, 5)])
+@pytest.mark.parametrize("shape", [(300, 130), (129, 257), (130, 33), (128, 256), (64, 64), (2, 2), (1, 4), (4, 1), (3, 5)])
 @pytest.mark.parametrize("form", ["tc", "fp32"])
 def test_warp_sum_forms(shape, form, monkeypatch):
     """Both spectral-sum kernels against the oracle: the tensor-core form
     (half spectrum, split FP16) over several 128-row chunks and stage-ring
     wraps, odd and even axes (Nyquist row and column), degenerate axes; the
-    FP32 CUDA-core form (FLCT_WARP_SUM=fp32) on the same inputs."""
+    FP32 CUDA-core form (FLCT_WARP_SUM=fp32) on the same inputs.  Power-of-
+    two shapes take the spectrum by FFTs, the others by DFT matrices."""
     if form == "fp32":
         monkeypatch.setenv("FLCT_WARP_SUM", "fp32")
     else:
