@@ -2578,8 +2578,10 @@ flct_status flct_gpu_warp_frac2d(flct_ctx* ctx, const double* arr, const double*
     if (tc) {
         ENSURE(ctx->b_whs, warp_tc_split_bytes(nx, ny));
         ENSURE(ctx->b_wmisc, 64);
+        unsigned long long stall_ns = 0;  // test hook: see k_wt_sum
+        if (const char* w = getenv("FLCT_TEST_WARP_STALL_NS")) stall_ns = strtoull(w, nullptr, 10);
         CK(launch_warp_sum_tc((const float2*)ctx->b_s2.p, (const float4*)ctx->b_means.p, nx, ny, ctx->b_whs.p,
-                              (unsigned*)ctx->b_wmisc.p, (double*)ctx->b_vx.p, st));
+                              (unsigned*)ctx->b_wmisc.p, (double*)ctx->b_vx.p, st, stall_ns));
     } else {
         CK(launch_warp_sum((const float2*)ctx->b_s2.p, (const float4*)ctx->b_means.p, nx, ny, (double*)ctx->b_vx.p,
                            st));

@@ -32,9 +32,10 @@ cudaError_t launch_warp_phase(const double* delx, const double* dely, int nx, in
 cudaError_t launch_warp_sum(const float2* F, const float4* ph, int nx, int ny, double* out, cudaStream_t st);
 // the same sum on the tensor cores (split FP16, half spectrum): hs is
 // warp_tc_split_bytes(nx, ny) of scratch, misc two words (the spectrum's
-// largest |component| and the status word, misc[1]: kStatusTimeout bits)
+// largest |component| and the status word, misc[1]: kStatusTimeout bits);
+// stall_ns > 0 is a test hook (the first MMA wait gives up after stall_ns)
 size_t warp_tc_split_bytes(int nx, int ny);
 cudaError_t launch_warp_sum_tc(const float2* F, const float4* ph, int nx, int ny, void* hs, unsigned* misc,
-                               double* out, cudaStream_t st);
+                               double* out, cudaStream_t st, unsigned long long stall_ns = 0);
 
 }  // namespace flct

@@ -154,12 +154,12 @@ __global__ void k_wt_hsplit(const float2* __restrict__ F, int nx, int ny, int nk
 __global__ void __launch_bounds__(kWtThreads, 1)
     k_wt_sum(const unsigned char* __restrict__ hs, const float4* __restrict__ ph, const float2* __restrict__ F,
              const unsigned* __restrict__ mx, int nx, int ny, int nq, int nkc, double normfac,
-             double* __restrict__ out, unsigned* __restrict__ status) {
+             double* __restrict__ out, unsigned* __restrict__ status, unsigned long long stall_ns) {
     extern __shared__ unsigned char wt_raw[];
     unsigned char* sm = reinterpret_cast<unsigned char*>(
         (reinterpret_cast<uintptr_t>(wt_raw) + 1023) & ~static_cast<uintptr_t>(1023));
     __shared__ __align__(8) uint64_t s_fa[kWtStages], s_fb[kWtStages], s_em[kWtStages];
-    __shared__ __align__(8) uint64_t s_accf, s_acce, s_fin;
+    __shared__ __align__(8) uint64_t s_accf, s_acce, s_fin, s_never;  // s_never: test hook only
     __shared__ uint32_t s_tmem;
     __shared__ volatile int s_abort;
 
@@ -173,6 +173,7 @@ __global__ void __launch_bounds__(kWtThreads, 1)
         tc::mbar_init(&s_accf, 1);
         tc::mbar_init(&s_acce, 8);
         tc::mbar_init(&s_fin, 1);
+        tc::mbar_init(&s_never, 1);
         s_abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -223,6 +224,12 @@ __global__ void __launch_bounds__(kWtThreads, 1)
                 if (ok) ++gc;
             }
             constexpr uint32_t id = tc::idesc(0, 128, 256, false, false);
+            // test hook: a first wait on a barrier nothing completes, with a
+            // short limit, takes the timeout path without a fault
+            if (ok && stall_ns && !tc::mbar_wait(&s_never, 0u, stall_ns)) {
+                s_abort = 1;
+                ok = false;
+            }
             for (int q = 0; q < nq && ok; ++q) {
                 if (q > 0) {
                     ok = wait(&s_acce, (uint32_t)((q - 1) & 1));
@@ -386,7 +393,7 @@ size_t warp_tc_split_bytes(int nx, int ny) {
 }
 
 cudaError_t launch_warp_sum_tc(const float2* F, const float4* ph, int nx, int ny, void* hs, unsigned* misc,
-                               double* out, cudaStream_t st) {
+                               double* out, cudaStream_t st, unsigned long long stall_ns) {
     const int nq = (nx + 127) / 128, nkc = (ny / 2 + 1 + 15) / 16;
     const long npx = (long)nx * ny;
     cudaError_t e = cudaMemsetAsync(misc, 0, 2 * sizeof(unsigned), st);
@@ -400,7 +407,8 @@ cudaError_t launch_warp_sum_tc(const float2* F, const float4* ph, int nx, int ny
     e = cudaFuncSetAttribute(k_wt_sum, cudaFuncAttributeMaxDynamicSharedMemorySize, kWtSmem);
     if (e != cudaSuccess) return e;
     k_wt_sum<<<(unsigned)((npx + kWtPx - 1) / kWtPx), kWtThreads, kWtSmem, st>>>(
-        reinterpret_cast<const unsigned char*>(hs), ph, F, misc, nx, ny, nq, nkc, 1.0 / (double)npx, out, misc + 1);
+        reinterpret_cast<const unsigned char*>(hs), ph, F, misc, nx, ny, nq, nkc, 1.0 / (double)npx, out, misc + 1,
+        stall_ns);
     return cudaGetLastError();
 }
 

@@ -114,6 +114,27 @@ def test_warp_sum_forms(shape, form, monkeypatch):
         assert close(got, ref, np.abs(img).max(), REL_WARP)
 
 
+def test_warp_sum_wait_timeout_reports_and_context_survives(monkeypatch):
+    """Failure detection without a GPU fault: the test hook makes the warp
+    sum's MMA thread wait first on a barrier that nothing completes, with a
+    1 ms limit; the CTA aborts every role's waits, drains its own copies,
+    frees its TMEM and returns, the call reports FLCT_ERR_TIMEOUT, and the
+    same context then computes the warp correctly."""
+    from pyflct_gb300 import _lib, synth
+    from pyflct_gb300.flct import FlctError, warp_frac2d
+    monkeypatch.delenv("FLCT_WARP_SUM", raising=False)
+    rng = np.random.default_rng(33)
+    img = synth.kfield((64, 48), rng)
+    dfast, dslow = synth.smooth_shift(img.shape, rng, rms=1.0)
+    monkeypatch.setenv("FLCT_TEST_WARP_STALL_NS", "1000000")
+    with pytest.raises(FlctError) as e:
+        warp_frac2d(img, dfast, dslow)
+    assert e.value.code == _lib.ERR_TIMEOUT
+    monkeypatch.delenv("FLCT_TEST_WARP_STALL_NS")
+    got = warp_frac2d(img, dfast, dslow)
+    assert close(got, po.warp_frac2d(img, dfast, dslow), np.abs(img).max(), REL_WARP)
+
+
 def test_warp_dispatch_and_constant_field():
     from pyflct_gb300.flct import FlctError, warp
     rng = np.random.default_rng(4)
